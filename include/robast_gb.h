@@ -1,0 +1,369 @@
+/*
+ * robast_gb.h -- C ABI of the GB300 non-sequential ray tracer.
+ *
+ * This is the drop-in boundary for ROBAST's hot path
+ *   AOpticsManager::TraceNonSequential(ARayArray&)   (src/AOpticsManager.cxx:523-587)
+ *   AOpticsManager::TraceNonSequential(TObjArray*)   (src/AOpticsManager.cxx:335-520)
+ *   AOpticsManager::TraceNonSequential(ARay&)        (src/AOpticsManager.cxx:327-332)
+ * declared at include/AOpticsManager.h:92-100.
+ *
+ * A caller (the C++ facade in robast_gb.hpp, the Python facade in the
+ * robast_gb300 package, or a ROOT-side binding inside AOpticsManager) describes
+ * the TGeo volume tree once as plain arrays (rbg_scene_desc), the library
+ * flattens it into physical nodes with composed transforms, bounding boxes and
+ * per-mother BVHs (rbg_scene), and rbg_trace() runs the whole per-ray state
+ * machine on the GPU.  No torch types, no C++ types: plain pointers and sizes.
+ *
+ * Units follow ROBAST: length in cm (include/AOpticsManager.h:59-65), time in
+ * s, wavelength in cm (400 nm = 4e-5), angles in rad unless a field says deg.
+ */
+#ifndef ROBAST_GB_H
+#define ROBAST_GB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RBG_ABI_VERSION 1
+
+/* ---- status codes (every entry point returns one) --------------------- */
+enum {
+  RBG_OK = 0,
+  RBG_ERR_ARG = 1,         /* null pointer, negative size, bad option */
+  RBG_ERR_SCENE = 2,       /* inconsistent scene description */
+  RBG_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  RBG_ERR_NAN = 4,         /* a ray had a NaN/zero direction or NaN origin */
+  RBG_ERR_CAP = 5,         /* a bounded device loop hit its iteration cap */
+  RBG_ERR_UNSUPPORTED = 6, /* feature outside this build (e.g. AGeo shape in CSG) */
+  RBG_ERR_NOMEM = 7,       /* allocation failed */
+  RBG_ERR_NODEVICE = 8     /* no CUDA device visible */
+};
+
+/* ---- per-ray fate: same values and order as ARay's private enum
+ *      {kRun, kStop, kExit, kFocus, kSuspend, kAbsorb} (include/ARay.h:26) */
+enum {
+  RBG_RUN = 0,
+  RBG_STOP = 1,
+  RBG_EXIT = 2,
+  RBG_FOCUS = 3,
+  RBG_SUSPEND = 4,
+  RBG_ABSORB = 5
+};
+
+/* ---- component kind = the C++ class of the TGeoVolume that the reference
+ *      tests with IsA() (include/AOpticsManager.h:45-53,76-90) -------------- */
+enum {
+  RBG_KIND_LENS = 0,   /* ALens            */
+  RBG_KIND_OBS = 1,    /* AObscuration     */
+  RBG_KIND_MIRROR = 2, /* AMirror          */
+  RBG_KIND_FOCUS = 3,  /* AFocalSurface    */
+  RBG_KIND_OPT = 4,    /* AOpticalComponent */
+  RBG_KIND_OTHER = 5   /* any other TGeoVolume */
+};
+
+/* ---- shapes ------------------------------------------------------------ */
+enum {
+  RBG_SHAPE_BOX = 1,            /* TGeoBBox                     */
+  RBG_SHAPE_TUBE = 2,           /* TGeoTube / TGeoTubeSeg       */
+  RBG_SHAPE_SPHERE = 3,         /* TGeoSphere                   */
+  RBG_SHAPE_PARABOLOID = 4,     /* TGeoParaboloid               */
+  RBG_SHAPE_PGON = 5,           /* TGeoPgon                     */
+  RBG_SHAPE_PCON = 6,           /* TGeoPcon / TGeoCone(Seg)     */
+  RBG_SHAPE_ASPHERIC_DISK = 7,  /* AGeoAsphericDisk             */
+  RBG_SHAPE_WINSTON_POLY = 8,   /* AGeoWinstonConePoly          */
+  RBG_SHAPE_COMPOSITE = 9       /* TGeoCompositeShape node      */
+};
+enum { RBG_OP_UNION = 0, RBG_OP_INTERSECTION = 1, RBG_OP_SUBTRACTION = 2 };
+
+/*
+ * Shape parameters, in rbg_scene_desc.params starting at param_offset.
+ * "User" layout (what a caller passes; mirrors each constructor):
+ *   BOX            dx dy dz ox oy oz                    (half lengths, origin)
+ *   TUBE           rmin rmax dz phi1 phi2               (deg; phi2-phi1>=360: full)
+ *   SPHERE         rmin rmax theta1 theta2 phi1 phi2    (deg)
+ *   PARABOLOID     rlo rhi dz
+ *   PGON           phi1 dphi nedges nz  z[nz] rmin[nz] rmax[nz]   (deg; r = apothem)
+ *   PCON           phi1 dphi nz  z[nz] rmin[nz] rmax[nz]           (deg)
+ *   ASPHERIC_DISK  z1 curve1 z2 curve2 rmax rmin conic1 conic2 npol1 npol2
+ *                  steps repeat  k1[npol1] k2[npol2]
+ *   WINSTON_POLY   r1 r2 n
+ *   COMPOSITE      (no params; op/left/right/left_matrix/right_matrix fields)
+ * The flattened scene (rbg_flat_scene) holds a canonical layout that adds
+ * derived quantities; it is documented in robast_gb300/csrc/scene_layout.h.
+ */
+typedef struct {
+  int32_t type;
+  int32_t param_offset;
+  int32_t n_params;
+  int32_t op;           /* composite only */
+  int32_t left, right;  /* composite only: operand shape ids */
+  int32_t left_matrix;  /* composite only: matrix id or -1 (identity) */
+  int32_t right_matrix;
+} rbg_shape_desc;
+
+/* Tabulated functions (TGraph::Eval; TH2::Interpolate on a rectilinear grid).
+ * 1D: params x[nx], y[nx].  2D: params x[nx], y[ny], z[nx*ny] with
+ * z[ix*ny+iy]. */
+enum { RBG_TABLE_1D = 1, RBG_TABLE_2D = 2 };
+typedef struct {
+  int32_t kind;
+  int32_t nx, ny;
+  int32_t param_offset;
+} rbg_table_desc;
+
+/* Refractive index models (include/ARefractiveIndex.h:25-68,
+ * src/ASellmeierFormula.cxx:46-54, src/ACauchyFormula.cxx,
+ * src/ASchottFormula.cxx, src/AMixedRefractiveIndex.cxx). k always comes from
+ * k_table (-1: k = 0).  TABLE with n_table = -1 gives n = 1. */
+enum {
+  RBG_INDEX_TABLE = 1,
+  RBG_INDEX_SELLMEIER = 2, /* coef: B1 B2 B3 C1 C2 C3 (um^2)          */
+  RBG_INDEX_CAUCHY = 3,    /* coef: A B C  n = A + B/l^2 + C/l^4 (um) */
+  RBG_INDEX_SCHOTT = 4,    /* coef: A0..A5                             */
+  RBG_INDEX_MIXED = 5      /* mix_a, mix_b index ids, coef[0] = fraction of a */
+};
+typedef struct {
+  int32_t kind;
+  int32_t n_table, k_table;
+  int32_t mix_a, mix_b;
+  double coef[6];
+} rbg_index_desc;
+
+/* AMultilayer: layers[layer_offset .. layer_offset+n_layers), first = top
+ * (incident) medium, last = bottom (substrate); their thickness is ignored
+ * (semi-infinite).  Coherent TMM only on the per-ray path. */
+typedef struct {
+  int32_t index;      /* refractive index id */
+  int32_t coherent;
+  double thickness;   /* cm */
+} rbg_layer_desc;
+typedef struct {
+  int32_t layer_offset;
+  int32_t n_layers;
+} rbg_multilayer_desc;
+
+/* ABorderSurfaceCondition(component1, component2)
+ * (include/ABorderSurfaceCondition.h:24-45).  component2 = -1 is a null
+ * component (outside of the top volume). */
+typedef struct {
+  int32_t component1, component2;  /* volume ids */
+  double sigma;                    /* Gaussian roughness (rad) */
+  int32_t multilayer;              /* multilayer id or -1 */
+  int32_t lambertian;
+} rbg_border_desc;
+
+/* A logical volume: TGeoVolume subclass + its optical properties. */
+typedef struct {
+  int32_t shape;
+  int32_t kind;            /* RBG_KIND_* */
+  double reflectance;      /* AMirror constant reflectance (default 1.0) */
+  int32_t refl_table;      /* AMirror table: 1D in lambda or 2D in (lambda, angle); -1 none */
+  int32_t index;           /* ALens refractive index id; -1: n = 1, k = 0 */
+  int32_t qe_lambda_table; /* AFocalSurface QE(lambda); -1 none (QE = 1) */
+  int32_t qe_angle_table;  /* AFocalSurface QE(angle);  -1 none */
+} rbg_volume_desc;
+
+/* TGeoVolume::AddNode / AddNodeOverlap */
+typedef struct {
+  int32_t mother;    /* volume id */
+  int32_t daughter;  /* volume id */
+  int32_t matrix;    /* matrix id (local -> mother) or -1 for identity */
+  int32_t copy_no;
+  int32_t overlap;
+} rbg_placement_desc;
+
+/* Scene description.  Matrices are 12 doubles each: a row-major 3x3 rotation
+ * R followed by a translation t, master = R * local + t (TGeoMatrix
+ * LocalToMaster convention). */
+typedef struct {
+  int32_t n_shapes;        const rbg_shape_desc* shapes;
+  int32_t n_matrices;      const double* matrices;
+  int32_t n_volumes;       const rbg_volume_desc* volumes;
+  int32_t n_placements;    const rbg_placement_desc* placements;
+  int32_t top_volume;
+  int32_t n_tables;        const rbg_table_desc* tables;
+  int32_t n_indices;       const rbg_index_desc* indices;
+  int32_t n_layers;        const rbg_layer_desc* layers;
+  int32_t n_multilayers;   const rbg_multilayer_desc* multilayers;
+  int32_t n_borders;       const rbg_border_desc* borders;
+  int64_t n_params;        const double* params;
+} rbg_scene_desc;
+
+/* ---- flattened scene (host view; what both the GPU tables and any CPU
+ *      checker read) ------------------------------------------------------- */
+typedef struct {
+  int32_t parent;        /* physical node id of the mother; -1 for the top */
+  int32_t volume;        /* logical volume id */
+  int32_t shape;         /* = volumes[volume].shape, cached */
+  int32_t kind;          /* = volumes[volume].kind, cached */
+  int32_t child_begin;   /* into rbg_flat_scene.children */
+  int32_t child_count;
+  int32_t bvh_root;      /* into rbg_flat_scene.bvh, -1: scan children */
+  int32_t depth;
+  double m[12];          /* local -> master (global) */
+  double lo[3], hi[3];   /* conservative master-frame bounding box */
+} rbg_node;
+
+/* Binary BVH over the children of one mother.  Leaves hold a range of
+ * rbg_flat_scene.bvh_items (physical node ids).  Boxes are rounded outward
+ * to float. */
+typedef struct {
+  float lo[3], hi[3];
+  int32_t left;        /* internal: child index; leaf: -1 */
+  int32_t right;       /* internal: child index; leaf: item count */
+  int32_t item_begin;  /* leaf: first item */
+  int32_t pad;
+} rbg_bvh_node;
+
+typedef struct {
+  int32_t n_nodes;      const rbg_node* nodes;
+  int32_t n_children;   const int32_t* children;
+  int32_t n_bvh;        const rbg_bvh_node* bvh;
+  int32_t n_bvh_items;  const int32_t* bvh_items;
+  /* canonical copies of the description tables */
+  int32_t n_shapes;     const rbg_shape_desc* shapes;
+  int32_t n_volumes;    const rbg_volume_desc* volumes;
+  int32_t n_tables;     const rbg_table_desc* tables;
+  int32_t n_indices;    const rbg_index_desc* indices;
+  int32_t n_layers;     const rbg_layer_desc* layers;
+  int32_t n_multilayers; const rbg_multilayer_desc* multilayers;
+  int32_t n_borders;    const rbg_border_desc* borders;
+  int64_t n_params;     const double* params;   /* canonical layout */
+  int32_t top_node;     /* always 0 */
+} rbg_flat_scene;
+
+typedef struct rbg_scene rbg_scene;
+
+/* ---- rays ------------------------------------------------------------- */
+/* Input rays, structure of arrays (ARay: last point x,y,z,t, direction,
+ * lambda; src/ARay.cxx:28-36).  Directions are normalised on entry exactly
+ * as ARay::SetDirection does (src/ARay.cxx:210-223). */
+typedef struct {
+  int64_t n;
+  const double *x, *y, *z, *t;
+  const double *dx, *dy, *dz;
+  const double* lambda;
+} rbg_rays;
+
+/* Output, structure of arrays.  Any pointer may be NULL (not written).
+ * npoints = ARay::GetNpoints() (the start point counts as one);
+ * last_node = physical node id of the last ARay::AddNode (-1: a null node,
+ * i.e. outside the top volume; -2: no node was ever added).
+ * Optional history: hist_cap points per ray, hist_xyzt[(i*hist_cap+j)*4+k],
+ * hist_node[i*hist_cap+j]; points past hist_cap are dropped. */
+typedef struct {
+  uint8_t* status;
+  int32_t* npoints;
+  int32_t* last_node;
+  double *x, *y, *z, *t;
+  double *dx, *dy, *dz;
+  int32_t hist_cap;
+  double* hist_xyzt;
+  int32_t* hist_node;
+} rbg_result;
+
+/* Trace options.  limit and disable_fresnel are AOpticsManager::SetLimit
+ * (src/AOpticsManager.cxx:590-594, default 100) and
+ * DisableFresnelReflection (include/AOpticsManager.h:73-75). */
+enum {
+  RBG_PREC_FP64 = 0,   /* plain FP64, one thread per ray */
+  RBG_PREC_MIXED = 1   /* mixed precision wavefront tracer */
+};
+typedef struct {
+  int32_t limit;
+  int32_t disable_fresnel;
+  uint64_t seed;          /* Philox key: every random draw is a function of
+                             (seed, ray id, draw number) */
+  uint64_t ray_id_offset; /* ray id of element 0 (for sharded/batched calls) */
+  int32_t precision;      /* RBG_PREC_* */
+  int32_t block_size;     /* 0: library default */
+} rbg_trace_opts;
+
+/* ---- entry points ------------------------------------------------------ */
+int rbg_abi_version(void);
+const char* rbg_status_string(int status);
+void rbg_trace_opts_default(rbg_trace_opts* opts);
+
+/* Flatten a description (host only, no device work).  Replaces the scene
+ * construction + TGeoManager::CloseGeometry() of the reference
+ * (e.g. tutorials/SimpleParabolicTelescope.C:22-83). */
+int rbg_scene_create(const rbg_scene_desc* desc, rbg_scene** out);
+void rbg_scene_destroy(rbg_scene* scene);
+int rbg_scene_flat(const rbg_scene* scene, rbg_flat_scene* out);
+/* Copy the flattened tables to the current CUDA device (done lazily by
+ * rbg_trace when needed). */
+int rbg_scene_upload(rbg_scene* scene);
+
+/* AOpticsManager::TraceNonSequential over n rays whose buffers live in
+ * DEVICE memory; asynchronous on `stream` (a cudaStream_t, NULL = legacy
+ * default).  The per-ray fates, points and directions land in `out`. */
+int rbg_trace(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
+              const rbg_trace_opts* opts, void* stream);
+
+/* Same, with HOST buffers: copies the rays in, traces, copies the results
+ * out and synchronises (the call a ROOT-side AOpticsManager binding makes,
+ * src/AOpticsManager.cxx:523). */
+int rbg_trace_host(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
+                   const rbg_trace_opts* opts);
+
+/* Number of kernel launches the last rbg_trace on this scene issued, and the
+ * device time of its dominant kernel in ms measured with events on the
+ * launching stream (NaN when not measured). */
+int rbg_last_launch_count(const rbg_scene* scene);
+
+/* ---- spot reductions ---------------------------------------------------- */
+/* Focused-ray statistics per group (e.g. per field angle / variant) on
+ * DEVICE arrays: sums[g*6 + k] accumulates (count, sum x, sum y, sum x^2,
+ * sum y^2, sum t) over rays with status == RBG_FOCUS and group[i] == g
+ * (group may be NULL: single group).  Used for the RMS spot size and the
+ * effective area (tutorials/SchwarzschildCouder.C:133-161). */
+int rbg_focal_moments(int64_t n, const uint8_t* status, const double* x,
+                      const double* y, const double* t, const int32_t* group,
+                      int32_t n_groups, double* sums, void* stream);
+
+/* 2D histogram of focused rays on DEVICE arrays: counts[ix*ny+iy]
+ * (TH2D::Fill semantics, under/overflow dropped). */
+int rbg_focal_histogram(int64_t n, const uint8_t* status, const double* x,
+                        const double* y, int32_t nx, double xlo, double xhi,
+                        int32_t ny, double ylo, double yhi, double* counts,
+                        void* stream);
+
+/* AGeoUtil::ContainmentRadius (src/AGeoUtil.cxx:198-308) on a DEVICE
+ * histogram counts[ix*ny+iy]; r, x, y are host outputs.  The O(nbins^2)
+ * SumInRadius probes (src/AGeoUtil.cxx:18-42) run as device reductions. */
+int rbg_containment_radius(const double* counts, int32_t nx, double xlo,
+                           double xhi, int32_t ny, double ylo, double yhi,
+                           double fraction, double* r, double* x, double* y,
+                           void* stream);
+
+/* ---- ray sources -------------------------------------------------------- */
+/* ARayShooter generators (include/ARayShooter.h:25-51,
+ * src/ARayShooter.cxx:122-459) writing HOST arrays: the x, y, z, t, dx, dy,
+ * dz and lambda arrays of `out` are written (their const is cast away) and
+ * out->n is the capacity on entry, the number of rays written on return.
+ * rot: row-major 3x3 (TGeoRotation, NULL = identity), tr: 3 (NULL = 0),
+ * dir: local direction (NULL = (0, 0, 1)).  Draws are Philox(seed, first_id
+ * + i) on a stream separate from the tracer's.
+ * params:  CIRCLE rmax nr nphi | RANDOM_CIRCLE rmax | RANDOM_CONE r d |
+ *          RANDOM_RECTANGLE dx dy | RANDOM_SPHERE - |
+ *          RANDOM_SPHERICAL_CONE theta(deg) | RECTANGLE dx dy nx ny */
+enum {
+  RBG_SHOOT_CIRCLE = 1,
+  RBG_SHOOT_RANDOM_CIRCLE = 2,
+  RBG_SHOOT_RANDOM_CONE = 3,
+  RBG_SHOOT_RANDOM_RECTANGLE = 4,
+  RBG_SHOOT_RANDOM_SPHERE = 5,
+  RBG_SHOOT_RANDOM_SPHERICAL_CONE = 6,
+  RBG_SHOOT_RECTANGLE = 7
+};
+int rbg_shoot(int32_t kind, const double* params, int64_t n, const double* rot,
+              const double* tr, const double* dir, uint64_t seed,
+              uint64_t first_id, double lambda, rbg_rays* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ROBAST_GB_H */

@@ -1,0 +1,559 @@
+// capi.cu -- C ABI of the tracer: device upload of a flattened scene, the
+// plain FP64 trace kernel, host-buffer tracing and focal-plane reductions.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "scene_internal.h"
+#include "tracer.cuh"
+
+struct rbg_device_scene {
+  rbg::DevScene view;
+  std::vector<void*> allocations;
+  unsigned* err_flags;  // device word of error bits
+};
+
+namespace rbg {
+
+namespace {
+
+template <typename T>
+int upload(std::vector<void*>& allocs, const std::vector<T>& v, const T** out) {
+  *out = nullptr;
+  if (v.empty()) return RBG_OK;
+  void* p = nullptr;
+  if (cudaMalloc(&p, v.size() * sizeof(T)) != cudaSuccess) return RBG_ERR_NOMEM;
+  allocs.push_back(p);
+  if (cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) return RBG_ERR_CUDA;
+  *out = static_cast<const T*>(p);
+  return RBG_OK;
+}
+
+int current_device(int* dev) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return RBG_ERR_NODEVICE;
+  if (cudaGetDevice(dev) != cudaSuccess) return RBG_ERR_CUDA;
+  return RBG_OK;
+}
+
+}  // namespace
+
+void release_device(rbg_scene* s) {
+  if (!s || !s->dev) return;
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (s->dev_id >= 0) cudaSetDevice(s->dev_id);
+  for (void* p : s->dev->allocations) cudaFree(p);
+  if (s->workspace) cudaFree(s->workspace);
+  if (prev >= 0) cudaSetDevice(prev);
+  delete s->dev;
+  s->dev = nullptr;
+  s->workspace = nullptr;
+  s->workspace_bytes = 0;
+  s->dev_id = -1;
+}
+
+int ensure_device(rbg_scene* s) {
+  int dev;
+  int rc = current_device(&dev);
+  if (rc != RBG_OK) return rc;
+  if (s->dev && s->dev_id == dev) return RBG_OK;
+  release_device(s);
+  auto* d = new rbg_device_scene();
+  d->err_flags = nullptr;
+  DevScene& v = d->view;
+  std::memset(&v, 0, sizeof(v));
+  if ((rc = upload(d->allocations, s->nodes, &v.nodes)) ||
+      (rc = upload(d->allocations, s->children, &v.children)) ||
+      (rc = upload(d->allocations, s->bvh, &v.bvh)) ||
+      (rc = upload(d->allocations, s->bvh_items, &v.bvh_items)) ||
+      (rc = upload(d->allocations, s->shapes, &v.shapes)) ||
+      (rc = upload(d->allocations, s->volumes, &v.volumes)) ||
+      (rc = upload(d->allocations, s->tables, &v.tables)) ||
+      (rc = upload(d->allocations, s->indices, &v.indices)) ||
+      (rc = upload(d->allocations, s->layers, &v.layers)) ||
+      (rc = upload(d->allocations, s->multilayers, &v.multilayers)) ||
+      (rc = upload(d->allocations, s->borders, &v.borders)) ||
+      (rc = upload(d->allocations, s->params, &v.params))) {
+    for (void* p : d->allocations) cudaFree(p);
+    delete d;
+    return rc;
+  }
+  void* ef = nullptr;
+  if (cudaMalloc(&ef, sizeof(unsigned)) != cudaSuccess) {
+    for (void* p : d->allocations) cudaFree(p);
+    delete d;
+    return RBG_ERR_NOMEM;
+  }
+  d->allocations.push_back(ef);
+  d->err_flags = static_cast<unsigned*>(ef);
+  v.n_nodes = (int32_t)s->nodes.size();
+  v.n_borders = (int32_t)s->borders.size();
+  v.n_multilayers = (int32_t)s->multilayers.size();
+  v.n_tables = (int32_t)s->tables.size();
+  s->dev = d;
+  s->dev_id = dev;
+  return RBG_OK;
+}
+
+// ---------------------------------------------------------------------
+// plain FP64 kernel: one thread per ray, whole path in registers
+// ---------------------------------------------------------------------
+struct KernelRays {
+  const double *x, *y, *z, *t, *dx, *dy, *dz, *lambda;
+};
+struct KernelOut {
+  uint8_t* status;
+  int32_t *npoints, *last_node;
+  double *x, *y, *z, *t, *dx, *dy, *dz;
+  int32_t hist_cap;
+  double* hist_xyzt;
+  int32_t* hist_node;
+};
+
+__global__ void __launch_bounds__(128) trace_fp64_kernel(DevScene S, KernelRays in, KernelOut out, int64_t n,
+                                                         int limit, int disable_fresnel, uint64_t seed,
+                                                         uint64_t id_offset, unsigned* err_flags) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    Ray r;
+    r.x = mk(in.x[i], in.y[i], in.z[i]);
+    r.t = in.t ? in.t[i] : 0.0;
+    r.lambda = in.lambda[i];
+    d3 dd = mk(in.dx[i], in.dy[i], in.dz[i]);
+    r.status = RBG_RUN;
+    r.npoints = 0;
+    r.last_node = -2;
+    r.err = 0;
+    r.hist_cap = out.hist_cap;
+    r.hist_xyzt = out.hist_cap ? out.hist_xyzt + (size_t)i * out.hist_cap * 4 : nullptr;
+    r.hist_node = out.hist_cap ? out.hist_node + (size_t)i * out.hist_cap : nullptr;
+    r.rng.init(seed, id_offset + (uint64_t)i, 0);
+    add_point(r, r.x, r.t);
+    double mag = sqrt(dot(dd, dd));
+    bool bad = !(mag > 0) || !isfinite(mag) || !isfinite(r.x.x) || !isfinite(r.x.y) || !isfinite(r.x.z);
+    if (bad) {
+      r.d = dd;
+      r.err |= ERR_BIT_NAN;
+    } else {
+      set_direction(r, dd);
+      trace_ray(S, r, limit, disable_fresnel != 0);
+    }
+    if (r.err) atomicOr(err_flags, r.err);
+    if (out.status) out.status[i] = (uint8_t)r.status;
+    if (out.npoints) out.npoints[i] = r.npoints;
+    if (out.last_node) out.last_node[i] = r.last_node;
+    if (out.x) out.x[i] = r.x.x;
+    if (out.y) out.y[i] = r.x.y;
+    if (out.z) out.z[i] = r.x.z;
+    if (out.t) out.t[i] = r.t;
+    if (out.dx) out.dx[i] = r.d.x;
+    if (out.dy) out.dy[i] = r.d.y;
+    if (out.dz) out.dz[i] = r.d.z;
+  }
+}
+
+int sm_count() {
+  static int cached = 0;
+  if (cached == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev);
+    if (cached <= 0) cached = 1;
+  }
+  return cached;
+}
+
+int stack_ready() {
+  static int done = 0;
+  if (!done) {
+    // the CSG walk and the rejection loops recurse/branch deeply: give each
+    // thread enough local stack for composite trees of depth <= 8
+    if (cudaDeviceSetLimit(cudaLimitStackSize, 4096) != cudaSuccess) return RBG_ERR_CUDA;
+    done = 1;
+  }
+  return RBG_OK;
+}
+
+int read_errors(rbg_scene* s, cudaStream_t st, unsigned* bits) {
+  if (cudaMemcpyAsync(bits, s->dev->err_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return RBG_ERR_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return RBG_ERR_CUDA;
+  return RBG_OK;
+}
+
+}  // namespace rbg
+
+using namespace rbg;
+
+extern "C" int rbg_scene_upload(rbg_scene* s) {
+  if (!s) return RBG_ERR_ARG;
+  return ensure_device(s);
+}
+
+extern "C" int rbg_last_launch_count(const rbg_scene* s) { return s ? s->last_launches : -1; }
+
+// forward declaration of the mixed-precision entry (trace_mixed.cu)
+namespace rbg {
+int launch_mixed(rbg_scene* s, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o,
+                 cudaStream_t st, int* launches);
+}
+
+extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, const rbg_trace_opts* opts,
+                         void* stream) {
+  if (!s || !in || !out || !opts) return RBG_ERR_ARG;
+  if (in->n < 0 || opts->limit <= 0) return RBG_ERR_ARG;
+  if (in->n > 0 && (!in->x || !in->y || !in->z || !in->dx || !in->dy || !in->dz || !in->lambda)) return RBG_ERR_ARG;
+  if (out->hist_cap < 0 || (out->hist_cap > 0 && (!out->hist_xyzt || !out->hist_node))) return RBG_ERR_ARG;
+  int rc = ensure_device(s);
+  if (rc) return rc;
+  if ((rc = stack_ready())) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  s->last_launches = 0;
+  if (in->n == 0) return RBG_OK;
+  if (cudaMemsetAsync(s->dev->err_flags, 0, sizeof(unsigned), st) != cudaSuccess) return RBG_ERR_CUDA;
+  KernelRays kr{in->x, in->y, in->z, in->t, in->dx, in->dy, in->dz, in->lambda};
+  KernelOut ko{out->status, out->npoints, out->last_node, out->x, out->y, out->z, out->t,
+               out->dx, out->dy, out->dz, out->hist_cap, out->hist_xyzt, out->hist_node};
+  if (opts->precision == RBG_PREC_MIXED && out->hist_cap == 0) {
+    int launches = 0;
+    rc = launch_mixed(s, kr, ko, in->n, *opts, st, &launches);
+    if (rc) return rc;
+    s->last_launches = launches;
+  } else {
+    int block = opts->block_size > 0 ? opts->block_size : 128;
+    if (block > 128) block = 128;
+    int64_t blocks64 = (in->n + block - 1) / block;
+    int64_t cap = (int64_t)sm_count() * 64;
+    int blocks = (int)(blocks64 < cap ? blocks64 : cap);
+    trace_fp64_kernel<<<blocks, block, 0, st>>>(s->dev->view, kr, ko, in->n, opts->limit, opts->disable_fresnel,
+                                                opts->seed, opts->ray_id_offset, s->dev->err_flags);
+    if (cudaGetLastError() != cudaSuccess) return RBG_ERR_CUDA;
+    s->last_launches = 1;
+  }
+  unsigned bits = 0;
+  if ((rc = read_errors(s, st, &bits))) return rc;
+  if (bits & ERR_BIT_NAN) return RBG_ERR_NAN;
+  if (bits & ERR_BIT_CAP) return RBG_ERR_CAP;
+  return RBG_OK;
+}
+
+namespace {
+struct DevBuf {
+  void* p = nullptr;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+};
+}  // namespace
+
+extern "C" int rbg_trace_host(rbg_scene* s, const rbg_rays* in, rbg_result* out, const rbg_trace_opts* opts) {
+  if (!s || !in || !out || !opts || in->n < 0) return RBG_ERR_ARG;
+  if (in->n > 0 && (!in->x || !in->y || !in->z || !in->dx || !in->dy || !in->dz || !in->lambda)) return RBG_ERR_ARG;
+  int rc = ensure_device(s);
+  if (rc) return rc;
+  const int64_t n = in->n;
+  if (n == 0) return RBG_OK;
+  // one device block holding every input and output array
+  const size_t d8 = (size_t)n * sizeof(double);
+  const size_t hist = out->hist_cap > 0 ? (size_t)n * out->hist_cap : 0;
+  size_t bytes = 8 * d8 + 7 * d8 + (size_t)n * (sizeof(int32_t) * 2 + 8) + hist * (4 * sizeof(double) + sizeof(int32_t));
+  DevBuf buf;
+  if (cudaMalloc(&buf.p, bytes) != cudaSuccess) return RBG_ERR_NOMEM;
+  char* base = static_cast<char*>(buf.p);
+  double* din[8];
+  for (int k = 0; k < 8; ++k) din[k] = reinterpret_cast<double*>(base + k * d8);
+  double* dout[7];
+  for (int k = 0; k < 7; ++k) dout[k] = reinterpret_cast<double*>(base + (8 + k) * d8);
+  char* tail = base + 15 * d8;
+  int32_t* dnp = reinterpret_cast<int32_t*>(tail);
+  int32_t* dln = dnp + n;
+  uint8_t* dst = reinterpret_cast<uint8_t*>(dln + n);
+  char* htail = reinterpret_cast<char*>(dst) + ((n + 7) / 8) * 8;
+  double* dhist = hist ? reinterpret_cast<double*>(htail) : nullptr;
+  int32_t* dhnode = hist ? reinterpret_cast<int32_t*>(htail + hist * 4 * sizeof(double)) : nullptr;
+  const double* src[8] = {in->x, in->y, in->z, in->t, in->dx, in->dy, in->dz, in->lambda};
+  cudaStream_t st = 0;
+  for (int k = 0; k < 8; ++k) {
+    if (!src[k]) continue;
+    if (cudaMemcpyAsync(din[k], src[k], d8, cudaMemcpyHostToDevice, st) != cudaSuccess) return RBG_ERR_CUDA;
+  }
+  rbg_rays dr{n, din[0], din[1], din[2], in->t ? din[3] : nullptr, din[4], din[5], din[6], din[7]};
+  rbg_result dres{};
+  dres.status = out->status ? dst : nullptr;
+  dres.npoints = out->npoints ? dnp : nullptr;
+  dres.last_node = out->last_node ? dln : nullptr;
+  double* hout[7] = {out->x, out->y, out->z, out->t, out->dx, out->dy, out->dz};
+  double** dslots[7] = {&dres.x, &dres.y, &dres.z, &dres.t, &dres.dx, &dres.dy, &dres.dz};
+  for (int k = 0; k < 7; ++k) *dslots[k] = hout[k] ? dout[k] : nullptr;
+  dres.hist_cap = hist ? out->hist_cap : 0;
+  dres.hist_xyzt = dhist;
+  dres.hist_node = dhnode;
+  int trc = rbg_trace(s, &dr, &dres, opts, st);
+  if (trc != RBG_OK && trc != RBG_ERR_NAN && trc != RBG_ERR_CAP) return trc;
+  if (out->status && cudaMemcpyAsync(out->status, dst, n, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return RBG_ERR_CUDA;
+  if (out->npoints && cudaMemcpyAsync(out->npoints, dnp, n * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return RBG_ERR_CUDA;
+  if (out->last_node && cudaMemcpyAsync(out->last_node, dln, n * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return RBG_ERR_CUDA;
+  for (int k = 0; k < 7; ++k)
+    if (hout[k] && cudaMemcpyAsync(hout[k], dout[k], d8, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return RBG_ERR_CUDA;
+  if (hist) {
+    if (cudaMemcpyAsync(out->hist_xyzt, dhist, hist * 4 * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+        cudaSuccess)
+      return RBG_ERR_CUDA;
+    if (cudaMemcpyAsync(out->hist_node, dhnode, hist * sizeof(int32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return RBG_ERR_CUDA;
+  }
+  if (cudaStreamSynchronize(st) != cudaSuccess) return RBG_ERR_CUDA;
+  return trc;
+}
+
+// ---------------------------------------------------------------------
+// focal-plane reductions
+// ---------------------------------------------------------------------
+namespace rbg {
+
+__global__ void focal_moments_kernel(int64_t n, const uint8_t* status, const double* x, const double* y,
+                                     const double* t, const int32_t* group, int32_t n_groups, double* sums) {
+  // per-block shared accumulators for up to 64 groups, then one atomic
+  // pass; larger group counts go straight to global atomics
+  __shared__ double acc[64 * 6];
+  const bool shared = n_groups <= 64;
+  if (shared)
+    for (int k = threadIdx.x; k < n_groups * 6; k += blockDim.x) acc[k] = 0;
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (status[i] != RBG_FOCUS) continue;
+    int g = group ? group[i] : 0;
+    if (g < 0 || g >= n_groups) continue;
+    double v[6] = {1.0, x[i], y[i], x[i] * x[i], y[i] * y[i], t ? t[i] : 0.0};
+    double* dst = shared ? acc + g * 6 : sums + g * 6;
+    for (int k = 0; k < 6; ++k) atomicAdd(dst + k, v[k]);
+  }
+  __syncthreads();
+  if (shared)
+    for (int k = threadIdx.x; k < n_groups * 6; k += blockDim.x)
+      if (acc[k] != 0) atomicAdd(sums + k, acc[k]);
+}
+
+__global__ void focal_hist_kernel(int64_t n, const uint8_t* status, const double* x, const double* y, int32_t nx,
+                                  double xlo, double xhi, int32_t ny, double ylo, double yhi, double* counts) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (status[i] != RBG_FOCUS) continue;
+    double fx = (x[i] - xlo) / (xhi - xlo) * nx, fy = (y[i] - ylo) / (yhi - ylo) * ny;
+    if (!(fx >= 0) || !(fy >= 0) || fx >= nx || fy >= ny) continue;
+    atomicAdd(counts + (int64_t)fx * ny + (int64_t)fy, 1.0);
+  }
+}
+
+// SumInRadius (src/AGeoUtil.cxx:18-42) for a batch of probes
+__global__ void sum_in_radius_kernel(const double* counts, int32_t nx, double xlo, double xw, int32_t ny,
+                                     double ylo, double yw, const double* probes, int nprobe, double* sums) {
+  extern __shared__ double part[];
+  for (int p = 0; p < nprobe; ++p) part[p * blockDim.x + threadIdx.x] = 0;
+  int64_t nb = (int64_t)nx * ny;
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nb; b += (int64_t)gridDim.x * blockDim.x) {
+    double c = counts[b];
+    if (c <= 0) continue;
+    int ix = (int)(b / ny), iy = (int)(b % ny);
+    double cx = xlo + (ix + 0.5) * xw, cy = ylo + (iy + 0.5) * yw;
+    for (int p = 0; p < nprobe; ++p) {
+      double dx = cx - probes[3 * p], dy = cy - probes[3 * p + 1], r = probes[3 * p + 2];
+      if (dx * dx + dy * dy <= r * r) part[p * blockDim.x + threadIdx.x] += c;
+    }
+  }
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s)
+      for (int p = 0; p < nprobe; ++p) part[p * blockDim.x + threadIdx.x] += part[p * blockDim.x + threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int p = 0; p < nprobe; ++p) atomicAdd(sums + p, part[p * blockDim.x]);
+}
+
+}  // namespace rbg
+
+extern "C" int rbg_focal_moments(int64_t n, const uint8_t* status, const double* x, const double* y,
+                                 const double* t, const int32_t* group, int32_t n_groups, double* sums,
+                                 void* stream) {
+  if (n < 0 || n_groups <= 0 || !status || !x || !y || !sums) return RBG_ERR_ARG;
+  if (n == 0) return RBG_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 8);
+  focal_moments_kernel<<<blocks, 256, 0, st>>>(n, status, x, y, t, group, n_groups, sums);
+  return cudaGetLastError() == cudaSuccess ? RBG_OK : RBG_ERR_CUDA;
+}
+
+extern "C" int rbg_focal_histogram(int64_t n, const uint8_t* status, const double* x, const double* y, int32_t nx,
+                                   double xlo, double xhi, int32_t ny, double ylo, double yhi, double* counts,
+                                   void* stream) {
+  if (n < 0 || nx <= 0 || ny <= 0 || !(xhi > xlo) || !(yhi > ylo) || !status || !x || !y || !counts)
+    return RBG_ERR_ARG;
+  if (n == 0) return RBG_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 8);
+  focal_hist_kernel<<<blocks, 256, 0, st>>>(n, status, x, y, nx, xlo, xhi, ny, ylo, yhi, counts);
+  return cudaGetLastError() == cudaSuccess ? RBG_OK : RBG_ERR_CUDA;
+}
+
+namespace {
+struct ProbeBatch {
+  double* dprobe = nullptr;
+  double* dsum = nullptr;
+  ~ProbeBatch() {
+    if (dprobe) cudaFree(dprobe);
+    if (dsum) cudaFree(dsum);
+  }
+};
+}  // namespace
+
+// AGeoUtil::ContainmentRadius with device SumInRadius probes
+extern "C" int rbg_containment_radius(const double* counts, int32_t nx, double xlo, double xhi, int32_t ny,
+                                      double ylo, double yhi, double fraction, double* pr, double* px, double* py,
+                                      void* stream) {
+  if (!counts || nx <= 0 || ny <= 0 || !pr || !px || !py || !(xhi > xlo) || !(yhi > ylo)) return RBG_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const double xw = (xhi - xlo) / nx, yw = (yhi - ylo) / ny;
+  ProbeBatch pb;
+  const int kMaxProbe = 8;
+  if (cudaMalloc(&pb.dprobe, 3 * kMaxProbe * sizeof(double)) != cudaSuccess) return RBG_ERR_NOMEM;
+  if (cudaMalloc(&pb.dsum, kMaxProbe * sizeof(double)) != cudaSuccess) return RBG_ERR_NOMEM;
+  const int block = 256;
+  const int blocks = (int)std::min<int64_t>(((int64_t)nx * ny + block - 1) / block, (int64_t)sm_count() * 4);
+  int failed = 0;
+  auto probe = [&](int np, const double* xyr, double* out) {
+    if (failed) {
+      for (int i = 0; i < np; ++i) out[i] = 0;
+      return;
+    }
+    if (cudaMemcpyAsync(pb.dprobe, xyr, 3 * np * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemsetAsync(pb.dsum, 0, np * sizeof(double), st) != cudaSuccess) {
+      failed = 1;
+      return;
+    }
+    sum_in_radius_kernel<<<blocks, block, np * block * sizeof(double), st>>>(counts, nx, xlo, xw, ny, ylo, yw,
+                                                                             pb.dprobe, np, pb.dsum);
+    if (cudaMemcpyAsync(out, pb.dsum, np * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+      failed = 1;
+    }
+  };
+  auto sum_in_radius = [&](double x, double y, double r) {
+    double q[3] = {x, y, r}, o = 0;
+    probe(1, q, &o);
+    return o;
+  };
+  // moments from bin centres: r = 1 probe at "infinite" radius is not enough,
+  // so read the histogram moments with one pass of 5 probes-worth of sums
+  std::vector<double> hc((size_t)nx * ny);
+  if (cudaMemcpyAsync(hc.data(), counts, hc.size() * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return RBG_ERR_CUDA;
+  double sw = 0, sx = 0, sy = 0, sxx = 0, syy = 0;
+  for (int ix = 0; ix < nx; ++ix) {
+    double cx = xlo + (ix + 0.5) * xw;
+    for (int iy = 0; iy < ny; ++iy) {
+      double cy = ylo + (iy + 0.5) * yw, c = hc[(size_t)ix * ny + iy];
+      sw += c;
+      sx += c * cx;
+      sy += c * cy;
+      sxx += c * cx * cx;
+      syy += c * cy * cy;
+    }
+  }
+  double x = sw ? sx / sw : 0, y = sw ? sy / sw : 0;
+  double vx = sw ? sxx / sw - x * x : 0, vy = sw ? syy / sw - y * y : 0;
+  double sdx = vx > 0 ? std::sqrt(vx) : 0, sdy = vy > 0 ? std::sqrt(vy) : 0;
+  double r = std::sqrt(sdx * sdx + sdy * sdy) * 1.5;
+  double dr = 0.1 * r;
+  double sum_goal = sw * fraction;
+  int no_shift = 0, no_stable = 0;
+  for (int i = 0; i < 100 && no_shift < 30; i++) {
+    bool stable_r = false, stable_x = true, stable_y = true;
+    double sum0 = sum_in_radius(x, y, r);
+    double next_r = r;
+    if (sum0 < sum_goal) {
+      double sum1 = sum_in_radius(x, y, r + dr);
+      if (sum1 == sum0) {
+        dr *= 2.;
+        continue;
+      }
+      next_r = r + dr * (sum_goal - sum0) / (sum1 - sum0);
+    } else if (sum0 != sum_goal) {
+      double sum1 = sum_in_radius(x, y, r - dr);
+      if (sum1 == sum0) {
+        dr *= 2.;
+        continue;
+      }
+      next_r = r - dr * (sum0 - sum_goal) / (sum0 - sum1);
+    }
+    if (next_r < 0.) next_r = 0.5 * r;
+    if (next_r < 0.5 * r) next_r = 0.5 * r;
+    if (next_r > 2. * r) next_r = 2. * r;
+    stable_r = std::fabs(next_r - r) < 0.0001 * r;
+    r = next_r;
+    {
+      double sum1 = sum_in_radius(x, y, r);
+      dr *= sum0 != sum_goal ? std::fabs((sum1 - sum_goal) / (sum0 - sum_goal)) : 0.5;
+      if (dr > 0.5 * r) dr = 0.5 * r;
+      if (dr < 0.0005 * r) dr = 0.0005 * r;
+      no_shift++;
+      for (double dx = 0.25 * r; dx > 0.1 * dr; dx *= 0.25) {
+        double q[6] = {x + dx, y, r, x - dx, y, r}, o[2];
+        probe(2, q, o);
+        double sx1 = o[0], sx2 = o[1];
+        while (sx1 > sum1) {
+          no_shift = 0;
+          x += dx;
+          sx2 = sum1;
+          sum1 = sx1;
+          sx1 = sum_in_radius(x + dx, y, r);
+          stable_x = false;
+        }
+        while (sx2 > sum1) {
+          no_shift = 0;
+          x -= dx;
+          sx1 = sum1;
+          sum1 = sx2;
+          sx2 = sum_in_radius(x - dx, y, r);
+          stable_x = false;
+        }
+      }
+    }
+    for (double dy = 0.1 * r; dy > 0.1 * dr; dy *= 0.25) {
+      double q[9] = {x, y, r, x, y + dy, r, x, y - dy, r}, o[3];
+      probe(3, q, o);
+      double sum1 = o[0], sy1 = o[1], sy2 = o[2];
+      while (sy1 > sum1) {
+        no_shift = 0;
+        y += dy;
+        sy2 = sum1;
+        sum1 = sy1;
+        sy1 = sum_in_radius(x, y + dy, r);
+        stable_y = false;
+      }
+      while (sy2 > sum1) {
+        no_shift = 0;
+        y -= dy;
+        sy1 = sum1;
+        sum1 = sy2;
+        sy2 = sum_in_radius(x, y - dy, r);
+        stable_y = false;
+      }
+    }
+    if (stable_r && stable_x && stable_y) no_stable++;
+    else no_stable = 0;
+    if (no_stable >= 4) break;
+  }
+  if (failed) return RBG_ERR_CUDA;
+  *pr = r;
+  *px = x;
+  *py = y;
+  return RBG_OK;
+}

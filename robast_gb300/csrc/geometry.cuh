@@ -1,0 +1,821 @@
+// geometry.cuh -- device shape queries in a node's local frame.
+//
+// TGeo primitives (box, tube, sphere, paraboloid, pgon, pcon) and their CSG
+// composites are exact solids: every ray/surface root is collected with a
+// compact surface code, the roots are sorted, and each segment between two
+// roots is classified with the point-containment test.  The first root that
+// enters (leaves) the solid past t = 0 is DistFromOutside (DistFromInside).
+// The normal is recomputed only for that root.
+//
+// AGeoAsphericDisk and AGeoWinstonConePoly follow the reference's own
+// algorithms (src/AGeoAsphericDisk.cxx, src/AGeoWinstonCone2D.cxx,
+// src/AGeoWinstonConePoly.cxx), including their single-root Newton and
+// parabola solvers.
+#pragma once
+#include "device_scene.cuh"
+
+namespace rbg {
+
+constexpr double kBig = RBG_BIG;
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kD2R = kPi / 180.0;
+
+RBG_D const double* SP(const DevScene& S, int shape) { return S.params + S.shapes[shape].param_offset; }
+
+// --------------------------------------------------------------------
+// containment
+// --------------------------------------------------------------------
+RBG_D bool phi_in(double x, double y, double phi1, double dphi) {
+  if (dphi >= 360.0) return true;
+  double rel = atan2(y, x) / kD2R - phi1;
+  while (rel < 0) rel += 360.0;
+  while (rel >= 360.0) rel -= 360.0;
+  return rel <= dphi;
+}
+
+RBG_D bool pxcon_contains(const double* P, bool pg, d3 p) {
+  const int head = pg ? 4 : 3;
+  const int nz = (int)P[pg ? 3 : 2];
+  const double* Z = P + head;
+  const double* RMIN = Z + nz;
+  const double* RMAX = RMIN + nz;
+  if (p.z < Z[0] || p.z > Z[nz - 1]) return false;
+  if (!phi_in(p.x, p.y, P[0], P[1])) return false;
+  double rho;
+  if (pg) {
+    int ned = (int)P[2];
+    double sector = P[1] / ned;
+    double rel = atan2(p.y, p.x) / kD2R - P[0];
+    while (rel < 0) rel += 360.0;
+    while (rel >= 360.0) rel -= 360.0;
+    int e = (int)floor(rel / sector);
+    if (e >= ned) e = ned - 1;
+    double pe = (P[0] + (e + 0.5) * sector) * kD2R;
+    rho = p.x * cos(pe) + p.y * sin(pe);
+  } else {
+    rho = sqrt(p.x * p.x + p.y * p.y);
+  }
+  for (int k = 0; k < nz - 1; ++k) {
+    if (p.z < Z[k] || p.z > Z[k + 1]) continue;
+    double h = Z[k + 1] - Z[k];
+    double rmn, rmx;
+    if (h == 0) {
+      rmn = fmin(RMIN[k], RMIN[k + 1]);
+      rmx = fmax(RMAX[k], RMAX[k + 1]);
+    } else {
+      double f = (p.z - Z[k]) / h;
+      rmn = RMIN[k] + f * (RMIN[k + 1] - RMIN[k]);
+      rmx = RMAX[k] + f * (RMAX[k + 1] - RMAX[k]);
+    }
+    if (rho >= rmn && rho <= rmx) return true;
+  }
+  return false;
+}
+
+RBG_D bool prim_contains(int type, const double* P, d3 p) {
+  switch (type) {
+    case RBG_SHAPE_BOX:
+      return fabs(p.x - P[RBG_BOX_OX]) <= P[RBG_BOX_DX] && fabs(p.y - P[RBG_BOX_OY]) <= P[RBG_BOX_DY] &&
+             fabs(p.z - P[RBG_BOX_OZ]) <= P[RBG_BOX_DZ];
+    case RBG_SHAPE_TUBE: {
+      if (fabs(p.z) > P[RBG_TUBE_DZ]) return false;
+      double r2 = p.x * p.x + p.y * p.y;
+      if (r2 > P[RBG_TUBE_RMAX] * P[RBG_TUBE_RMAX] || r2 < P[RBG_TUBE_RMIN] * P[RBG_TUBE_RMIN]) return false;
+      return phi_in(p.x, p.y, P[RBG_TUBE_PHI1], P[RBG_TUBE_DPHI]);
+    }
+    case RBG_SHAPE_SPHERE: {
+      double r2 = dot(p, p);
+      if (r2 > P[RBG_SPH_RMAX] * P[RBG_SPH_RMAX] || r2 < P[RBG_SPH_RMIN] * P[RBG_SPH_RMIN]) return false;
+      double th = atan2(sqrt(p.x * p.x + p.y * p.y), p.z) / kD2R;
+      if (th < P[RBG_SPH_TH1] || th > P[RBG_SPH_TH2]) return false;
+      return phi_in(p.x, p.y, P[RBG_SPH_PHI1], P[RBG_SPH_DPHI]);
+    }
+    case RBG_SHAPE_PARABOLOID: {
+      if (fabs(p.z) > P[RBG_PARA_DZ]) return false;
+      double f = P[RBG_PARA_A] * (p.x * p.x + p.y * p.y) + P[RBG_PARA_B];
+      return P[RBG_PARA_A] > 0 ? f <= p.z : f >= p.z;
+    }
+    case RBG_SHAPE_PGON:
+      return pxcon_contains(P, true, p);
+    case RBG_SHAPE_PCON:
+      return pxcon_contains(P, false, p);
+  }
+  return false;
+}
+
+// iterative CSG containment (composite trees are shallow; explicit stack)
+RBG_D bool csg_contains(const DevScene& S, int shape, d3 p) {
+  const rbg_shape_desc sh = S.shapes[shape];
+  if (sh.type != RBG_SHAPE_COMPOSITE) return prim_contains(sh.type, SP(S, shape), p);
+  // depth-2 composites (the common case) are resolved without recursion;
+  // deeper trees recurse through this same function
+  const double* P = SP(S, shape);
+  d3 pl = to_local(P + RBG_COMP_ML, p);
+  bool a = csg_contains(S, sh.left, pl);
+  if (sh.op == RBG_OP_INTERSECTION && !a) return false;
+  if (sh.op == RBG_OP_SUBTRACTION && !a) return false;
+  if (sh.op == RBG_OP_UNION && a) return true;
+  d3 pr = to_local(P + RBG_COMP_MR, p);
+  bool b = csg_contains(S, sh.right, pr);
+  if (sh.op == RBG_OP_SUBTRACTION) return !b;
+  return b;
+}
+
+// --------------------------------------------------------------------
+// crossing lists
+// --------------------------------------------------------------------
+struct XList {
+  double t[RBG_MAX_XINGS];
+  uint32_t code[RBG_MAX_XINGS];  // leaf << 16 | surface
+  int n;
+  bool overflow;
+};
+
+RBG_D void xl_add(XList& L, double t, uint32_t code) {
+  if (!isfinite(t)) return;
+  if (L.n >= RBG_MAX_XINGS) {
+    L.overflow = true;
+    return;
+  }
+  L.t[L.n] = t;
+  L.code[L.n] = code;
+  ++L.n;
+}
+
+RBG_D void add_plane(XList& L, d3 o, d3 d, d3 n, double rhs, uint32_t code) {
+  double den = dot(n, d);
+  if (den == 0) return;
+  xl_add(L, (rhs - dot(n, o)) / den, code);
+}
+
+// surface codes per primitive:
+//  BOX 0..5 (axis*2+side) | TUBE 0,1 z, 2 rmax, 3 rmin, 4,5 phi
+//  SPHERE 0 rmax, 1 rmin, 2 th1, 3 th2, 4,5 phi | PARABOLOID 0,1 z, 2 surface
+//  PGON k<nz z-plane k; nz + (k*2+w)*ned + e face; 0x3ffe/0x3fff phi
+//  PCON k<nz z-plane k; nz + k*2+w cone face; 0x3ffe/0x3fff phi
+constexpr uint32_t kPhi1 = 0x3ffe, kPhi2 = 0x3fff;
+
+RBG_D void add_phi(XList& L, d3 o, d3 d, double phi1, double dphi, uint32_t leaf) {
+  if (dphi >= 360.0) return;
+  double a1 = phi1 * kD2R, a2 = (phi1 + dphi) * kD2R;
+  add_plane(L, o, d, mk(-sin(a1), cos(a1), 0), 0.0, leaf | kPhi1);
+  add_plane(L, o, d, mk(-sin(a2), cos(a2), 0), 0.0, leaf | kPhi2);
+}
+
+RBG_D void prim_collect(int type, const double* P, d3 o, d3 d, uint32_t leaf, XList& L) {
+  double r[2];
+  switch (type) {
+    case RBG_SHAPE_BOX: {
+      const double oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        if (dd[k] == 0) continue;
+        xl_add(L, (P[3 + k] - P[k] - oo[k]) / dd[k], leaf | (uint32_t)(2 * k));
+        xl_add(L, (P[3 + k] + P[k] - oo[k]) / dd[k], leaf | (uint32_t)(2 * k + 1));
+      }
+      break;
+    }
+    case RBG_SHAPE_TUBE: {
+      if (d.z != 0) {
+        xl_add(L, (-P[RBG_TUBE_DZ] - o.z) / d.z, leaf | 0u);
+        xl_add(L, (P[RBG_TUBE_DZ] - o.z) / d.z, leaf | 1u);
+      }
+      double A = d.x * d.x + d.y * d.y, B = 2 * (o.x * d.x + o.y * d.y), C0 = o.x * o.x + o.y * o.y;
+      int k = quad_roots(A, B, C0 - P[RBG_TUBE_RMAX] * P[RBG_TUBE_RMAX], r);
+      for (int i = 0; i < k; ++i) xl_add(L, r[i], leaf | 2u);
+      if (P[RBG_TUBE_RMIN] > 0) {
+        k = quad_roots(A, B, C0 - P[RBG_TUBE_RMIN] * P[RBG_TUBE_RMIN], r);
+        for (int i = 0; i < k; ++i) xl_add(L, r[i], leaf | 3u);
+      }
+      add_phi(L, o, d, P[RBG_TUBE_PHI1], P[RBG_TUBE_DPHI], leaf);
+      break;
+    }
+    case RBG_SHAPE_SPHERE: {
+      double A = dot(d, d), B = 2 * dot(o, d), C0 = dot(o, o);
+      int k = quad_roots(A, B, C0 - P[RBG_SPH_RMAX] * P[RBG_SPH_RMAX], r);
+      for (int i = 0; i < k; ++i) xl_add(L, r[i], leaf | 0u);
+      if (P[RBG_SPH_RMIN] > 0) {
+        k = quad_roots(A, B, C0 - P[RBG_SPH_RMIN] * P[RBG_SPH_RMIN], r);
+        for (int i = 0; i < k; ++i) xl_add(L, r[i], leaf | 1u);
+      }
+      for (int w = 0; w < 2; ++w) {
+        double th = w == 0 ? P[RBG_SPH_TH1] : P[RBG_SPH_TH2];
+        if ((w == 0 && th <= 0) || (w == 1 && th >= 180)) continue;
+        double c2 = cos(th * kD2R);
+        c2 *= c2;
+        double s2 = 1 - c2;
+        double Ac = d.z * d.z * s2 - c2 * (d.x * d.x + d.y * d.y);
+        double Bc = 2 * (o.z * d.z * s2 - c2 * (o.x * d.x + o.y * d.y));
+        double Cc = o.z * o.z * s2 - c2 * (o.x * o.x + o.y * o.y);
+        k = quad_roots(Ac, Bc, Cc, r);
+        for (int i = 0; i < k; ++i) xl_add(L, r[i], leaf | (uint32_t)(2 + w));
+      }
+      add_phi(L, o, d, P[RBG_SPH_PHI1], P[RBG_SPH_DPHI], leaf);
+      break;
+    }
+    case RBG_SHAPE_PARABOLOID: {
+      if (d.z != 0) {
+        xl_add(L, (-P[RBG_PARA_DZ] - o.z) / d.z, leaf | 0u);
+        xl_add(L, (P[RBG_PARA_DZ] - o.z) / d.z, leaf | 1u);
+      }
+      double a = P[RBG_PARA_A], b = P[RBG_PARA_B];
+      double A = a * (d.x * d.x + d.y * d.y);
+      double B = 2 * a * (o.x * d.x + o.y * d.y) - d.z;
+      double C = a * (o.x * o.x + o.y * o.y) + b - o.z;
+      int k = quad_roots(A, B, C, r);
+      for (int i = 0; i < k; ++i) xl_add(L, r[i], leaf | 2u);
+      break;
+    }
+    case RBG_SHAPE_PGON: {
+      const int ned = (int)P[2], nz = (int)P[3];
+      const double* Z = P + 4;
+      const double* RMIN = Z + nz;
+      const double* RMAX = RMIN + nz;
+      if (d.z != 0)
+        for (int k = 0; k < nz; ++k) xl_add(L, (Z[k] - o.z) / d.z, leaf | (uint32_t)k);
+      const double sector = P[1] / ned;
+      for (int k = 0; k < nz - 1; ++k) {
+        double h = Z[k + 1] - Z[k];
+        if (h <= 0) continue;
+        for (int w = 0; w < 2; ++w) {
+          const double* R = w ? RMIN : RMAX;
+          if (w && R[k] == 0 && R[k + 1] == 0) continue;
+          double s = (R[k + 1] - R[k]) / h;
+          for (int e = 0; e < ned; ++e) {
+            double pe = (P[0] + (e + 0.5) * sector) * kD2R;
+            add_plane(L, o, d, mk(cos(pe), sin(pe), -s), R[k] - s * Z[k],
+                      leaf | (uint32_t)(nz + (k * 2 + w) * ned + e));
+          }
+        }
+      }
+      add_phi(L, o, d, P[0], P[1], leaf);
+      break;
+    }
+    case RBG_SHAPE_PCON: {
+      const int nz = (int)P[2];
+      const double* Z = P + 3;
+      const double* RMIN = Z + nz;
+      const double* RMAX = RMIN + nz;
+      if (d.z != 0)
+        for (int k = 0; k < nz; ++k) xl_add(L, (Z[k] - o.z) / d.z, leaf | (uint32_t)k);
+      for (int k = 0; k < nz - 1; ++k) {
+        double h = Z[k + 1] - Z[k];
+        if (h <= 0) continue;
+        for (int w = 0; w < 2; ++w) {
+          const double* R = w ? RMIN : RMAX;
+          if (w && R[k] == 0 && R[k + 1] == 0) continue;
+          double s = (R[k + 1] - R[k]) / h;
+          double c0 = R[k] - s * Z[k];
+          double A = d.x * d.x + d.y * d.y - s * s * d.z * d.z;
+          double B = 2 * (o.x * d.x + o.y * d.y - s * d.z * (c0 + s * o.z));
+          double C = o.x * o.x + o.y * o.y - (c0 + s * o.z) * (c0 + s * o.z);
+          int m = quad_roots(A, B, C, r);
+          for (int i = 0; i < m; ++i) xl_add(L, r[i], leaf | (uint32_t)(nz + k * 2 + w));
+        }
+      }
+      add_phi(L, o, d, P[0], P[1], leaf);
+      break;
+    }
+  }
+}
+
+// local normal of a primitive surface at point p (leaf frame)
+RBG_D d3 prim_normal(int type, const double* P, uint32_t surf, d3 p) {
+  if (surf == kPhi1 || surf == kPhi2) {
+    double phi1 = type == RBG_SHAPE_TUBE ? P[RBG_TUBE_PHI1] : type == RBG_SHAPE_SPHERE ? P[RBG_SPH_PHI1] : P[0];
+    double dphi = type == RBG_SHAPE_TUBE ? P[RBG_TUBE_DPHI] : type == RBG_SHAPE_SPHERE ? P[RBG_SPH_DPHI] : P[1];
+    double a = (surf == kPhi1 ? phi1 : phi1 + dphi) * kD2R;
+    return mk(-sin(a), cos(a), 0);
+  }
+  switch (type) {
+    case RBG_SHAPE_BOX: {
+      int axis = surf / 2;
+      return mk(axis == 0, axis == 1, axis == 2);
+    }
+    case RBG_SHAPE_TUBE:
+      if (surf < 2) return mk(0, 0, 1);
+      return mk(p.x, p.y, 0);
+    case RBG_SHAPE_SPHERE:
+      if (surf < 2) return p;
+      {
+        double th = surf == 2 ? P[RBG_SPH_TH1] : P[RBG_SPH_TH2];
+        double c2 = cos(th * kD2R);
+        c2 *= c2;
+        return mk(-c2 * p.x, -c2 * p.y, (1 - c2) * p.z);
+      }
+    case RBG_SHAPE_PARABOLOID:
+      if (surf < 2) return mk(0, 0, 1);
+      return mk(2 * P[RBG_PARA_A] * p.x, 2 * P[RBG_PARA_A] * p.y, -1);
+    case RBG_SHAPE_PGON: {
+      const int ned = (int)P[2], nz = (int)P[3];
+      if ((int)surf < nz) return mk(0, 0, 1);
+      int f = (int)surf - nz;
+      int e = f % ned, kw = f / ned, k = kw / 2, w = kw % 2;
+      const double* Z = P + 4;
+      const double* R = (w ? Z + nz : Z + 2 * nz);
+      double s = (R[k + 1] - R[k]) / (Z[k + 1] - Z[k]);
+      double pe = (P[0] + (e + 0.5) * (P[1] / ned)) * kD2R;
+      return mk(cos(pe), sin(pe), -s);
+    }
+    case RBG_SHAPE_PCON: {
+      const int nz = (int)P[2];
+      if ((int)surf < nz) return mk(0, 0, 1);
+      int f = (int)surf - nz;
+      int k = f / 2, w = f % 2;
+      const double* Z = P + 3;
+      const double* R = (w ? Z + nz : Z + 2 * nz);
+      double s = (R[k + 1] - R[k]) / (Z[k + 1] - Z[k]);
+      double c0 = R[k] - s * Z[k];
+      return mk(p.x, p.y, -s * (c0 + s * p.z));
+    }
+  }
+  return mk(0, 0, 1);
+}
+
+// Collect crossings of a (possibly composite) shape.  Leaves are numbered
+// in depth-first order; M maps the shape's frame to the query frame.
+// Recursion depth is bounded by the composite depth checked at build.
+RBG_D void csg_collect(const DevScene& S, int shape, const double* M, d3 o, d3 d, uint32_t& leaf, XList& L) {
+  const rbg_shape_desc sh = S.shapes[shape];
+  if (sh.type != RBG_SHAPE_COMPOSITE) {
+    d3 ol = to_local(M, o), dl = dir_to_local(M, d);
+    prim_collect(sh.type, SP(S, shape), ol, dl, leaf << 16, L);
+    ++leaf;
+    return;
+  }
+  const double* P = SP(S, shape);
+  M12 ML = mat_mul(M, P + RBG_COMP_ML);
+  csg_collect(S, sh.left, ML.v, o, d, leaf, L);
+  M12 MR = mat_mul(M, P + RBG_COMP_MR);
+  csg_collect(S, sh.right, MR.v, o, d, leaf, L);
+}
+
+// find leaf #target (depth-first) and its matrix
+RBG_D bool csg_find_leaf(const DevScene& S, int shape, const double* M, uint32_t target, uint32_t& leaf,
+                         int& leaf_shape, M12& leafM) {
+  const rbg_shape_desc sh = S.shapes[shape];
+  if (sh.type != RBG_SHAPE_COMPOSITE) {
+    if (leaf == target) {
+      leaf_shape = shape;
+#pragma unroll
+      for (int i = 0; i < 12; ++i) leafM.v[i] = M[i];
+      return true;
+    }
+    ++leaf;
+    return false;
+  }
+  const double* P = SP(S, shape);
+  M12 ML = mat_mul(M, P + RBG_COMP_ML);
+  if (csg_find_leaf(S, sh.left, ML.v, target, leaf, leaf_shape, leafM)) return true;
+  M12 MR = mat_mul(M, P + RBG_COMP_MR);
+  return csg_find_leaf(S, sh.right, MR.v, target, leaf, leaf_shape, leafM);
+}
+
+// Distance to enter (exit = false) or leave (exit = true) a TGeo primitive or
+// composite; on success code/normal describe the crossed surface (normal in
+// the shape frame, not oriented).
+RBG_D double csg_dist(const DevScene& S, int shape, d3 o, d3 d, bool exit, d3& nrm, unsigned& err) {
+  XList L;
+  L.n = 0;
+  L.overflow = false;
+  uint32_t leaf = 0;
+  M12 I = mat_identity();
+  csg_collect(S, shape, I.v, o, d, leaf, L);
+  if (L.overflow) {
+    err |= ERR_BIT_CAP;
+    return kBig;
+  }
+  // insertion sort on t
+  for (int i = 1; i < L.n; ++i) {
+    double t = L.t[i];
+    uint32_t c = L.code[i];
+    int j = i - 1;
+    while (j >= 0 && L.t[j] > t) {
+      L.t[j + 1] = L.t[j];
+      L.code[j + 1] = L.code[j];
+      --j;
+    }
+    L.t[j + 1] = t;
+    L.code[j + 1] = c;
+  }
+  int j0 = 0;
+  while (j0 < L.n && L.t[j0] <= 0) ++j0;
+  if (j0 == L.n) return kBig;
+  bool in_prev = false;
+  if (j0 > 0) {
+    double tm = 0.5 * (L.t[j0 - 1] + L.t[j0]);
+    in_prev = csg_contains(S, shape, o + tm * d);
+  }
+  for (int j = j0; j < L.n; ++j) {
+    bool in_next = false;
+    if (j + 1 < L.n) {
+      double tm = 0.5 * (L.t[j] + L.t[j + 1]);
+      in_next = csg_contains(S, shape, o + tm * d);
+    }
+    if ((!exit && !in_prev && in_next) || (exit && in_prev && !in_next)) {
+      double t = L.t[j];
+      uint32_t target = L.code[j] >> 16, surf = L.code[j] & 0xffffu;
+      uint32_t cnt = 0;
+      int ls = shape;
+      M12 LM = mat_identity();
+      csg_find_leaf(S, shape, I.v, target, cnt, ls, LM);
+      d3 pl = to_local(LM.v, o + t * d);
+      d3 nl = prim_normal(S.shapes[ls].type, SP(S, ls), surf, pl);
+      nrm = dir_to_master(LM.v, normalized(nl));
+      return t;
+    }
+    in_prev = in_next;
+  }
+  return kBig;
+}
+
+// --------------------------------------------------------------------
+// AGeoAsphericDisk (src/AGeoAsphericDisk.cxx)
+// --------------------------------------------------------------------
+struct Asph {
+  const double* P;
+  RBG_D double z(int s) const { return P[s == 1 ? RBG_ASPH_Z1 : RBG_ASPH_Z2]; }
+  RBG_D double c(int s) const { return P[s == 1 ? RBG_ASPH_C1 : RBG_ASPH_C2]; }
+  RBG_D double kap(int s) const { return P[s == 1 ? RBG_ASPH_KAPPA1 : RBG_ASPH_KAPPA2]; }
+  RBG_D int npol(int s) const { return (int)P[s == 1 ? RBG_ASPH_NPOL1 : RBG_ASPH_NPOL2]; }
+  RBG_D const double* K(int s) const {
+    return P + RBG_ASPH_K + (s == 1 ? 0 : (int)P[RBG_ASPH_NPOL1]);
+  }
+  RBG_D double rmin() const { return P[RBG_ASPH_RMIN]; }
+  RBG_D double rmax() const { return P[RBG_ASPH_RMAX]; }
+  RBG_D bool rseg() const { return P[RBG_ASPH_RSEG] != 0; }
+};
+
+// CalcF1/CalcF2 (:126-153): Horner in r^2 for the polynomial terms
+RBG_D bool asph_F(const Asph& a, int s, double r, double& f) {
+  double c = a.c(s), k = a.kap(s);
+  double p = r * r * c * c * k;
+  if (1 - p < 0) return false;
+  double r2 = r * r;
+  int n = a.npol(s);
+  const double* K = a.K(s);
+  double poly = 0;
+  for (int i = n - 1; i >= 0; --i) poly = (poly + K[i]) * r2;
+  f = a.z(s) + r2 * c / (1 + sqrt(1 - p)) + poly;
+  return true;
+}
+// CalcdF1dr/CalcdF2dr (:96-123)
+RBG_D bool asph_dF(const Asph& a, int s, double r, double& f) {
+  double c = a.c(s), k = a.kap(s);
+  double p = r * r * c * c * k;
+  if (1 - p <= 0) return false;
+  double r2 = r * r;
+  int n = a.npol(s);
+  const double* K = a.K(s);
+  double poly = 0;  // sum 2 i K_i r^(2i-1)
+  for (int i = n - 1; i >= 0; --i) poly = poly * r2 + 2 * (i + 1) * K[i];
+  f = r * c / sqrt(1 - p) + poly * r;
+  return true;
+}
+RBG_D bool asph_contains(const Asph& a, d3 p) {
+  double r = sqrt(p.x * p.x + p.y * p.y);
+  if (r > a.rmax() || r < a.rmin()) return false;
+  double f1, f2;
+  if (!asph_F(a, 1, r, f1) || !asph_F(a, 2, r, f2)) return false;
+  return !(p.z < f1 || f2 < p.z);
+}
+
+// DistToAsphere (:415-526)
+RBG_D double asph_dist_surface(const Asph& a, int n, d3 point, d3 dir) {
+  const double curve = a.c(n), kappa = a.kap(n);
+  const int npol = a.npol(n);
+  const double* K = a.K(n);
+  double H2 = point.x * point.x + point.y * point.y;
+  const double d = a.z(n);
+  double p = -((point.z - d) * dir.z + point.x * dir.x + point.y * dir.y);
+  double M = p * dir.z + point.z - d;
+  double M2 = (point.z - d) * (point.z - d) + H2 - p * p;
+  double check = 1 - (M2 * curve - 2 * M) * curve / dir.z / dir.z;
+  if (check < 0) return kBig;
+  double q = p + (M2 * curve - 2 * M) / (dir.z * (1 + sqrt(check)));
+  d3 np = mk(point.x + q * dir.x, point.y + q * dir.y, point.z + q * dir.z - d);
+  for (int i = 0;; i++) {
+    if (i > 100) return kBig;
+    H2 = np.x * np.x + np.y * np.y;
+    check = 1 - kappa * H2 * curve * curve;
+    if (check < 0) return kBig;
+    double l = sqrt(check);
+    // x = conic sag + sum K_j H2^(j+1); v = sum 2(j+1) K_j H2^j
+    double x = 0, v = 0;
+    for (int j = npol - 1; j >= 0; --j) {
+      x = (x + K[j]) * H2;
+      v = v * H2 + 2 * (j + 1) * K[j];
+    }
+    if (curve != 0) x += (1 - l) / curve / kappa;
+    v = curve * kappa + l * v;
+    double m = -np.x * v, nn = -np.y * v;
+    double norm = sqrt(l * l + m * m + nn * nn);
+    l /= norm;
+    m /= norm;
+    nn /= norm;
+    check = dir.z * l + dir.x * m + dir.y * nn;
+    if (check == 0) return kBig;
+    double e = l * (x - np.z) / check;
+    np = np + e * dir;
+    if (fabs(e) < 1e-10) break;
+  }
+  np.z += d;
+  d3 dv = np - point;
+  if (dot(dir, dv) < 0) return kBig;
+  double rz = sqrt(np.x * np.x + np.y * np.y);
+  if (rz < a.rmin() || rz > a.rmax()) return kBig;
+  return sqrt(dot(dv, dv));
+}
+
+// DistToInner / DistToOuter (:529-684)
+RBG_D double asph_dist_wall(const Asph& a, bool outer, d3 point, d3 dir) {
+  if (!outer && !a.rseg()) return kBig;
+  double rsq = point.x * point.x + point.y * point.y;
+  double nsq = dir.x * dir.x + dir.y * dir.y;
+  if (sqrt(nsq) < 1e-10) return kBig;
+  double rdotn = point.x * dir.x + point.y * dir.y;
+  double R = outer ? a.rmax() : a.rmin();
+  // TGeoTube::DistToTube
+  double b = rdotn / nsq;
+  double delta = b * b - (rsq - R * R) / nsq;
+  delta = delta > 0 ? sqrt(delta) : -1;
+  if (delta < 0) return kBig;
+  double t1 = -b + delta, t2 = -b - delta;
+  if (t1 < 0 && t2 < 0) return kBig;
+  double zmin, zmax;
+  if (!asph_F(a, 1, R, zmin) || !asph_F(a, 2, R, zmax)) return kBig;
+  if (t2 > 0) {
+    if (t1 > 0) {
+      double z1 = t1 * dir.z + point.z, z2 = t2 * dir.z + point.z;
+      if (z1 < zmin || zmax < z1) t1 = kBig;
+      if (z2 < zmin || zmax < z2) t2 = kBig;
+      return t1 < t2 ? t1 : t2;
+    }
+  } else if (t2 == 0) {
+    if (t1 > 0) {
+      if (zmin <= point.z && point.z <= zmax) return 0;
+      double z1 = t1 * dir.z + point.z;
+      if (zmin <= z1 && z1 <= zmax) return t1;
+    } else if (t1 == 0) {
+      if (zmin <= point.z && point.z <= zmax) return 0;
+    }
+  } else {
+    if (t1 > 0) {
+      double z1 = t1 * dir.z + point.z;
+      if (zmin <= z1 && z1 <= zmax) return t1;
+    } else if (t1 == 0) {
+      if (zmin <= point.z && point.z <= zmax) return 0;
+    }
+  }
+  return kBig;
+}
+
+RBG_D double asph_dist4(const Asph& a, d3 p, d3 d) {
+  double best = asph_dist_surface(a, 1, p, d);
+  double v = asph_dist_surface(a, 2, p, d);
+  if (v < best) best = v;
+  v = asph_dist_wall(a, false, p, d);
+  if (v < best) best = v;
+  v = asph_dist_wall(a, true, p, d);
+  if (v < best) best = v;
+  return best;
+}
+
+// reach of the bounding hollow tube (rmin, rmax, dz) at t >= 0 (the
+// TGeoTube::DistFromOutsideS test of DistFromOutside, :393-395)
+RBG_D bool tube_reached(d3 o, d3 d, double rmin, double rmax, double dz) {
+  double P[RBG_TUBE_NP] = {rmin, rmax, dz, 0, 360};
+  if (prim_contains(RBG_SHAPE_TUBE, P, o)) return true;
+  XList L;
+  L.n = 0;
+  L.overflow = false;
+  prim_collect(RBG_SHAPE_TUBE, P, o, d, 0u, L);
+  for (int i = 1; i < L.n; ++i) {
+    double t = L.t[i];
+    int j = i - 1;
+    while (j >= 0 && L.t[j] > t) {
+      L.t[j + 1] = L.t[j];
+      --j;
+    }
+    L.t[j + 1] = t;
+  }
+  for (int j = 0; j + 1 < L.n; ++j) {
+    if (L.t[j + 1] <= 0) continue;
+    double tm = 0.5 * (L.t[j] + L.t[j + 1]);
+    if (prim_contains(RBG_SHAPE_TUBE, P, o + tm * d)) return true;
+  }
+  return false;
+}
+
+RBG_D double asph_dist_out(const Asph& a, d3 p, d3 d) {
+  d3 pp = mk(p.x, p.y, p.z - a.P[RBG_ASPH_ORIGIN_Z]);
+  if (!tube_reached(pp, d, a.rmin(), a.rmax(), a.P[RBG_ASPH_DZ])) return kBig;
+  return asph_dist4(a, p, d);
+}
+
+// ComputeNormal (:246-327)
+RBG_D d3 asph_normal(const Asph& a, d3 point, d3 dir) {
+  double r = sqrt(point.x * point.x + point.y * point.y);
+  double phi = atan2(point.y, point.x);
+  double saf[4];
+  saf[0] = a.rseg() ? fabs(r - a.rmin()) : kBig;
+  saf[1] = fabs(r - a.rmax());
+  double f1, f2, df1 = kBig, df2 = kBig;
+  if (!asph_F(a, 1, r, f1)) f1 = -kBig;
+  if (f1 == -kBig) saf[2] = kBig;
+  else saf[2] = asph_dF(a, 1, r, df1) ? fabs(f1 - point.z) / sqrt(1 + df1 * df1) : kBig;
+  if (!asph_F(a, 2, r, f2)) f2 = kBig;
+  if (f2 == kBig) saf[3] = kBig;
+  else saf[3] = asph_dF(a, 2, r, df2) ? fabs(f2 - point.z) / sqrt(1 + df2 * df2) : kBig;
+  int i = 0;
+  for (int k = 1; k < 4; ++k)
+    if (saf[k] < saf[i]) i = k;
+  d3 nv = mk(0, 0, 0);
+  if (i <= 1) {
+    nv.x = 1;
+  } else {
+    double df = i == 2 ? df1 : df2;
+    if (df == 0) nv.z = 1;
+    else {
+      nv.x = df / sqrt(1 + df * df);
+      nv.z = -1 / sqrt(1 + df * df);
+    }
+  }
+  double c = cos(phi), s = sin(phi);
+  d3 n = mk(c * nv.x - s * nv.y, s * nv.x + c * nv.y, nv.z);
+  if (dot(n, dir) < 0) n = neg(n);
+  return n;
+}
+
+// --------------------------------------------------------------------
+// AGeoWinstonConePoly
+// --------------------------------------------------------------------
+struct Win {
+  double r1, r2, theta, f, dz;
+  int n;
+};
+RBG_D Win win_load(const double* P) {
+  Win w;
+  w.r1 = P[RBG_WIN_R1];
+  w.r2 = P[RBG_WIN_R2];
+  w.n = (int)P[RBG_WIN_N];
+  w.theta = P[RBG_WIN_THETA];
+  w.f = P[RBG_WIN_F];
+  w.dz = P[RBG_WIN_DZ];
+  return w;
+}
+// CalcR (AGeoWinstonCone2D.cxx:82-98)
+RBG_D bool win_R(const Win& w, double z, double& r) {
+  if (fabs(z) > w.dz + 1e-10) return false;
+  double sint = sin(w.theta), cost = cos(w.theta);
+  double t = z + w.dz;
+  double a0 = t * t * sint * sint - 4. * w.f * (t * cost + w.f);
+  double a1 = 2. * t * sint * cost + 4. * w.f * sint;
+  double a2 = cost * cost;
+  r = (-a1 + sqrt(a1 * a1 - 4. * a0 * a2)) / (2 * a2) - w.r2;
+  return true;
+}
+// CalcdRdZ (:59-79)
+RBG_D double win_dRdZ(const Win& w, double z) {
+  double sint = sin(w.theta), cost = cos(w.theta);
+  double t = z + w.dz;
+  double a0 = t * t * sint * sint - 4. * w.f * (t * cost + w.f);
+  double a1 = 2. * t * sint * cost + 4. * w.f * sint;
+  double a2 = cost * cost;
+  double da0dt = 2 * t * sint * sint - 4 * w.f * cost;
+  double da1dt = 2 * sint * cost;
+  return (-da1dt + (a1 * da1dt - 2 * da0dt * a2) / sqrt(a1 * a1 - 4 * a0 * a2)) / (2 * a2);
+}
+// InsidePolygon (ConePoly.cxx:293-309)
+RBG_D bool win_inside_polygon(const Win& w, double x, double y, double r) {
+  double th = atan2(y, x);
+  while (th > kPi / w.n) th -= 2 * kPi / w.n;
+  while (th < -kPi / w.n) th += 2 * kPi / w.n;
+  return !(sqrt(x * x + y * y) * cos(th) > r);
+}
+RBG_D bool win_contains(const Win& w, d3 p) {
+  if (fabs(p.z) > w.dz) return false;
+  double r;
+  if (!win_R(w, p.z, r)) return false;
+  return win_inside_polygon(w, p.x, p.y, r);
+}
+// DistToParabola (Cone2D.cxx:325-428)
+RBG_D double win_dist_parabola(const Win& w, d3 point, d3 dir, double phi, double open) {
+  double cp = cos(phi), sp = sin(phi);
+  double x = cp * point.x + sp * point.y;
+  double y = -sp * point.x + cp * point.y;
+  double z = point.z;
+  double px = cp * dir.x + sp * dir.y;
+  double py = -sp * dir.x + cp * dir.y;
+  double pz = dir.z;
+  if (px == 0 && pz == 0) return kBig;
+  double cost = cos(w.theta), sint = sin(w.theta);
+  double X = cost * (x + w.r2) + (z + w.dz) * sint;
+  double Z = -sint * (x + w.r2) + (z + w.dz) * cost + w.f;
+  double alpha = atan2(pz, px);
+  double tanA = tan(alpha - w.theta);
+  double tmp = tanA * tanA - (X * tanA - Z) / w.f;
+  if (tmp < 0) return kBig;
+  double Xp, Xm;
+  if (w.dz * 2 / fabs(tanA) < 1e-10) {
+    Xp = X;
+    Xm = X;
+  } else {
+    double sq = sqrt(tmp);
+    Xp = 2 * w.f * (tanA + sq);
+    Xm = 2 * w.f * (tanA - sq);
+  }
+  double best = kBig;
+  for (int s = 0; s < 2; ++s) {
+    double Xc = s == 0 ? Xp : Xm;
+    double Zc = Xc * Xc / 4. / w.f;
+    double xc = cost * Xc - sint * (Zc - w.f) - w.r2;
+    double zc = sint * Xc + cost * (Zc - w.f) - w.dz;
+    double yc;
+    if (fabs(px) <= fabs(pz) && fabs(py) <= fabs(pz)) yc = y + (zc - z) * py / pz;
+    else if (fabs(py) <= fabs(px) && fabs(pz) <= fabs(px)) yc = y + (xc - x) * py / px;
+    else yc = y + (fabs(px) < 1e-5 ? (zc - z) * py / pz : (xc - x) * py / px);
+    double dx = xc - x, dy = yc - y, dz = zc - z;
+    double v;
+    if (xc < w.r2 || w.r1 < xc || zc < -w.dz || w.dz < zc || dx * px + dz * pz < 0) v = kBig;
+    else v = fabs(atan2(yc, xc)) <= open / 2. ? sqrt(dx * dx + dy * dy + dz * dz) : kBig;
+    if (v < best) best = v;
+  }
+  return best;
+}
+RBG_D double win_dist_in(const Win& w, d3 p, d3 d) {
+  double best = kBig;
+  if (d.z < 0) best = (-p.z - w.dz) / d.z;
+  else if (d.z > 0) best = (w.dz - p.z) / d.z;
+  for (int i = 0; i < w.n; i++) {
+    double v = win_dist_parabola(w, p, d, i * 2 * kPi / w.n, kPi);
+    if (v < best) best = v;
+  }
+  return best;
+}
+RBG_D double win_dist_out(const Win& w, d3 p, d3 d) {
+  if (p.z <= -w.dz) {
+    if (d.z <= 0) return kBig;
+    double s = -(w.dz + p.z) / d.z;
+    if (win_inside_polygon(w, p.x + s * d.x, p.y + s * d.y, w.r2)) return s;
+  } else if (p.z >= w.dz) {
+    if (d.z >= 0) return kBig;
+    double s = (w.dz - p.z) / d.z;
+    if (win_inside_polygon(w, p.x + s * d.x, p.y + s * d.y, w.r1)) return s;
+  }
+  double best = kBig;
+  for (int i = 0; i < w.n; i++) {
+    double v = win_dist_parabola(w, p, d, i * 2 * kPi / w.n, 2 * kPi / w.n);
+    if (v < best) best = v;
+  }
+  return best;
+}
+// ComputeNormal (ConePoly.cxx:67-122)
+RBG_D d3 win_normal(const Win& w, d3 point, d3 dir) {
+  double x = point.x, y = point.y, z = point.z;
+  double saf0 = fabs(fabs(w.dz) - fabs(z)), saf1;
+  double phi = atan2(y, x);
+  while (phi > kPi / w.n) phi -= 2 * kPi / w.n;
+  while (phi < -kPi / w.n) phi += 2 * kPi / w.n;
+  double R;
+  saf1 = win_R(w, z, R) ? fabs(R - sqrt(x * x + y * y) * cos(phi)) : kBig;
+  d3 n;
+  if (saf0 <= saf1) {
+    n = mk(0, 0, 1);
+  } else {
+    phi = atan2(y, x);
+    if (phi < -kPi / w.n) phi += 2 * kPi;
+    int k = (int)floor((phi + kPi / w.n) / (2 * kPi / w.n));
+    n = mk(cos(k * 2 * kPi / w.n), sin(k * 2 * kPi / w.n), -win_dRdZ(w, z));
+  }
+  n = normalized(n);
+  if (dot(n, dir) < 0) n = neg(n);
+  return n;
+}
+
+// --------------------------------------------------------------------
+// dispatch
+// --------------------------------------------------------------------
+RBG_D bool shape_contains(const DevScene& S, int shape, d3 p) {
+  const int type = S.shapes[shape].type;
+  if (type == RBG_SHAPE_ASPHERIC_DISK) return asph_contains(Asph{SP(S, shape)}, p);
+  if (type == RBG_SHAPE_WINSTON_POLY) return win_contains(win_load(SP(S, shape)), p);
+  return csg_contains(S, shape, p);
+}
+
+RBG_D double shape_dist(const DevScene& S, int shape, d3 p, d3 d, bool exit, d3& nrm, unsigned& err) {
+  const int type = S.shapes[shape].type;
+  if (type == RBG_SHAPE_ASPHERIC_DISK) {
+    Asph a{SP(S, shape)};
+    return exit ? asph_dist4(a, p, d) : asph_dist_out(a, p, d);
+  }
+  if (type == RBG_SHAPE_WINSTON_POLY) {
+    Win w = win_load(SP(S, shape));
+    return exit ? win_dist_in(w, p, d) : win_dist_out(w, p, d);
+  }
+  return csg_dist(S, shape, p, d, exit, nrm, err);
+}
+
+RBG_D bool is_ageo(int type) { return type == RBG_SHAPE_ASPHERIC_DISK || type == RBG_SHAPE_WINSTON_POLY; }
+
+}  // namespace rbg

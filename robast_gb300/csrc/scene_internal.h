@@ -1,0 +1,40 @@
+// scene_internal.h -- host-side representation of a flattened scene.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "robast_gb.h"
+#include "robast_gb_layout.h"
+
+struct rbg_device_scene;  // defined in trace_common.cuh
+
+struct rbg_scene {
+  // canonical description tables (ids identical to the user description)
+  std::vector<rbg_shape_desc> shapes;
+  std::vector<double> params;
+  std::vector<rbg_volume_desc> volumes;
+  std::vector<rbg_table_desc> tables;
+  std::vector<rbg_index_desc> indices;
+  std::vector<rbg_layer_desc> layers;
+  std::vector<rbg_multilayer_desc> multilayers;
+  std::vector<rbg_border_desc> borders;
+  // physical tree
+  std::vector<rbg_node> nodes;
+  std::vector<int32_t> children;
+  std::vector<rbg_bvh_node> bvh;
+  std::vector<int32_t> bvh_items;
+  // local bounding boxes per shape: lo[3], hi[3]
+  std::vector<double> shape_box;
+
+  // device mirror, owned by the CUDA side (capi.cu)
+  rbg_device_scene* dev = nullptr;
+  int dev_id = -1;
+  int last_launches = 0;
+  void* workspace = nullptr;
+  size_t workspace_bytes = 0;
+};
+
+// host helpers shared with the C-ABI implementation
+namespace rbg {
+void release_device(rbg_scene* s);  // capi.cu
+}

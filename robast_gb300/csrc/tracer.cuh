@@ -1,0 +1,658 @@
+// tracer.cuh -- navigation and the AOpticsManager state machine on the
+// device (src/AOpticsManager.cxx:52-520), one thread per ray.
+#pragma once
+#include "geometry.cuh"
+
+namespace rbg {
+
+// --------------------------------------------------------------------
+// navigation (TGeoNavigator semantics restated)
+// --------------------------------------------------------------------
+struct Nav {
+  int node;   // current node, -1 outside the top volume
+  d3 p, d;    // navigator point and direction (master frame)
+  int xnode;  // node whose surface the last step crossed
+  d3 xn;      // its normal for TGeo primitives (node frame)
+};
+
+RBG_D bool in_box(const double* lo, const double* hi, d3 p) {
+  return !(p.x < lo[0] || p.x > hi[0] || p.y < lo[1] || p.y > hi[1] || p.z < lo[2] || p.z > hi[2]);
+}
+RBG_D bool in_fbox(const float* lo, const float* hi, d3 p) {
+  return !(p.x < lo[0] || p.x > hi[0] || p.y < lo[1] || p.y > hi[1] || p.z < lo[2] || p.z > hi[2]);
+}
+
+RBG_D bool node_contains(const DevScene& S, int k, d3 p) {
+  const rbg_node& N = S.nodes[k];
+  if (!in_box(N.lo, N.hi, p)) return false;
+  return shape_contains(S, N.shape, to_local(N.m, p));
+}
+
+// segment [0, smax] of the ray against a box
+template <typename T>
+RBG_D bool seg_box(d3 o, d3 inv, d3 d, double smax, const T* lo, const T* hi) {
+  double t0 = 0, t1 = smax;
+  const double oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z}, ii[3] = {inv.x, inv.y, inv.z};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (dd[a] == 0) {
+      if (oo[a] < (double)lo[a] || oo[a] > (double)hi[a]) return false;
+      continue;
+    }
+    double ta = ((double)lo[a] - oo[a]) * ii[a], tb = ((double)hi[a] - oo[a]) * ii[a];
+    if (ta > tb) {
+      double s = ta;
+      ta = tb;
+      tb = s;
+    }
+    t0 = fmax(t0, ta);
+    t1 = fmin(t1, tb);
+    if (t0 > t1) return false;
+  }
+  return true;
+}
+
+// first child (in placement order) of node k containing p, or -1
+RBG_D int first_child_containing(const DevScene& S, int k, d3 p) {
+  const rbg_node& N = S.nodes[k];
+  if (N.bvh_root < 0) {
+    for (int i = 0; i < N.child_count; ++i) {
+      int c = S.children[N.child_begin + i];
+      if (node_contains(S, c, p)) return c;
+    }
+    return -1;
+  }
+  int best = -1;
+  int stack[32];
+  int sp = 0;
+  stack[sp++] = N.bvh_root;
+  while (sp > 0) {
+    const rbg_bvh_node& b = S.bvh[stack[--sp]];
+    if (!in_fbox(b.lo, b.hi, p)) continue;
+    if (b.left < 0) {
+      for (int i = 0; i < b.right; ++i) {
+        int c = S.bvh_items[b.item_begin + i];
+        if ((best < 0 || c < best) && node_contains(S, c, p)) best = c;
+      }
+    } else if (sp + 2 <= 32) {
+      stack[sp++] = b.left;
+      stack[sp++] = b.right;
+    }
+  }
+  return best;
+}
+
+RBG_D int locate_down(const DevScene& S, int k, d3 p) {
+  for (int depth = 0; depth < 64; ++depth) {
+    int c = first_child_containing(S, k, p);
+    if (c < 0) return k;
+    k = c;
+  }
+  return k;
+}
+RBG_D int locate_from_top(const DevScene& S, d3 p) {
+  if (!node_contains(S, 0, p)) return -1;
+  return locate_down(S, 0, p);
+}
+
+// candidate daughter test shared by the scan and the BVH walk
+RBG_D void try_child(const DevScene& S, int k, d3 p, d3 d, double& best, int& xnode, bool& enter, d3& nbest,
+                     unsigned& err) {
+  const rbg_node& K = S.nodes[k];
+  d3 nrm = mk(0, 0, 1);
+  double s = shape_dist(S, K.shape, to_local(K.m, p), dir_to_local(K.m, d), false, nrm, err);
+  // ties: leaving the mother first, then the lowest node id (placement order)
+  if (s < best || (s == best && enter && k < xnode)) {
+    best = s;
+    xnode = k;
+    enter = true;
+    nbest = nrm;
+  }
+}
+
+// TGeoNavigator::FindNextBoundaryAndStep
+RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, unsigned& err) {
+  const int c = nv.node;
+  double best;
+  d3 nbest = mk(0, 0, 1);
+  int xnode;
+  bool enter;
+  if (c < 0) {
+    const rbg_node& T = S.nodes[0];
+    best = shape_dist(S, T.shape, to_local(T.m, nv.p), dir_to_local(T.m, nv.d), false, nbest, err);
+    if (best >= kBig) {
+      step = 0;
+      nv.xnode = -1;
+      return -1;
+    }
+    xnode = 0;
+    enter = true;
+  } else {
+    const rbg_node& N = S.nodes[c];
+    best = shape_dist(S, N.shape, to_local(N.m, nv.p), dir_to_local(N.m, nv.d), true, nbest, err);
+    xnode = c;
+    enter = false;
+    d3 inv = mk(1.0 / nv.d.x, 1.0 / nv.d.y, 1.0 / nv.d.z);
+    if (N.bvh_root < 0) {
+      for (int i = 0; i < N.child_count; ++i) {
+        int k = S.children[N.child_begin + i];
+        const rbg_node& K = S.nodes[k];
+        if (!seg_box(nv.p, inv, nv.d, best, K.lo, K.hi)) continue;
+        try_child(S, k, nv.p, nv.d, best, xnode, enter, nbest, err);
+      }
+    } else {
+      int stack[32];
+      int sp = 0;
+      stack[sp++] = N.bvh_root;
+      while (sp > 0) {
+        const rbg_bvh_node& b = S.bvh[stack[--sp]];
+        if (!seg_box(nv.p, inv, nv.d, best, b.lo, b.hi)) continue;
+        if (b.left < 0) {
+          for (int i = 0; i < b.right; ++i) {
+            int k = S.bvh_items[b.item_begin + i];
+            const rbg_node& K = S.nodes[k];
+            if (!seg_box(nv.p, inv, nv.d, best, K.lo, K.hi)) continue;
+            try_child(S, k, nv.p, nv.d, best, xnode, enter, nbest, err);
+          }
+        } else if (sp + 2 <= 32) {
+          stack[sp++] = b.right;
+          stack[sp++] = b.left;
+        } else {
+          err |= ERR_BIT_CAP;
+        }
+      }
+    }
+  }
+  nv.p = nv.p + (best + RBG_BOUNDARY_PUSH) * nv.d;
+  nv.xnode = xnode;
+  nv.xn = nbest;
+  int next;
+  if (enter) {
+    next = locate_down(S, xnode, nv.p);
+  } else {
+    int q = S.nodes[c].parent;
+    while (q >= 0 && !node_contains(S, q, nv.p)) q = S.nodes[q].parent;
+    next = q < 0 ? -1 : locate_down(S, q, nv.p);
+  }
+  nv.node = next;
+  step = best;
+  return next;
+}
+
+// TGeoNavigator::FindNormal: master-frame normal, n . d >= 0
+RBG_D d3 find_normal(const DevScene& S, const Nav& nv) {
+  if (nv.xnode < 0) return mk(0, 0, 1);
+  const rbg_node& N = S.nodes[nv.xnode];
+  const int type = S.shapes[N.shape].type;
+  d3 nl;
+  if (type == RBG_SHAPE_ASPHERIC_DISK) {
+    nl = asph_normal(Asph{SP(S, N.shape)}, to_local(N.m, nv.p), dir_to_local(N.m, nv.d));
+  } else if (type == RBG_SHAPE_WINSTON_POLY) {
+    nl = win_normal(win_load(SP(S, N.shape)), to_local(N.m, nv.p), dir_to_local(N.m, nv.d));
+  } else {
+    nl = nv.xn;
+  }
+  d3 n = normalized(dir_to_master(N.m, nl));
+  if (dot(n, nv.d) < 0) n = neg(n);
+  return n;
+}
+
+// --------------------------------------------------------------------
+// complex arithmetic for the transfer matrices
+// --------------------------------------------------------------------
+struct cplx {
+  double re, im;
+};
+RBG_D cplx cx(double r, double i = 0) { return cplx{r, i}; }
+RBG_D cplx operator+(cplx a, cplx b) { return cplx{a.re + b.re, a.im + b.im}; }
+RBG_D cplx operator-(cplx a, cplx b) { return cplx{a.re - b.re, a.im - b.im}; }
+RBG_D cplx operator*(cplx a, cplx b) { return cplx{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+RBG_D cplx operator*(double s, cplx a) { return cplx{s * a.re, s * a.im}; }
+RBG_D cplx cdiv(cplx a, cplx b) {
+  // Smith's algorithm
+  if (fabs(b.re) >= fabs(b.im)) {
+    double r = b.im / b.re, den = b.re + b.im * r;
+    return cplx{(a.re + a.im * r) / den, (a.im - a.re * r) / den};
+  }
+  double r = b.re / b.im, den = b.re * r + b.im;
+  return cplx{(a.re * r + a.im) / den, (a.im * r - a.re) / den};
+}
+RBG_D double cabs_(cplx a) { return hypot(a.re, a.im); }
+RBG_D cplx cexp_(cplx a) {
+  double e = exp(a.re);
+  double s, c;
+  sincos(a.im, &s, &c);
+  return cplx{e * c, e * s};
+}
+RBG_D cplx ccos_(cplx a) {
+  double s, c;
+  sincos(a.re, &s, &c);
+  return cplx{c * cosh(a.im), -s * sinh(a.im)};
+}
+RBG_D cplx csin_(cplx a) {
+  double s, c;
+  sincos(a.re, &s, &c);
+  return cplx{s * cosh(a.im), c * sinh(a.im)};
+}
+RBG_D cplx csqrt_(cplx a) {
+  // principal square root
+  if (a.re == 0 && a.im == 0) return cplx{0, a.im};
+  double m = hypot(a.re, a.im);
+  double t = sqrt(0.5 * (m + fabs(a.re)));
+  if (a.re >= 0) return cplx{t, a.im / (2 * t)};
+  return cplx{fabs(a.im) / (2 * t), copysign(t, a.im)};
+}
+RBG_D cplx clog_(cplx a) { return cplx{log(hypot(a.re, a.im)), atan2(a.im, a.re)}; }
+// principal arcsine: -i log(i z + sqrt(1 - z^2))
+RBG_D cplx casin_(cplx z) {
+  cplx one_m = cx(1) - z * z;
+  cplx w = cplx{-z.im, z.re} + csqrt_(one_m);
+  cplx l = clog_(w);
+  return cplx{l.im, -l.re};
+}
+
+RBG_D bool is_forward_angle(cplx n, cplx th) {
+  const double eps = 2.220446049250313e-16;
+  cplx nc = n * ccos_(th);
+  if (fabs(nc.im) > 100 * eps) return nc.im > 0;
+  return nc.re > 0;
+}
+
+// AMultilayer::CoherentTMM (src/AMultilayer.cxx:240-481), pol 0 = s, 1 = p
+RBG_D void coherent_tmm(const DevScene& S, int ml, int pol, double th0r, double lam, double& R, double& T) {
+  const rbg_multilayer_desc M = S.multilayers[ml];
+  const int N = M.n_layers;
+  // pass 1: first and last media and forward angles
+  auto nidx = [&](int i) {
+    const rbg_layer_desc& L = S.layers[M.layer_offset + i];
+    return cx(index_n(S, L.index, lam), index_k(S, L.index, lam));
+  };
+  cplx th0 = cx(th0r);
+  cplx n0 = nidx(0);
+  cplx n0s = n0 * csin_(th0);
+  cplx th_first = casin_(cdiv(n0s, n0));
+  if (!is_forward_angle(n0, th_first)) th_first = cx(kPi) - th_first;
+  // running transfer-matrix product over layers 1..N-2, built front to back
+  cplx a = cx(1), b = cx(0), c = cx(0), d = cx(1);
+  cplx n_prev = n0, ct_prev = ccos_(th_first);
+  cplx r0 = cx(0), t0 = cx(1);
+  for (int i = 1; i < N; ++i) {
+    cplx ni = nidx(i);
+    cplx thi = casin_(cdiv(n0s, ni));
+    if (i == N - 1 && !is_forward_angle(ni, thi)) thi = cx(kPi) - thi;
+    cplx cti = ccos_(thi);
+    // interface (i-1) -> i
+    cplx ii = n_prev * ct_prev, r, t;
+    if (pol == 0) {
+      cplx ff = ni * cti;
+      r = cdiv(ii - ff, ii + ff);
+      t = cdiv(2.0 * ii, ii + ff);
+    } else {
+      cplx fi = ni * ct_prev, iff = n_prev * cti;
+      r = cdiv(fi - iff, fi + iff);
+      t = cdiv(2.0 * ii, fi + iff);
+    }
+    if (i == 1) {
+      r0 = r;
+      t0 = t;
+    } else {
+      // layer i-1 matrix: (1/t) diag(e^{-i delta}, e^{i delta}) [[1, r],[r, 1]]
+      const rbg_layer_desc& L = S.layers[M.layer_offset + i - 1];
+      cplx kz = (2 * kPi / lam) * (n_prev * ct_prev);
+      cplx delta = L.thickness * kz;
+      if (delta.im > 35) delta.im = 35;
+      cplx em = cexp_(cplx{delta.im, -delta.re});
+      cplx ep = cexp_(cplx{-delta.im, delta.re});
+      cplx it = cdiv(cx(1), t);
+      cplx m00 = em * it, m01 = em * r * it, m10 = ep * r * it, m11 = ep * it;
+      cplx na = a * m00 + b * m10, nb = a * m01 + b * m11;
+      cplx nc = c * m00 + d * m10, nd = c * m01 + d * m11;
+      a = na;
+      b = nb;
+      c = nc;
+      d = nd;
+    }
+    n_prev = ni;
+    ct_prev = cti;
+  }
+  // prepend the first interface: (1/t0) [[1, r0],[r0, 1]] * Mtilde
+  cplx it0 = cdiv(cx(1), t0);
+  cplx A = (a + r0 * c) * it0, Cc = (r0 * a + c) * it0;
+  cplx rr = cdiv(Cc, A), tt = cdiv(cx(1), A);
+  double ar = cabs_(rr);
+  R = ar * ar;
+  cplx ct0 = ccos_(th0);
+  cplx nf = n_prev, ctf = ct_prev;
+  double tt2 = cabs_(tt * tt);
+  if (pol == 0) T = tt2 * ((nf * ctf).re / (n0 * ct0).re);
+  else T = tt2 * ((nf * cx(ctf.re, -ctf.im)).re / (n0 * cx(ct0.re, -ct0.im)).re);
+}
+
+RBG_D void coherent_tmm_mixed(const DevScene& S, int ml, double th0, double lam, double& R, double& T) {
+  double rp, tp, rs, ts;
+  coherent_tmm(S, ml, 1, th0, lam, rp, tp);
+  coherent_tmm(S, ml, 0, th0, lam, rs, ts);
+  R = (rp + rs) / 2.;
+  T = (tp + ts) / 2.;
+}
+
+// --------------------------------------------------------------------
+// ray record and random draws
+// --------------------------------------------------------------------
+struct Ray {
+  d3 x;
+  double t;
+  d3 d;
+  double lambda;
+  int status, npoints, last_node;
+  RayRng rng;
+  unsigned err;
+  // history
+  int hist_cap;
+  double* hist_xyzt;
+  int32_t* hist_node;
+};
+
+RBG_D double rng_u(Ray& r) {
+  Philox4 b = r.rng.next();
+  return u53(b.v[0], b.v[1]);
+}
+RBG_D double rng_gaus(Ray& r, double sigma) {
+  Philox4 b = r.rng.next();
+  double a = u53(b.v[0], b.v[1]), c = u53(b.v[2], b.v[3]);
+  return sigma * sqrt(-2.0 * log(1.0 - a)) * cos(2.0 * kPi * c);
+}
+
+RBG_D void add_point(Ray& r, d3 p, double t) {
+  r.x = p;
+  r.t = t;
+  if (r.npoints < r.hist_cap) {
+    double* h = r.hist_xyzt + 4 * (size_t)r.npoints;
+    h[0] = p.x;
+    h[1] = p.y;
+    h[2] = p.z;
+    h[3] = t;
+    r.hist_node[r.npoints] = -2;
+  }
+  r.npoints++;
+}
+RBG_D void add_node(Ray& r, int node) {
+  r.last_node = node;
+  int idx = r.npoints - 1;
+  if (idx >= 0 && idx < r.hist_cap) r.hist_node[idx] = node;
+}
+RBG_D void set_direction(Ray& r, d3 v) {
+  double mag = sqrt(dot(v, v));
+  if (mag > 0) r.d = mk(v.x / mag, v.y / mag, v.z / mag);
+}
+
+enum { kLens = 0, kObs = 1, kMirror = 2, kFocus = 3, kOpt = 4, kOther = 5, kNull = 6 };
+RBG_D int kind_of(const DevScene& S, int node) { return node < 0 ? kNull : S.nodes[node].kind; }
+
+RBG_D int find_border(const DevScene& S, int cur, int next) {
+  if (cur < 0) return -1;
+  int c1 = S.nodes[cur].volume, c2 = next < 0 ? -1 : S.nodes[next].volume;
+  for (int i = 0; i < S.n_borders; ++i)
+    if (S.borders[i].component1 == c1 && S.borders[i].component2 == c2) return i;
+  return -1;
+}
+
+RBG_D double lens_n(const DevScene& S, int node, double lam) {
+  return index_n(S, S.volumes[S.nodes[node].volume].index, lam);
+}
+
+// TVector3::RotateUz
+RBG_D d3 rotate_uz(d3 v, d3 u) {
+  double up = u.x * u.x + u.y * u.y;
+  if (up > 0) {
+    up = sqrt(up);
+    return mk((u.x * u.z * v.x - u.y * v.y) / up + u.x * v.z, (u.y * u.z * v.x + u.x * v.y) / up + u.y * v.z,
+              -up * v.x + u.z * v.z);
+  }
+  if (u.z < 0.) return mk(-v.x, v.y, -v.z);
+  return v;
+}
+
+// GetFacetNormal (:250-301)
+RBG_D d3 get_facet_normal(const DevScene& S, const Nav& nv, Ray& r, int cur, int next) {
+  d3 normal = find_normal(S, nv);
+  int bi = find_border(S, cur, next);
+  if (bi < 0) return normal;
+  const rbg_border_desc B = S.borders[bi];
+  if (B.lambertian) return normal;
+  if (B.sigma == 0) return normal;
+  const double sigma = B.sigma;
+  const double f_max = fmin(1., 4. * sigma);
+  int tries = 0;
+  for (;;) {
+    double alpha;
+    for (;;) {
+      alpha = rng_gaus(r, sigma);
+      double u = f_max * rng_u(r);
+      if (!(u > sin(alpha) || alpha >= kPi / 2)) break;
+      if (++tries > RBG_ROUGH_MAX_TRIES) {
+        r.err |= ERR_BIT_CAP;
+        return normal;
+      }
+    }
+    double phi = 2 * kPi * rng_u(r);
+    double sa, ca, sp, cp;
+    sincos(alpha, &sa, &ca);
+    sincos(phi, &sp, &cp);
+    d3 facet = rotate_uz(mk(sa * cp, sa * sp, ca), normal);
+    if (dot(nv.d, facet) > 0.0) return facet;
+    if (++tries > RBG_ROUGH_MAX_TRIES) {
+      r.err |= ERR_BIT_CAP;
+      return normal;
+    }
+  }
+}
+
+// TGeoRotation(phi, theta, psi) in degrees applied to v
+RBG_D d3 euler_apply(double phi, double theta, double psi, d3 v) {
+  double sf, cf, st, ct, sp, cp;
+  sincos(phi * kD2R, &sf, &cf);
+  sincos(theta * kD2R, &st, &ct);
+  sincos(psi * kD2R, &sp, &cp);
+  double R0 = cp * cf - ct * sf * sp, R1 = -sp * cf - ct * sf * cp, R2 = st * sf;
+  double R3 = cp * sf + ct * cf * sp, R4 = -sp * sf + ct * cf * cp, R5 = -st * cf;
+  double R6 = sp * st, R7 = cp * st, R8 = ct;
+  return mk(R0 * v.x + R1 * v.y + R2 * v.z, R3 * v.x + R4 * v.y + R5 * v.z, R6 * v.x + R7 * v.y + R8 * v.z);
+}
+
+// DoReflection (:170-247); `normal` may be null (computed here)
+RBG_D void do_reflection(const DevScene& S, Nav& nv, Ray& r, double n1, double step, int cur, int next,
+                         const d3* normal) {
+  d3 n = normal ? *normal : get_facet_normal(S, nv, r, cur, next);
+  const d3 d1 = r.d;
+  double cos1 = dot(d1, n);
+  int bi = find_border(S, cur, next);
+  bool absorbed = false;
+  if (kind_of(S, next) == kMirror) {
+    double angle = acos(cos1);
+    double ref;
+    if (bi >= 0 && S.borders[bi].multilayer >= 0) {
+      double tr;
+      coherent_tmm_mixed(S, S.borders[bi].multilayer, angle, r.lambda, ref, tr);
+    } else {
+      const rbg_volume_desc& v = S.volumes[S.nodes[next].volume];
+      if (v.refl_table >= 0)
+        ref = S.tables[v.refl_table].kind == RBG_TABLE_2D ? table2d(S, v.refl_table, r.lambda, angle)
+                                                          : table1d(S, v.refl_table, r.lambda);
+      else
+        ref = v.reflectance;
+      ref = ref > 1 ? 1 : ref;
+      ref = ref < 0 ? 0 : ref;
+    }
+    if (ref < rng_u(r)) {
+      absorbed = true;
+      r.status = RBG_ABSORB;
+    }
+  }
+  d3 d2;
+  if (bi >= 0 && S.borders[bi].lambertian) {
+    double y = 0.5 * rng_u(r);
+    double theta = asin(sqrt(2 * y));
+    double phi = 2 * kPi * rng_u(r);
+    double th_n = (n.x == 0 && n.y == 0 && n.z == 0) ? 0 : atan2(sqrt(n.x * n.x + n.y * n.y), n.z);
+    double ph_n = (n.x == 0 && n.y == 0) ? 0 : atan2(n.y, n.x);
+    d3 v = mk(sin(theta) * cos(phi), sin(theta) * sin(phi), cos(theta));
+    d2 = euler_apply(ph_n / kD2R + 90, th_n / kD2R + 180, 0, v);
+  } else {
+    d2 = d1 - (2 * cos1) * n;
+  }
+  if (!absorbed) set_direction(r, d2);
+  double t = r.t + step / (RBG_SPEED_OF_LIGHT_CM / n1);
+  nv.p = nv.p - RBG_REFLECT_BACKSTEP * d1;
+  nv.node = locate_from_top(S, nv.p);
+  nv.d = d2;
+  add_point(r, nv.p, t);
+  add_node(r, next);
+}
+
+// DoFresnel (:52-167)
+RBG_D void do_fresnel(const DevScene& S, Nav& nv, Ray& r, double n1, double n2, double k2, double step, int cur,
+                      int next, bool disable_fresnel) {
+  d3 n = get_facet_normal(S, nv, r, cur, next);
+  const d3 d1 = r.d;
+  double cos1 = dot(d1, n);
+  double sin1 = sqrt(1 - cos1 * cos1);
+  double sin2 = n1 * sin1 / n2;
+  double cos2 = sqrt(1 - sin2 * sin2);
+  int bi = find_border(S, cur, next);
+  bool absorbed = false;
+  bool transmit = false;
+  if (bi >= 0 && S.borders[bi].multilayer >= 0) {
+    double refl, trans;
+    coherent_tmm_mixed(S, S.borders[bi].multilayer, acos(cos1), r.lambda, refl, trans);
+    double rnd = rng_u(r);
+    if (rnd < refl) {
+      do_reflection(S, nv, r, n1, step, cur, next, &n);
+      return;
+    }
+    absorbed = !(rnd < refl + trans);
+    transmit = true;
+  }
+  if (!transmit) {
+    if (sin2 > 1.) {
+      do_reflection(S, nv, r, n1, step, cur, next, &n);
+      return;
+    }
+    if (!disable_fresnel) {
+      double Rs, Rp;
+      if (k2 <= 0.) {
+        double eta1S = n1 * cos1, eta2S = n2 * cos2, eta1P = n1 / cos1, eta2P = n2 / cos2;
+        double a = (eta1S - eta2S) / (eta1S + eta2S), b = (eta1P - eta2P) / (eta1P + eta2P);
+        Rs = a * a;
+        Rp = b * b;
+      } else {
+        double x1S = n1 * cos1, x1P = n1 / cos1;
+        double u = n2 * n2 - k2 * k2 - (n1 * sin1) * (n1 * sin1);
+        double v = 2 * n2 * k2;
+        double tmp = sqrt(u * u + v * v);
+        double cosxi2 = sqrt(1 + u / tmp) / sqrt(2.0);
+        double sinxi2 = sqrt(1 - u / tmp) / sqrt(2.0);
+        double x2S = sqrt(tmp) * cosxi2, y2S = sqrt(tmp) * sinxi2;
+        tmp = x2S * x2S + y2S * y2S;
+        double x2P = (2 * n2 * k2 * y2S + (n2 * n2 - k2 * k2) * x2S) / tmp;
+        double y2P = (2 * n2 * k2 * x2S - (n2 * n2 - k2 * k2) * y2S) / tmp;
+        Rs = ((x1S - x2S) * (x1S - x2S) + y2S * y2S) / ((x1S + x2S) * (x1S + x2S) + y2S * y2S);
+        Rp = ((x1P - x2P) * (x1P - x2P) + y2P * y2P) / ((x1P + x2P) * (x1P + x2P) + y2P * y2P);
+      }
+      double R = (Rs + Rp) / 2.;
+      if (rng_u(r) < R) {
+        do_reflection(S, nv, r, n1, step, cur, next, &n);
+        return;
+      }
+    }
+  }
+  d3 d2 = sin1 != 0 ? (sin2 / sin1) * (d1 - cos1 * n) + cos2 * n : d1;
+  double t = r.t + step / (RBG_SPEED_OF_LIGHT_CM / n1);
+  add_point(r, nv.p, t);
+  add_node(r, next);
+  if (absorbed) {
+    r.status = RBG_ABSORB;
+  } else {
+    set_direction(r, d2);
+    nv.d = d2;
+  }
+}
+
+// TraceNonSequential(TObjArray*) body for one ray (:346-518)
+RBG_D void trace_ray(const DevScene& S, Ray& r, int limit, bool disable_fresnel) {
+  Nav nv;
+  nv.p = r.x;
+  nv.d = r.d;
+  nv.node = locate_from_top(S, nv.p);
+  nv.xnode = -1;
+  nv.xn = mk(0, 0, 1);
+  const double lambda = r.lambda;
+  while (r.status == RBG_RUN) {
+    const d3 x1 = r.x;
+    const double t1 = r.t;
+    const d3 d1 = r.d;
+    const int cur = nv.node;
+    double step;
+    const int next = find_next_boundary_and_step(S, nv, step, r.err);
+    const int tc = kind_of(S, cur), tn = kind_of(S, next);
+
+    if (tc == kLens) {
+      int idx = S.volumes[S.nodes[cur].volume].index;
+      double k = index_k(S, idx, lambda);
+      double abs_len = k <= 0. ? INFINITY : lambda / (4 * kPi * k);
+      if (abs_len > 0 && abs_len != INFINITY) {
+        double abs_step = -abs_len * log(1.0 - rng_u(r));
+        if (abs_step < step) {
+          double n1 = index_n(S, idx, lambda);
+          add_point(r, x1 + abs_step * d1, t1 + abs_step / (RBG_SPEED_OF_LIGHT_CM / n1));
+          add_node(r, next);
+          r.status = RBG_ABSORB;
+          continue;
+        }
+      }
+    }
+
+    if ((tc == kNull || tc == kOpt || tc == kLens || tc == kOther) && tn == kMirror) {
+      double n1 = tc == kLens ? lens_n(S, cur, lambda) : 1.;
+      do_reflection(S, nv, r, n1, step, cur, next, nullptr);
+    } else if ((tc == kNull || tc == kOpt || tc == kOther) && tn == kLens) {
+      int idx = S.volumes[S.nodes[next].volume].index;
+      do_fresnel(S, nv, r, 1, index_n(S, idx, lambda), index_k(S, idx, lambda), step, cur, next, disable_fresnel);
+    } else if ((tc == kNull || tc == kLens || tc == kOpt || tc == kOther) && (tn == kObs || tn == kFocus)) {
+      double speed = tc == kLens ? RBG_SPEED_OF_LIGHT_CM / lens_n(S, cur, lambda) : RBG_SPEED_OF_LIGHT_CM;
+      add_point(r, nv.p, t1 + step / speed);
+      add_node(r, next);
+    } else if ((tc == kNull || tc == kOpt || tc == kOther) && (tn == kOther || tn == kOpt)) {
+      add_point(r, nv.p, t1 + step / RBG_SPEED_OF_LIGHT_CM);
+      add_node(r, next);
+    } else if (tc == kLens && tn == kLens) {
+      int idx = S.volumes[S.nodes[next].volume].index;
+      do_fresnel(S, nv, r, lens_n(S, cur, lambda), index_n(S, idx, lambda), index_k(S, idx, lambda), step, cur,
+                 next, disable_fresnel);
+    } else if (tc == kLens && (tn == kNull || tn == kOpt || tn == kOther)) {
+      do_fresnel(S, nv, r, lens_n(S, cur, lambda), 1, 0, step, cur, next, disable_fresnel);
+    }
+
+    if (tn == kNull) {
+      add_point(r, nv.p, t1 + step / RBG_SPEED_OF_LIGHT_CM);
+      add_node(r, next);
+      r.status = RBG_EXIT;
+    } else if (tc == kFocus || tc == kObs || tc == kMirror || tn == kObs) {
+      r.status = RBG_STOP;
+    } else if (tn == kFocus) {
+      const rbg_volume_desc& v = S.volumes[S.nodes[next].volume];
+      double angle = 0.;
+      if (v.qe_angle_table >= 0) {
+        d3 n = get_facet_normal(S, nv, r, cur, next);
+        angle = acos(dot(r.d, n));
+      }
+      double qe = v.qe_lambda_table >= 0 ? table1d(S, v.qe_lambda_table, lambda) : 1.;
+      if (v.qe_angle_table >= 0) qe *= table1d(S, v.qe_angle_table, angle);
+      if (qe == 1 || rng_u(r) < qe) r.status = RBG_FOCUS;
+      else r.status = RBG_STOP;
+    }
+    if (r.status == RBG_RUN && r.npoints >= limit) r.status = RBG_SUSPEND;
+  }
+}
+
+}  // namespace rbg
