@@ -1,0 +1,272 @@
+"""Benchmark: AOpticsManager::TraceNonSequential on the Schwarzschild-Couder
+telescope (two 8-term AGeoAsphericDisk mirrors, 1e7 rays at 400 nm over
+0-4 deg field), one GB300.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+A step traces the whole 1e7-ray batch to termination.  `value` is rays/s
+with the batch already in HBM (inputs 640 MB > L2, so no L2 flush is
+needed); `e2e` is the same through the host-buffer C ABI call
+rbg_trace_host (host->device copy of the rays, trace, device->host copy of
+fates, points and directions inside the timed region).  The CPU baseline is
+the FP64 oracle (the restatement of the reference algorithm) on all host
+cores over a bounded sample.  With --impl reference only that CPU path runs.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+METRIC = "Mrays/s & grad-evals/s: chosen form vs plain GPU tracer at equal PSF d80 error"
+UNIT = "rays/s"
+N_RAYS = 10_000_000
+CPU_SAMPLE = 200_000
+# algorithmic bytes (per ray: 40 B in + 48 B out; per segment 52 B read + 52 B write)
+BYTES_PER_RAY = 88
+BYTES_PER_SEGMENT = 104
+
+
+def workload_config(n, precision):
+    return {"workload": "schwarzschild_couder", "rays": n, "field_deg": [0, 1, 2, 3, 4], "lambda_nm": 400,
+            "mirrors": "AGeoAsphericDisk x2, 8 coefficients, N(0,1e-3) rel perturbation",
+            "precision": precision, "l2": "inputs 640 MB > L2 (no flush)", "parallelism": "replicas"}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.rows = []
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, nm in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(man, batch, sample):
+    import oracle_ref
+
+    from robast_gb300 import configs
+
+    idx = np.linspace(0, len(batch["x"]) - 1, sample).astype(np.int64)
+    sub = {k: v[idx] for k, v in batch.items()}
+    arr = configs.to_array(sub)
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    st, _ = oracle_ref.trace(man, arr, threads=cores)
+    dt = time.perf_counter() - t0
+    return {"value": sample / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{sample} rays spread over the 1e7-ray batch (all 5 field angles), oracle FP64, "
+                      f"{cores} threads, contiguous chunks"}, st
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from robast_gb300 import build, configs
+
+    build.build_library()
+    build.build_oracle()
+    man, batch = configs.schwarzschild_couder(n_rays=N_RAYS)
+    sample = args.cpu_sample
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb, st = cpu_baseline(man, batch, sample)
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = float(np.median(vals))
+    cb["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sample / v * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": workload_config(N_RAYS, "fp64-cpu"), "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference = CPU FP64 restatement (ROOT, which the reference needs, is not installable)"}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--rays", type=int, default=N_RAYS)
+    ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from robast_gb300 import _native as N
+    from robast_gb300 import build, configs, device
+
+    build.build_library()
+    build.build_oracle()
+    prec = N.PREC_MIXED if args.precision == "mixed" else N.PREC_FP64
+    man, batch = configs.schwarzschild_couder(n_rays=args.rays)
+    man.ray_id_offset = rank * args.rays
+    n = args.rays
+    rays = device.to_device(batch, f"cuda:{local}")
+    res = device.alloc_result(n, f"cuda:{local}")
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        device.trace(man, rays, res, precision=prec)
+    torch.cuda.synchronize()
+    launches = N.lib().rbg_last_launch_count(man.scene.handle)
+    seg = int((res["npoints"].to(torch.int64) - 1).sum().item())
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            device.trace(man, rays, res, precision=prec)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if ws > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n * ws / (ms / 1e3)
+
+    # end to end through the host-buffer C ABI call
+    from robast_gb300.manager import make_result
+
+    arr = configs.to_array(batch)
+    pinned = {}
+    for f in ("x", "y", "z", "t", "dx", "dy", "dz", "lam"):
+        pt = torch.empty(n, dtype=torch.float64).pin_memory()
+        pt.numpy()[:] = getattr(arr, f)
+        pinned[f] = pt
+    dp = C.POINTER(C.c_double)
+    rs = N.Rays(n, *(C.cast(C.c_void_p(pinned[f].data_ptr()), dp) for f in ("x", "y", "z", "t", "dx", "dy",
+                                                                             "dz", "lam")))
+    host_out = {f: torch.empty(n, dtype=torch.float64).pin_memory() for f in ("x", "y", "z", "t", "dx", "dy",
+                                                                              "dz")}
+    host_out["status"] = torch.empty(n, dtype=torch.uint8).pin_memory()
+    host_out["npoints"] = torch.empty(n, dtype=torch.int32).pin_memory()
+    host_out["last_node"] = torch.empty(n, dtype=torch.int32).pin_memory()
+    rr = N.Result()
+    rr.status = C.cast(C.c_void_p(host_out["status"].data_ptr()), C.POINTER(C.c_uint8))
+    rr.npoints = C.cast(C.c_void_p(host_out["npoints"].data_ptr()), C.POINTER(C.c_int32))
+    rr.last_node = C.cast(C.c_void_p(host_out["last_node"].data_ptr()), C.POINTER(C.c_int32))
+    for f in ("x", "y", "z", "t", "dx", "dy", "dz"):
+        setattr(rr, f, C.cast(C.c_void_p(host_out[f].data_ptr()), dp))
+    opts = man.trace_options(prec)
+    N.lib().rbg_trace_host(man.scene.handle, C.byref(rs), C.byref(rr), C.byref(opts))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        N.lib().rbg_trace_host(man.scene.handle, C.byref(rs), C.byref(rr), C.byref(opts))
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    barrier()
+    e2e = {"value": n * ws / t_e2e, "unit": UNIT, "h2d_bytes_per_step": n * 8 * 8,
+           "d2h_bytes_per_step": n * (7 * 8 + 4 + 4 + 1)}
+
+    if rank != 0:
+        return
+    hbm, how = peaks()
+    alg_bytes = n * BYTES_PER_RAY + seg * BYTES_PER_SEGMENT
+    achieved = alg_bytes / (ms / 1e3) / 1e9
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if prec == N.PREC_FP64 else "f32+f64", "data": "synthetic",
+            "config": workload_config(n, args.precision), "gpu_launches": launches * args.steps,
+            "segments_per_step": seg,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None, "peak_source": how,
+                         "note": "algorithmic ray-state bytes; the kernel is FP64-pipe bound, see profiles/"},
+            "e2e": e2e, "clocks": clk.summary()}
+    cb, _ = cpu_baseline(man, batch, args.cpu_sample)
+    line["cpu_baseline"] = cb
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

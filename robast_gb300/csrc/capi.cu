@@ -170,8 +170,8 @@ int stack_ready() {
   static int done = 0;
   if (!done) {
     // the CSG walk and the rejection loops recurse/branch deeply: give each
-    // thread enough local stack for composite trees of depth <= 8
-    if (cudaDeviceSetLimit(cudaLimitStackSize, 4096) != cudaSuccess) return RBG_ERR_CUDA;
+    // thread enough local stack for composite trees of depth <= 6
+    if (cudaDeviceSetLimit(cudaLimitStackSize, 8192) != cudaSuccess) return RBG_ERR_CUDA;
     done = 1;
   }
   return RBG_OK;

@@ -21,6 +21,7 @@ constexpr int kMaxNodes = 1 << 24;
 constexpr int kMaxDepth = 64;
 constexpr int kBvhLeaf = 4;
 constexpr int kBvhMinChildren = 9;
+constexpr int kMaxCompositeDepth = 6;
 
 struct Box {
   double lo[3], hi[3];
@@ -151,6 +152,7 @@ struct Builder {
   const rbg_scene_desc* d;
   rbg_scene* s;
   std::vector<int> shape_state;  // 0 = todo, 1 = in progress, 2 = done
+  std::vector<int> composite_depth;
 
   int fail(int code) { return code; }
 
@@ -192,6 +194,7 @@ struct Builder {
         double phi1 = u.n_params >= 5 ? p[3] : 0.0, phi2 = u.n_params >= 5 ? p[4] : 360.0;
         if (rmin < 0 || rmax <= rmin) return RBG_ERR_SCENE;
         double dphi = phi2 - phi1;
+        if (!std::isfinite(dphi)) return RBG_ERR_SCENE;
         while (dphi <= 0) dphi += 360.0;
         q = {rmin, rmax, dz, phi1, dphi >= 360.0 ? 360.0 : dphi};
         b = {{-rmax, -rmax, -dz}, {rmax, rmax, dz}};
@@ -204,6 +207,7 @@ struct Builder {
         double ph1 = u.n_params >= 6 ? p[4] : 0.0, ph2 = u.n_params >= 6 ? p[5] : 360.0;
         if (rmin < 0 || rmax <= rmin || th1 < 0 || th2 > 180 || th2 <= th1) return RBG_ERR_SCENE;
         double dphi = ph2 - ph1;
+        if (!std::isfinite(dphi)) return RBG_ERR_SCENE;
         while (dphi <= 0) dphi += 360.0;
         q = {rmin, rmax, th1, th2, ph1, dphi >= 360.0 ? 360.0 : dphi};
         const double d2r = M_PI / 180.0;
@@ -327,6 +331,10 @@ struct Builder {
         int rc;
         if ((rc = canon_shape(u.left)) != RBG_OK) return rc;
         if ((rc = canon_shape(u.right)) != RBG_OK) return rc;
+        // the device walks composite trees recursively: bound their depth
+        int depth = 1 + std::max(composite_depth[u.left], composite_depth[u.right]);
+        if (depth > kMaxCompositeDepth) return RBG_ERR_UNSUPPORTED;
+        composite_depth[id] = depth;
         for (int opnd : {u.left, u.right}) {
           int t = d->shapes[opnd].type;
           if (t == RBG_SHAPE_ASPHERIC_DISK || t == RBG_SHAPE_WINSTON_POLY) return RBG_ERR_UNSUPPORTED;
@@ -515,6 +523,7 @@ struct Builder {
     s->shapes.assign(d->shapes, d->shapes + d->n_shapes);
     s->shape_box.assign(6 * (size_t)d->n_shapes, 0.0);
     shape_state.assign(d->n_shapes, 0);
+    composite_depth.assign(d->n_shapes, 0);
     int rc;
     for (int i = 0; i < d->n_shapes; ++i)
       if ((rc = canon_shape(i)) != RBG_OK) return rc;

@@ -1,0 +1,133 @@
+"""Device-resident tracing: ray batches held as CUDA tensors.
+
+PyTorch provides device memory and streams only; all work is done by the
+library's kernels through the C ABI (rbg_trace, rbg_focal_moments,
+rbg_focal_histogram, rbg_containment_radius).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import _native as N
+
+RAY_FIELDS = ("x", "y", "z", "t", "dx", "dy", "dz", "lam")
+OUT_F64 = ("x", "y", "z", "t", "dx", "dy", "dz")
+
+
+def _torch():
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("no CUDA device: the tracer has no CPU path")
+    return torch
+
+
+def _ptr(t) -> C.c_void_p:
+    return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
+
+
+def to_device(batch: Dict[str, np.ndarray], device="cuda:0") -> Dict[str, "object"]:
+    torch = _torch()
+    out = {}
+    n = len(batch["x"])
+    for f in RAY_FIELDS:
+        src = batch.get(f)
+        if src is None:
+            src = np.zeros(n)
+        out[f] = torch.as_tensor(np.ascontiguousarray(src, dtype=np.float64)).to(device)
+    if "group" in batch:
+        out["group"] = torch.as_tensor(np.ascontiguousarray(batch["group"], dtype=np.int32)).to(device)
+    return out
+
+
+def alloc_result(n: int, device="cuda:0", history: int = 0):
+    torch = _torch()
+    res = {f: torch.empty(n, dtype=torch.float64, device=device) for f in OUT_F64}
+    res["status"] = torch.empty(n, dtype=torch.uint8, device=device)
+    res["npoints"] = torch.empty(n, dtype=torch.int32, device=device)
+    res["last_node"] = torch.empty(n, dtype=torch.int32, device=device)
+    if history:
+        res["hist_xyzt"] = torch.empty((n, history, 4), dtype=torch.float64, device=device)
+        res["hist_node"] = torch.empty((n, history), dtype=torch.int32, device=device)
+    return res
+
+
+def _rays_struct(rays) -> N.Rays:
+    dp = C.POINTER(C.c_double)
+    n = rays["x"].numel()
+    ptrs = [C.cast(C.c_void_p(rays[f].data_ptr()), dp) for f in RAY_FIELDS]
+    return N.Rays(n, *ptrs)
+
+
+def _result_struct(res) -> N.Result:
+    dp = C.POINTER(C.c_double)
+    ip = C.POINTER(C.c_int32)
+    r = N.Result()
+    r.status = C.cast(C.c_void_p(res["status"].data_ptr()), C.POINTER(C.c_uint8)) if "status" in res else None
+    r.npoints = C.cast(C.c_void_p(res["npoints"].data_ptr()), ip) if "npoints" in res else None
+    r.last_node = C.cast(C.c_void_p(res["last_node"].data_ptr()), ip) if "last_node" in res else None
+    for f in OUT_F64:
+        setattr(r, f, C.cast(C.c_void_p(res[f].data_ptr()), dp) if f in res else None)
+    if "hist_xyzt" in res:
+        r.hist_cap = res["hist_xyzt"].shape[1]
+        r.hist_xyzt = C.cast(C.c_void_p(res["hist_xyzt"].data_ptr()), dp)
+        r.hist_node = C.cast(C.c_void_p(res["hist_node"].data_ptr()), ip)
+    else:
+        r.hist_cap = 0
+    return r
+
+
+def trace(manager, rays, res=None, precision: Optional[int] = None, stream=None, check: bool = True):
+    """AOpticsManager::TraceNonSequential on device tensors; returns the
+    result dict and the C status."""
+    torch = _torch()
+    scene = manager._ensure_scene()
+    n = rays["x"].numel()
+    if res is None:
+        res = alloc_result(n, rays["x"].device)
+    rs = _rays_struct(rays)
+    rr = _result_struct(res)
+    opts = manager.trace_options(precision)
+    st_ptr = (stream if stream is not None else torch.cuda.current_stream()).cuda_stream
+    status = N.lib().rbg_trace(scene.handle, C.byref(rs), C.byref(rr), C.byref(opts), C.c_void_p(st_ptr))
+    if check and status not in (N.RBG_OK, N.RBG_ERR_CAP):
+        N.check(status, "rbg_trace")
+    return res, status
+
+
+def focal_moments(res, group=None, n_groups: int = 1, stream=None):
+    """(count, sum x, sum y, sum x^2, sum y^2, sum t) of focused rays per group."""
+    torch = _torch()
+    n = res["x"].numel()
+    sums = torch.zeros((n_groups, 6), dtype=torch.float64, device=res["x"].device)
+    st = (stream if stream is not None else torch.cuda.current_stream()).cuda_stream
+    N.check(N.lib().rbg_focal_moments(n, _ptr(res["status"]), _ptr(res["x"]), _ptr(res["y"]), _ptr(res["t"]),
+                                      _ptr(group), n_groups, _ptr(sums), C.c_void_p(st)), "rbg_focal_moments")
+    return sums
+
+
+def focal_histogram(res, nx, xlo, xhi, ny, ylo, yhi, mask=None, stream=None):
+    torch = _torch()
+    status = res["status"]
+    if mask is not None:
+        status = torch.where(mask, status, torch.zeros_like(status))
+    counts = torch.zeros((nx, ny), dtype=torch.float64, device=res["x"].device)
+    st = (stream if stream is not None else torch.cuda.current_stream()).cuda_stream
+    N.check(N.lib().rbg_focal_histogram(res["x"].numel(), _ptr(status), _ptr(res["x"]), _ptr(res["y"]), nx, xlo,
+                                        xhi, ny, ylo, yhi, _ptr(counts), C.c_void_p(st)), "rbg_focal_histogram")
+    return counts
+
+
+def containment_radius(counts, xlo, xhi, ylo, yhi, fraction=0.8, stream=None):
+    """AGeoUtil::ContainmentRadius of a device histogram -> (r, x, y)."""
+    torch = _torch()
+    counts = counts.contiguous()
+    nx, ny = counts.shape
+    r, x, y = C.c_double(), C.c_double(), C.c_double()
+    st = (stream if stream is not None else torch.cuda.current_stream()).cuda_stream
+    N.check(N.lib().rbg_containment_radius(_ptr(counts), nx, xlo, xhi, ny, ylo, yhi, fraction, C.byref(r),
+                                           C.byref(x), C.byref(y), C.c_void_p(st)), "rbg_containment_radius")
+    return r.value, x.value, y.value

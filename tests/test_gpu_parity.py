@@ -1,0 +1,79 @@
+"""GPU tracer vs CPU FP64 oracle on the same seeded rays (parity gate).
+
+Deterministic optics (no roughness / Fresnel / absorption draws) must give
+identical fates, point counts and last nodes; final positions and
+directions agree to 1e-6 relative (the oracle and the GPU run the same
+FP64 algorithm, differing only by rounding and FMA contraction).  The
+random draws are Philox keyed by (seed, ray id, draw number) in both, so
+stochastic scenes are compared ray by ray too, with a small allowance for
+rays whose draw sequence forks on a last-ulp difference.
+"""
+import numpy as np
+import pytest
+
+import oracle_ref
+from robast_gb300 import configs
+
+pytestmark = pytest.mark.gpu
+
+POS_RTOL = 1e-6
+
+
+def _gpu_trace(man, batch, precision=None, history=0):
+    import torch
+
+    from robast_gb300 import device
+
+    rays = device.to_device(batch, "cuda:0")
+    res = device.alloc_result(len(batch["x"]), "cuda:0", history)
+    res, st = device.trace(man, rays, res, precision=precision)
+    torch.cuda.synchronize()
+    return st, {k: v.cpu().numpy() for k, v in res.items()}
+
+
+def compare(gpu, ref, min_agree=0.9999, pos_rtol=POS_RTOL):
+    same = (gpu["status"] == ref["status"]) & (gpu["npoints"] == ref["npoints"]) & \
+           (gpu["last_node"] == ref["last_node"])
+    assert same.mean() >= min_agree, f"fate agreement {same.mean():.6f}"
+    for k in ("x", "y", "z"):
+        scale = np.maximum(1.0, np.abs(ref[k][same]))
+        err = np.abs(gpu[k][same] - ref[k][same]) / scale
+        assert err.max(initial=0) <= pos_rtol, (k, err.max())
+    for k in ("dx", "dy", "dz"):
+        err = np.abs(gpu[k][same] - ref[k][same])
+        assert err.max(initial=0) <= pos_rtol, (k, err.max())
+    return same
+
+
+@pytest.mark.parametrize("n", [0, 1, 7, 20000])
+def test_paraboloid_parity(n):
+    man, batch = configs.paraboloid(n_rays=max(n, 4), seed=11)
+    if n < 4:
+        batch = {k: v[:n] for k, v in batch.items()}
+    st, gpu = _gpu_trace(man, batch)
+    assert st == 0
+    ost, ref = oracle_ref.trace(man, configs.to_array(batch), threads=8)
+    assert ost == 0
+    if n:
+        compare(gpu, ref)
+
+
+def test_schwarzschild_couder_parity():
+    man, batch = configs.schwarzschild_couder(n_rays=20000, seed=5)
+    st, gpu = _gpu_trace(man, batch)
+    assert st == 0
+    ost, ref = oracle_ref.trace(man, configs.to_array(batch), threads=8)
+    assert ost == 0
+    compare(gpu, ref)
+    assert (gpu["status"] == 3).sum() > 5000
+
+
+def test_history_parity():
+    """Full point/node histories agree point by point."""
+    man, batch = configs.paraboloid(n_rays=2000, seed=12)
+    st, gpu = _gpu_trace(man, batch, history=8)
+    assert st == 0
+    ost, ref = oracle_ref.trace(man, configs.to_array(batch), threads=4, history=8)
+    same = compare(gpu, ref)
+    assert (gpu["hist_node"][same] == ref["hist_node"][same]).all()
+    np.testing.assert_allclose(gpu["hist_xyzt"][same], ref["hist_xyzt"][same], rtol=1e-9, atol=1e-7)
