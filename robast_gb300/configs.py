@@ -161,3 +161,260 @@ def plate_scale_sc():
     """cm on the focal surface per degree of field (10 cm per degree for OS2
     as used by tutorials/SchwarzschildCouder.C:148)."""
     return 10 * cm
+
+
+# ---------------------------------------------------------------------------
+# 2. Davies-Cotton (tutorials/DaviesCotton.C:30-160)
+# ---------------------------------------------------------------------------
+def _hex_lattice(pitch, n):
+    """The n hexagonal-lattice sites nearest the origin (flat-to-flat pitch)."""
+    k = int(math.ceil(math.sqrt(n))) + 4
+    pts = []
+    for i in range(-k, k + 1):
+        for j in range(-k, k + 1):
+            x = pitch * (i + 0.5 * j)
+            y = pitch * (math.sqrt(3) / 2.0) * j
+            pts.append((x * x + y * y, x, y))
+    pts.sort()
+    return [(x, y) for _, x, y in pts[:n]]
+
+
+def davies_cotton(n_rays: int = 10_000_000, n_angles: int = 11, max_angle: float = 2.5, seed: int = 2,
+                  n_facets: int = 380, tilt_sigma: float = 0.5e-3, roughness: float = 1e-3):
+    F = 15 * m
+    Rc = 2 * F
+    D = 60 * cm  # facet flat-to-flat
+    T = 0.1 * mm
+    rng = np.random.default_rng(seed)
+    man = AOpticsManager("manager", "Davies-Cotton System")
+    man.DisableFresnelReflection(True)
+    world = AOpticalComponent("world", TGeoBBox("boxWorld", 20 * m, 20 * m, 20 * m))
+    man.SetTopVolume(world)
+    # facet: spherical shell cap intersected with a hexagonal prism
+    mir_cut = TGeoPgon("mirCut", 0., 360., 6, 2)
+    mir_cut.DefineSection(0, -100 * mm, 0, D / 2.)
+    mir_cut.DefineSection(1, 100 * mm, 0, D / 2.)
+    theta = math.degrees(math.asin(D / math.sqrt(3) / Rc))
+    TGeoSphere("mirSphere", Rc, Rc + T, 180. - theta, 180.)
+    TGeoTranslation("transZ", 0, 0, Rc).RegisterYourself()
+    comp = TGeoCompositeShape("mirComposite", "mirSphere:transZ*mirCut")
+    mirror = AMirror("mirror", comp)
+    mirror.SetReflectance(0.85)
+    cond = ABorderSurfaceCondition(world, mirror)
+    cond.SetGaussianRoughness(roughness)
+    for i, (x, y) in enumerate(_hex_lattice(D, n_facets)):
+        r2 = x * x + y * y
+        z = F - math.sqrt(F * F - r2)
+        phi = math.degrees(math.atan2(y, x))
+        rot = TGeoRotation(f"mirRot{i}", -phi + 90., 0, 0)
+        th = math.degrees(math.atan2(math.sqrt(r2), 2 * F - z))
+        rot2 = TGeoRotation("", phi - 90., th, 0)
+        rot.MultiplyBy(rot2, False)
+        # per-facet alignment error
+        err = TGeoRotation("", 0, 0, 0)
+        err.RotateX(math.degrees(tilt_sigma * rng.standard_normal()))
+        err.RotateY(math.degrees(tilt_sigma * rng.standard_normal()))
+        rot.MultiplyBy(err, True)
+        world.AddNode(mirror, i + 1, TGeoCombiTrans(TGeoTranslation(x, y, z), rot))
+    # focal plane 1.5 m across and an open-bottom camera box around it
+    focal = AFocalSurface("focalPlane", TGeoTube("tubeCamera", 0, 75 * cm, 1 * mm))
+    world.AddNode(focal, 1, TGeoTranslation(0, 0, F + 1 * mm))
+    box_d, box_h, t = 1.7 * m, 1 * m, 10 * cm
+    TGeoBBox("boxCamera", box_d / 2., box_d / 2., box_h / 2.)
+    TGeoBBox("boxCamera2", box_d / 2. - t, box_d / 2. - t, box_h / 2. - t)
+    TGeoTranslation("transZ1", 0, 0, F + box_h / 2.).RegisterYourself()
+    TGeoTranslation("transZ2", 0, 0, F + box_h / 2. - t - 1 * mm).RegisterYourself()
+    camera = AObscuration("cameraBox", TGeoCompositeShape("boxComposite", "boxCamera:transZ1-boxCamera2:transZ2"))
+    world.AddNode(camera, 1)
+    man.CloseGeometry()
+    angles = np.linspace(0.0, max_angle, n_angles)
+    batches = []
+    for g, (a, n) in enumerate(zip(angles, _split(n_rays, n_angles))):
+        r = a * deg
+        tr = TGeoTranslation(-2 * F * math.sin(r), 0, 2 * F * math.cos(r))
+        rot = TGeoRotation("", -90.0, a, 90.0)
+        arr = ARayShooter.RandomCircle(400 * nm, 6.2 * m, n, rot, tr, (0.0, 0.0, -1.0), seed=seed * 1000 + g)
+        b = _batch(arr, g)
+        b["lam"] = np.random.default_rng(seed * 7919 + g).uniform(300 * nm, 600 * nm, n)
+        batches.append(b)
+    return man, _concat(batches)
+
+
+# ---------------------------------------------------------------------------
+# 4. light guide: 7x7 hexagonal Winston cones behind a window
+# ---------------------------------------------------------------------------
+SELLMEIER_WINDOW = (1.04, 0.23, 1.01, 0.0060, 0.020, 103.6)
+
+
+def _light_guide_unit(world, tag, origin, r1, r2, window_index, reflectance, gap=1 * mm):
+    """One 7x7 cone array + window, entrance plane at origin z."""
+    cone = AGeoWinstonConePoly(f"cone{tag}", r1, r2, 6)
+    dz = cone.GetDZ()
+    pitch = 2 * r1
+    # rows of 7 hexagons, alternate rows offset by half a pitch
+    centres = [(pitch * (i + 0.5 * (j % 2)), pitch * (math.sqrt(3) / 2.0) * j) for i in range(7) for j in range(7)]
+    cx = np.mean([c[0] for c in centres])
+    cy = np.mean([c[1] for c in centres])
+    centres = [(x - cx, y - cy) for x, y in centres]
+    half = max(max(abs(x), abs(y)) for x, y in centres) + 2 * r1
+    ox, oy, oz = origin
+    block = AMirror(f"block{tag}", TGeoBBox(f"blockbox{tag}", half, half, dz))
+    block.SetReflectance(reflectance)
+    interior = AOpticalComponent(f"guide{tag}", cone)
+    for k, (x, y) in enumerate(centres):
+        block.AddNode(interior, k + 1, TGeoTranslation(x, y, 0))
+    world.AddNode(block, 1, TGeoTranslation(ox, oy, oz - dz))
+    window = ALens(f"window{tag}", TGeoBBox(f"windowbox{tag}", half, half, 0.25 * cm))
+    window.SetRefractiveIndex(window_index)
+    world.AddNode(window, 1, TGeoTranslation(ox, oy, oz + gap + 0.25 * cm))
+    sensor = AFocalSurface(f"sensor{tag}", TGeoBBox(f"sensorbox{tag}", half, half, 0.05 * mm))
+    world.AddNode(sensor, 1, TGeoTranslation(ox, oy, oz - 2 * dz - 0.05 * mm))
+    return half
+
+
+def light_guide(n_rays: int = 10_000_000, n_variants: int = 64, max_angle: float = 40.0, seed: int = 4):
+    """64 variants of (entrance, exit) apothem around 25 mm / 12.5 mm, each a
+    full 7x7 array + 5 mm window; the cone length follows from r1, r2
+    (AGeoWinstonConePoly::SetWinstonDimensions)."""
+    man = AOpticsManager("manager", "light guide")
+    world = AOpticalComponent("world", TGeoBBox("worldbox", 20 * m, 20 * m, 5 * m))
+    man.SetTopVolume(world)
+    idx = ASellmeierFormula(*SELLMEIER_WINDOW)
+    k = TGraph()
+    for i, wl in enumerate((250 * nm, 700 * nm)):  # absorption length 1 m: k = lambda / (4 pi 100 cm)
+        k.SetPoint(i, wl, ARefractiveIndex.AbsorptionLengthToExtinctionCoefficient(1 * m, wl))
+    idx.SetExtinctionCoefficient(k)
+    side = int(math.ceil(math.sqrt(n_variants)))
+    spacing = 60 * cm
+    rng = np.random.default_rng(seed)
+    units = []
+    for v in range(n_variants):
+        r1 = 2.5 * cm * (1 + 0.1 * ((v % 8) - 3.5) / 3.5)
+        r2 = 1.25 * cm * (1 + 0.1 * ((v // 8) - 3.5) / 3.5)
+        origin = (spacing * (v % side - (side - 1) / 2), spacing * (v // side - (side - 1) / 2), 0.0)
+        half = _light_guide_unit(world, v, origin, r1, r2, idx, 0.9)
+        units.append((origin, half))
+    man.CloseGeometry()
+    batches = []
+    for v, n in enumerate(_split(n_rays, n_variants)):
+        (ox, oy, oz), half = units[v]
+        gen = np.random.default_rng(seed * 100003 + v)
+        th = np.radians(gen.uniform(0, max_angle, n))
+        ph = gen.uniform(0, 2 * np.pi, n)
+        d = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), -np.cos(th)], axis=-1)
+        # aim at a uniform point on the window top, start 3 cm above it
+        tx = ox + gen.uniform(-0.9, 0.9, n) * half
+        ty = oy + gen.uniform(-0.9, 0.9, n) * half
+        tz = oz + 1 * mm + 0.5 * cm
+        s = 3 * cm / np.cos(th)
+        b = {"x": tx - s * d[:, 0], "y": ty - s * d[:, 1], "z": tz - s * d[:, 2], "dx": d[:, 0], "dy": d[:, 1],
+             "dz": d[:, 2], "lam": gen.uniform(300 * nm, 600 * nm, n), "group": np.full(n, v, dtype=np.int32)}
+        batches.append(b)
+    return man, _concat(batches)
+
+
+# ---------------------------------------------------------------------------
+# 5. Schmidt-Cassegrain (tutorials/SchmidtCassegrain.C:39-110 prescription,
+#    scaled from a 24-inch to a 2-m primary), 20-layer quarter-wave coating
+# ---------------------------------------------------------------------------
+LITHOSIL_Q = (0.670710810, 0.433322857, 0.877379057, 0.00449192312, 0.0132812976, 95.8899878)
+INCH = 2.54 * cm
+
+
+def _quarter_wave_stack(air, substrate, n_pairs=10, lam0=450 * nm, nh=2.4, nl=1.46):
+    hi, lo = ARefractiveIndex(nh), ARefractiveIndex(nl)
+    ml = AMultilayer(air, substrate)
+    for _ in range(n_pairs):
+        ml.InsertLayer(hi, lam0 / 4 / nh)
+        ml.InsertLayer(lo, lam0 / 4 / nl)
+    return ml
+
+
+def _sct_unit(world, tag, origin, corrector_index, coating, decenter=(0.0, 0.0), tilt=(0.0, 0.0)):
+    s = 100 * cm / (12.183 * INCH)  # 2-m primary
+    off = 10 * cm
+    ox, oy, oz = origin
+
+    def tr(x, y, z):
+        return TGeoTranslation(ox + x, oy + y, oz + z)
+
+    # corrector: flat entrance, aspheric exit (polynomial in r^4.., scaled)
+    c2 = -8.721454939626e-05 / INCH / s
+    k = [0.0, 3.68090959e-7 / INCH ** 3 / s ** 3, 2.73643352e-11 / INCH ** 5 / s ** 5,
+         3.20036892e-14 / INCH ** 7 / s ** 7]
+    disk = AGeoAsphericDisk(f"corr{tag}", off * s, 0.0, (0.65 * INCH + off) * s, c2, 12 * INCH * s, 0.0)
+    disk.SetPolynomials(0, [], 4, k)
+    lens = ALens(f"corrector{tag}", disk)
+    lens.SetRefractiveIndex(corrector_index)
+    world.AddNode(lens, 1, tr(0, 0, 0))
+    z_mid = 0.5 * (off * s + (0.65 * INCH + off) * s)
+    half = 0.5 * 0.65 * INCH * s + 0.1 * mm
+    ap = AObscuration(f"aperture{tag}", TGeoTube(f"aptube{tag}", 12 * INCH * s, 18 * INCH * s, half))
+    world.AddNode(ap, 1, tr(0, 0, z_mid))
+    # primary (concave, hole of 4 inch scaled)
+    zp = ((0.65 + 40. + 32.) * INCH + off) * s
+    cp = -1.049567394559e-002 / INCH / s
+    pdisk = AGeoAsphericDisk(f"prim{tag}", zp, cp, zp + 0.1 * INCH * s, cp, 12.183 * INCH * s, 4 * INCH * s)
+    pdisk.SetConicConstants(0.077235, 0.077235)
+    primary = AMirror(f"primary{tag}", pdisk)
+    world.AddNode(primary, 1, tr(0, 0, 0))
+    # secondary (convex), with misalignment about its vertex
+    zs = ((0.65 + 40. + 32. - 30.86635) * INCH + off) * s
+    cs = -2.01270013787e-002 / INCH / s
+    sdisk = AGeoAsphericDisk(f"sec{tag}", zs - 0.1 * INCH * s, cs, zs, cs, 4.322385947053 * INCH * s, 0)
+    secondary = AMirror(f"secondary{tag}", sdisk)
+    rot = TGeoRotation("", 0, 0, 0)
+    rot.RotateX(math.degrees(tilt[0]))
+    rot.RotateY(math.degrees(tilt[1]))
+    c = np.array([0.0, 0.0, zs])
+    t = c - rot.R @ c + np.array([decenter[0], decenter[1], 0.0]) + np.array([ox, oy, oz])
+    world.AddNode(secondary, 1, TGeoCombiTrans(t[0], t[1], t[2], rot))
+    # focal screen behind the primary
+    zf = ((0.65 + 40. + 32. - 30.86635 + 50.6706488) * INCH + off) * s
+    screen = AFocalSurface(f"screen{tag}", TGeoBBox(f"screenbox{tag}", 5 * INCH * s, 5 * INCH * s, 5 * um))
+    world.AddNode(screen, 1, tr(0, 0, zf + 5 * um))
+    for mir in (primary, secondary):
+        cond = ABorderSurfaceCondition(world, mir)
+        cond.SetMultilayer(coating)
+    return 12 * INCH * s, off * s
+
+
+def schmidt_cassegrain(n_rays: int = 100_000_000, n_samples: int = 256, seed: int = 5,
+                       decenter_sigma: float = 0.02 * cm, tilt_sigma: float = 0.1e-3):
+    man = AOpticsManager("manager", "Schmidt-Cassegrain")
+    man.DisableFresnelReflection(True)
+    side = int(math.ceil(math.sqrt(n_samples)))
+    spacing = 3.2 * m
+    half_world = max(20 * m, spacing * side / 2 + 3 * m)
+    world = AOpticalComponent("world", TGeoBBox("worldbox", half_world, half_world, 10 * m))
+    man.SetTopVolume(world)
+    air = ARefractiveIndex(1.0, 0.0)
+    silica = ASellmeierFormula(*LITHOSIL_Q)
+    coating = _quarter_wave_stack(air, silica)
+    rng = np.random.default_rng(seed)
+    units = []
+    for v in range(n_samples):
+        origin = (spacing * (v % side - (side - 1) / 2), spacing * (v // side - (side - 1) / 2), 0.0)
+        dec = tuple(decenter_sigma * rng.standard_normal(2))
+        tilt = tuple(tilt_sigma * rng.standard_normal(2))
+        rap, zc = _sct_unit(world, v, origin, silica, coating, dec, tilt)
+        units.append((origin, rap, zc))
+    man.CloseGeometry()
+    batches = []
+    for v, n in enumerate(_split(n_rays, n_samples)):
+        (ox, oy, oz), rap, zc = units[v]
+        tr = TGeoTranslation(ox, oy, oz + zc - 20 * cm)
+        arr = ARayShooter.RandomCircle(450 * nm, rap * 0.98, n, None, tr, (0.0, 0.0, 1.0), seed=seed * 100003 + v)
+        b = _batch(arr, v)
+        b["lam"] = np.random.default_rng(seed * 7 + v).uniform(350 * nm, 650 * nm, n)
+        batches.append(b)
+    return man, _concat(batches)
+
+
+CONFIGS = {
+    "paraboloid": paraboloid,
+    "davies_cotton": davies_cotton,
+    "schwarzschild_couder": schwarzschild_couder,
+    "light_guide": light_guide,
+    "schmidt_cassegrain": schmidt_cassegrain,
+}

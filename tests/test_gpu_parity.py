@@ -75,5 +75,29 @@ def test_history_parity():
     assert st == 0
     ost, ref = oracle_ref.trace(man, configs.to_array(batch), threads=4, history=8)
     same = compare(gpu, ref)
-    assert (gpu["hist_node"][same] == ref["hist_node"][same]).all()
-    np.testing.assert_allclose(gpu["hist_xyzt"][same], ref["hist_xyzt"][same], rtol=1e-9, atol=1e-7)
+    # slots past npoints are never written
+    valid = np.arange(8)[None, :] < np.minimum(ref["npoints"], 8)[:, None]
+    valid &= same[:, None]
+    assert (gpu["hist_node"][valid] == ref["hist_node"][valid]).all()
+    np.testing.assert_allclose(gpu["hist_xyzt"][valid], ref["hist_xyzt"][valid], rtol=1e-9, atol=1e-7)
+
+
+@pytest.mark.parametrize("name,kw", [
+    ("davies_cotton", dict(n_rays=22000)),
+    ("light_guide", dict(n_rays=16000, n_variants=4)),
+    ("schmidt_cassegrain", dict(n_rays=16000, n_samples=4)),
+])
+def test_config_parity(name, kw):
+    """Stochastic configs (roughness, Fresnel, absorption, TMM draws): the
+    Philox streams are identical, so rays agree one by one unless a draw
+    comparison flips on a last-ulp difference."""
+    man, batch = configs.CONFIGS[name](**kw)
+    st, gpu = _gpu_trace(man, batch)
+    assert st == 0
+    ost, ref = oracle_ref.trace(man, configs.to_array(batch), threads=8)
+    assert ost == 0
+    compare(gpu, ref, min_agree=0.999)
+    # the fate histograms agree closely as well
+    g = np.bincount(gpu["status"], minlength=6)
+    r = np.bincount(ref["status"], minlength=6)
+    assert np.abs(g - r).max() <= max(5, 0.002 * len(batch["x"]))
