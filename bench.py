@@ -157,7 +157,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--rays", type=int, default=N_RAYS)
     ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE)
     args = ap.parse_args()
@@ -191,29 +192,58 @@ def main():
 
             dist.barrier()
 
-    for _ in range(args.warmup):
-        device.trace(man, rays, res, precision=prec)
-    torch.cuda.synchronize()
-    launches = N.lib().rbg_last_launch_count(man.scene.handle)
-    seg = int((res["npoints"].to(torch.int64) - 1).sum().item())
-    barrier()
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        ev0.record(stream)
-        for _ in range(args.steps):
-            device.trace(man, rays, res, precision=prec)
-        ev1.record(stream)
+    def timed(p, out):
+        for _ in range(args.warmup):
+            device.trace(man, rays, out, precision=p)
         torch.cuda.synchronize()
-    barrier()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if ws > 1:
-        import torch.distributed as dist
+        nl = N.lib().rbg_last_launch_count(man.scene.handle)
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as ck:
+            e0.record(stream)
+            for _ in range(args.steps):
+                device.trace(man, rays, out, precision=p)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        barrier()
+        t = e0.elapsed_time(e1) / args.steps
+        if ws > 1:
+            import torch.distributed as dist
 
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+            tt = torch.tensor([t], device=f"cuda:{local}")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            t = float(tt.item())
+        return t, nl, ck.summary()
+
+    ms, launches, clocks = timed(prec, res)
+    seg = int((res["npoints"].to(torch.int64) - 1).sum().item())
     value = n * ws / (ms / 1e3)
+    group = rays["group"]
+    n_groups = int(batch["group"].max()) + 1
+    compare = None
+    if not args.no_compare and prec != N.PREC_FP64:
+        res64 = device.alloc_result(n, f"cuda:{local}")
+        ms64, _, _ = timed(N.PREC_FP64, res64)
+        agree = float((res64["status"] == res["status"]).double().mean().item())
+        d80 = {"chosen": [], "fp64": []}
+        mom = device.focal_moments(res64, group, n_groups).cpu().numpy()
+        for g in range(n_groups):
+            cnt = mom[g, 0]
+            if cnt < 10:
+                continue
+            mx, my = mom[g, 1] / cnt, mom[g, 2] / cnt
+            sd = max(np.sqrt(max(mom[g, 3] / cnt - mx * mx, 0) + max(mom[g, 4] / cnt - my * my, 0)), 1e-6)
+            hw = 6 * sd
+            for key, rr in (("chosen", res), ("fp64", res64)):
+                h = device.focal_histogram(rr, 500, mx - hw, mx + hw, 500, my - hw, my + hw, mask=group == g)
+                d80[key].append(device.containment_radius(h, mx - hw, mx + hw, my - hw, my + hw, 0.8)[0])
+        rel = [abs(a - b) / b for a, b in zip(d80["chosen"], d80["fp64"]) if b > 0]
+        compare = {"plain_fp64_rays_per_s": n * ws / (ms64 / 1e3), "plain_fp64_ms_per_step": ms64,
+                   "speedup_vs_plain_fp64": ms64 / ms, "fate_agreement": agree,
+                   "d80_cm_chosen": d80["chosen"], "d80_cm_fp64": d80["fp64"],
+                   "d80_max_rel_diff": max(rel) if rel else None}
+        del res64
 
     # end to end through the host-buffer C ABI call
     from robast_gb300.manager import make_result
@@ -262,7 +292,7 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": None, "peak_source": how,
                          "note": "algorithmic ray-state bytes; the kernel is FP64-pipe bound, see profiles/"},
-            "e2e": e2e, "clocks": clk.summary()}
+            "e2e": e2e, "clocks": clocks, "vs_plain_fp64": compare}
     cb, _ = cpu_baseline(man, batch, args.cpu_sample)
     line["cpu_baseline"] = cb
     print(json.dumps(line))

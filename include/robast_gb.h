@@ -339,6 +339,42 @@ int rbg_containment_radius(const double* counts, int32_t nx, double xlo,
                            double fraction, double* r, double* x, double* y,
                            void* stream);
 
+/* ---- gradients ---------------------------------------------------------- */
+/* Parameters the adjoint differentiates.  Shifts and rotations are small
+ * rigid motions of a physical node applied in the master frame (the
+ * derivative is taken at zero motion); coefficients are the polynomial
+ * terms K_j of an AGeoAsphericDisk (SetPolynomials, src/AGeoAsphericDisk.cxx:
+ * 1187-1204), on its lower (bit 0) and/or upper (bit 1) surface. */
+enum {
+  RBG_ADJ_ASPH_COEF = 1,   /* node, index = j, faces = bit mask */
+  RBG_ADJ_NODE_SHIFT = 2,  /* node, index = master axis 0..2 */
+  RBG_ADJ_NODE_ROTATE = 3  /* node, index = master axis 0..2, about pivot */
+};
+typedef struct {
+  int32_t kind;
+  int32_t node;
+  int32_t index;
+  int32_t faces;
+  double pivot[3];
+} rbg_adjoint_param;
+
+/* Reverse-mode derivative of the final ray points (no counterpart in ROBAST,
+ * which has no gradients: replaces the finite-difference Minuit scans of
+ * tutorials/Optimize.C:60-205).  `fwd` is the DEVICE result of a trace of
+ * the same rays with a point/node history (hist_cap >= the points of every
+ * contributing ray); dL_dx/dy/dz are DEVICE cotangents of each ray's final
+ * point (NULL = 0).  Accumulates (+=) into the DEVICE array dL_dparams:
+ *   dL/dp_k = sum_i dL/dx_i . dx_i/dp_k
+ * Segments are recomputed from the recorded hit points; reflections and
+ * surface intersections are differentiated (implicit-function rule at each
+ * hit, mirror-normal curvature included).  Rays whose path refracts are
+ * skipped and counted in *n_skipped (host, may be NULL). */
+int rbg_trace_adjoint(rbg_scene* scene, int64_t n, const rbg_result* fwd,
+                      const double* dL_dx, const double* dL_dy,
+                      const double* dL_dz, int32_t n_params,
+                      const rbg_adjoint_param* params, double* dL_dparams,
+                      int64_t* n_skipped, void* stream);
+
 /* ---- ray sources -------------------------------------------------------- */
 /* ARayShooter generators (include/ARayShooter.h:25-51,
  * src/ARayShooter.cxx:122-459) writing HOST arrays: the x, y, z, t, dx, dy,

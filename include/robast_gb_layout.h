@@ -77,7 +77,13 @@
 #define RBG_ASPH_ORIGIN_Z 10
 #define RBG_ASPH_DZ 11
 #define RBG_ASPH_RSEG 12
-#define RBG_ASPH_K 13
+/* CalcF1/CalcF2 at rmin and rmax (the wall z ranges of DistToInner/Outer,
+ * src/AGeoAsphericDisk.cxx:556-557,633-634); NaN where the sag is undefined */
+#define RBG_ASPH_F1RMIN 13
+#define RBG_ASPH_F2RMIN 14
+#define RBG_ASPH_F1RMAX 15
+#define RBG_ASPH_F2RMAX 16
+#define RBG_ASPH_K 17
 #define RBG_ASPH_MAXPOL 16
 
 /* WINSTON_POLY (AGeoWinstonConePoly) */

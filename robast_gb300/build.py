@@ -24,7 +24,7 @@ ORACLE = os.path.join(ROOT, "oracle")
 ORACLE_BUILD = os.path.join(ORACLE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["capi.cu", "trace_mixed.cu"]
+CU_SOURCES = ["capi.cu", "trace_mixed.cu", "adjoint.cu"]
 CPP_SOURCES = ["scene.cpp", "shoot.cpp"]
 
 
@@ -73,7 +73,7 @@ def build_library(verbose: bool = False, force: bool = False) -> str:
         jobs.append((obj, cmd))
     for f in CPP_SOURCES:
         obj = os.path.join(BUILD, f + ".o")
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-c", os.path.join(CSRC, f), "-o", obj, *common]
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c", os.path.join(CSRC, f), "-o", obj, *common]
         jobs.append((obj, cmd))
     logs = []
     with cf.ThreadPoolExecutor(max_workers=max(2, min(8, os.cpu_count() or 2))) as ex:

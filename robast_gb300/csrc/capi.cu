@@ -8,13 +8,8 @@
 #include <vector>
 
 #include "scene_internal.h"
+#include "device_state.cuh"
 #include "tracer.cuh"
-
-struct rbg_device_scene {
-  rbg::DevScene view;
-  std::vector<void*> allocations;
-  unsigned* err_flags;  // device word of error bits
-};
 
 namespace rbg {
 
@@ -83,13 +78,14 @@ int ensure_device(rbg_scene* s) {
     return rc;
   }
   void* ef = nullptr;
-  if (cudaMalloc(&ef, sizeof(unsigned)) != cudaSuccess) {
+  if (cudaMalloc(&ef, 16) != cudaSuccess) {
     for (void* p : d->allocations) cudaFree(p);
     delete d;
     return RBG_ERR_NOMEM;
   }
   d->allocations.push_back(ef);
   d->err_flags = static_cast<unsigned*>(ef);
+  d->counter = reinterpret_cast<unsigned long long*>(static_cast<char*>(ef) + 8);
   v.n_nodes = (int32_t)s->nodes.size();
   v.n_borders = (int32_t)s->borders.size();
   v.n_multilayers = (int32_t)s->multilayers.size();
@@ -102,56 +98,14 @@ int ensure_device(rbg_scene* s) {
 // ---------------------------------------------------------------------
 // plain FP64 kernel: one thread per ray, whole path in registers
 // ---------------------------------------------------------------------
-struct KernelRays {
-  const double *x, *y, *z, *t, *dx, *dy, *dz, *lambda;
-};
-struct KernelOut {
-  uint8_t* status;
-  int32_t *npoints, *last_node;
-  double *x, *y, *z, *t, *dx, *dy, *dz;
-  int32_t hist_cap;
-  double* hist_xyzt;
-  int32_t* hist_node;
-};
-
 __global__ void __launch_bounds__(128) trace_fp64_kernel(DevScene S, KernelRays in, KernelOut out, int64_t n,
                                                          int limit, int disable_fresnel, uint64_t seed,
                                                          uint64_t id_offset, unsigned* err_flags) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     Ray r;
-    r.x = mk(in.x[i], in.y[i], in.z[i]);
-    r.t = in.t ? in.t[i] : 0.0;
-    r.lambda = in.lambda[i];
-    d3 dd = mk(in.dx[i], in.dy[i], in.dz[i]);
-    r.status = RBG_RUN;
-    r.npoints = 0;
-    r.last_node = -2;
-    r.err = 0;
-    r.hist_cap = out.hist_cap;
-    r.hist_xyzt = out.hist_cap ? out.hist_xyzt + (size_t)i * out.hist_cap * 4 : nullptr;
-    r.hist_node = out.hist_cap ? out.hist_node + (size_t)i * out.hist_cap : nullptr;
-    r.rng.init(seed, id_offset + (uint64_t)i, 0);
-    add_point(r, r.x, r.t);
-    double mag = sqrt(dot(dd, dd));
-    bool bad = !(mag > 0) || !isfinite(mag) || !isfinite(r.x.x) || !isfinite(r.x.y) || !isfinite(r.x.z);
-    if (bad) {
-      r.d = dd;
-      r.err |= ERR_BIT_NAN;
-    } else {
-      set_direction(r, dd);
-      trace_ray(S, r, limit, disable_fresnel != 0);
-    }
+    if (load_ray(in, out, i, seed, id_offset, r)) trace_ray<false>(S, r, limit, disable_fresnel != 0);
     if (r.err) atomicOr(err_flags, r.err);
-    if (out.status) out.status[i] = (uint8_t)r.status;
-    if (out.npoints) out.npoints[i] = r.npoints;
-    if (out.last_node) out.last_node[i] = r.last_node;
-    if (out.x) out.x[i] = r.x.x;
-    if (out.y) out.y[i] = r.x.y;
-    if (out.z) out.z[i] = r.x.z;
-    if (out.t) out.t[i] = r.t;
-    if (out.dx) out.dx[i] = r.d.x;
-    if (out.dy) out.dy[i] = r.d.y;
-    if (out.dz) out.dz[i] = r.d.z;
+    store_ray(out, i, r);
   }
 }
 
@@ -197,8 +151,8 @@ extern "C" int rbg_last_launch_count(const rbg_scene* s) { return s ? s->last_la
 
 // forward declaration of the mixed-precision entry (trace_mixed.cu)
 namespace rbg {
-int launch_mixed(rbg_scene* s, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o,
-                 cudaStream_t st, int* launches);
+int launch_mixed(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o,
+                 cudaStream_t st, unsigned* err_flags, unsigned long long* counter, int* launches);
 }
 
 extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, const rbg_trace_opts* opts,
@@ -217,9 +171,9 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
   KernelRays kr{in->x, in->y, in->z, in->t, in->dx, in->dy, in->dz, in->lambda};
   KernelOut ko{out->status, out->npoints, out->last_node, out->x, out->y, out->z, out->t,
                out->dx, out->dy, out->dz, out->hist_cap, out->hist_xyzt, out->hist_node};
-  if (opts->precision == RBG_PREC_MIXED && out->hist_cap == 0) {
+  if (opts->precision == RBG_PREC_MIXED) {
     int launches = 0;
-    rc = launch_mixed(s, kr, ko, in->n, *opts, st, &launches);
+    rc = launch_mixed(s->dev->view, kr, ko, in->n, *opts, st, s->dev->err_flags, s->dev->counter, &launches);
     if (rc) return rc;
     s->last_launches = launches;
   } else {

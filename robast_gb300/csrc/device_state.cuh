@@ -1,0 +1,17 @@
+// device_state.cuh -- the device mirror a scene owns once uploaded.
+#pragma once
+#include <vector>
+
+#include "device_scene.cuh"
+
+struct rbg_device_scene {
+  rbg::DevScene view;
+  std::vector<void*> allocations;
+  unsigned* err_flags;          // device word of error bits
+  unsigned long long* counter;  // ray queue head of the persistent kernel
+};
+
+namespace rbg {
+int ensure_device(rbg_scene* s);  // upload on first use (capi.cu)
+int sm_count();
+}  // namespace rbg

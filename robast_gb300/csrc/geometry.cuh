@@ -542,8 +542,9 @@ RBG_D double asph_dist_wall(const Asph& a, bool outer, d3 point, d3 dir) {
   if (delta < 0) return kBig;
   double t1 = -b + delta, t2 = -b - delta;
   if (t1 < 0 && t2 < 0) return kBig;
-  double zmin, zmax;
-  if (!asph_F(a, 1, R, zmin) || !asph_F(a, 2, R, zmax)) return kBig;
+  const double zmin = a.P[outer ? RBG_ASPH_F1RMAX : RBG_ASPH_F1RMIN];
+  const double zmax = a.P[outer ? RBG_ASPH_F2RMAX : RBG_ASPH_F2RMIN];
+  if (isnan(zmin) || isnan(zmax)) return kBig;
   if (t2 > 0) {
     if (t1 > 0) {
       double z1 = t1 * dir.z + point.z, z2 = t2 * dir.z + point.z;
@@ -570,9 +571,110 @@ RBG_D double asph_dist_wall(const Asph& a, bool outer, d3 point, d3 dir) {
   return kBig;
 }
 
+// Mixed precision DistToAsphere: the same iteration (spherical start, Newton
+// along the ray with the reference's update formula) run in FP32 in
+// coordinates relative to the surface vertex, then polished in FP64 with
+// the FP32 slope: each polish step evaluates only the sag residual
+// x(H2) - z in FP64 (Horner in H2), so it converges by ~7 digits per step.
+// The stopping rule and the final checks are the reference's (|e| < 1e-10,
+// forward, rmin <= r <= rmax).  Any FP32 breakdown falls back to the FP64
+// routine.
+RBG_D double asph_dist_surface_mixed(const Asph& a, int n, d3 point, d3 dir) {
+  const double d = a.z(n);
+  const float curve = (float)a.c(n), kappa = (float)a.kap(n);
+  const int npol = a.npol(n);
+  const double* K = a.K(n);
+  const float px = (float)point.x, py = (float)point.y, pz = (float)(point.z - d);
+  const float dx = (float)dir.x, dy = (float)dir.y, dz = (float)dir.z;
+  float H2 = px * px + py * py;
+  float p = -(pz * dz + px * dx + py * dy);
+  float M = p * dz + pz;
+  float M2 = pz * pz + H2 - p * p;
+  float check = 1.f - (M2 * curve - 2.f * M) * curve / dz / dz;
+  if (check < 0) return asph_dist_surface(a, n, point, dir);
+  float q = p + (M2 * curve - 2.f * M) / (dz * (1.f + sqrtf(check)));
+  float nx = px + q * dx, ny = py + q * dy, nz = pz + q * dz;
+  float Kf[RBG_ASPH_MAXPOL];
+  for (int j = 0; j < npol; ++j) Kf[j] = (float)K[j];
+  float l = 1.f, scale = 1.f;
+  bool ok = false;
+  for (int i = 0; i < 40; i++) {
+    H2 = nx * nx + ny * ny;
+    check = 1.f - kappa * H2 * curve * curve;
+    if (check < 0) break;
+    l = sqrtf(check);
+    float x = 0.f, v = 0.f;
+    for (int j = npol - 1; j >= 0; --j) {
+      x = (x + Kf[j]) * H2;
+      v = v * H2 + 2.f * (j + 1) * Kf[j];
+    }
+    if (curve != 0.f) x += (1.f - l) / curve / kappa;
+    v = curve * kappa + l * v;
+    float m = -nx * v, nn = -ny * v;
+    float norm = sqrtf(l * l + m * m + nn * nn);
+    l /= norm;
+    m /= norm;
+    nn /= norm;
+    check = dz * l + dx * m + dy * nn;
+    if (check == 0.f) break;
+    scale = l / check;  // dt per unit sag residual
+    float e = scale * (x - nz);
+    nx += e * dx;
+    ny += e * dy;
+    nz += e * dz;
+    if (fabsf(e) < 4e-6f * (1.f + fabsf(nz) + sqrtf(H2))) {
+      ok = true;
+      break;
+    }
+  }
+  if (!ok) return asph_dist_surface(a, n, point, dir);
+  // FP64 polish on t, the distance along the ray from `point`; the FP32
+  // estimate of t uses the largest direction cosine
+  double t;
+  {
+    double ax = fabs(dir.x), ay = fabs(dir.y), az = fabs(dir.z);
+    if (az >= ax && az >= ay) t = ((double)nz - (point.z - d)) / dir.z;
+    else if (ax >= ay) t = ((double)nx - point.x) / dir.x;
+    else t = ((double)ny - point.y) / dir.y;
+  }
+  const double kap64 = a.kap(n), c64 = a.c(n);
+  const double sc = (double)scale;
+  d3 np;
+  bool conv = false;
+  for (int it = 0; it < 8; ++it) {
+    np = mk(point.x + t * dir.x, point.y + t * dir.y, point.z - d + t * dir.z);
+    double h2 = np.x * np.x + np.y * np.y;
+    double chk = 1 - kap64 * h2 * c64 * c64;
+    if (chk < 0) return asph_dist_surface(a, n, point, dir);
+    double x = 0;
+    for (int j = npol - 1; j >= 0; --j) x = (x + K[j]) * h2;
+    if (c64 != 0) x += (1 - sqrt(chk)) / c64 / kap64;
+    double e = sc * (x - np.z);
+    t += e;
+    if (fabs(e) < 1e-10) {
+      conv = true;
+      np = mk(point.x + t * dir.x, point.y + t * dir.y, point.z - d + t * dir.z);
+      break;
+    }
+  }
+  if (!conv) return asph_dist_surface(a, n, point, dir);
+  np.z += d;
+  d3 dv = np - point;
+  if (dot(dir, dv) < 0) return kBig;
+  double rz = sqrt(np.x * np.x + np.y * np.y);
+  if (rz < a.rmin() || rz > a.rmax()) return kBig;
+  return sqrt(dot(dv, dv));
+}
+
+template <bool MIXED>
+RBG_D double asph_surface(const Asph& a, int n, d3 p, d3 d) {
+  return MIXED ? asph_dist_surface_mixed(a, n, p, d) : asph_dist_surface(a, n, p, d);
+}
+
+template <bool MIXED = false>
 RBG_D double asph_dist4(const Asph& a, d3 p, d3 d) {
-  double best = asph_dist_surface(a, 1, p, d);
-  double v = asph_dist_surface(a, 2, p, d);
+  double best = asph_surface<MIXED>(a, 1, p, d);
+  double v = asph_surface<MIXED>(a, 2, p, d);
   if (v < best) best = v;
   v = asph_dist_wall(a, false, p, d);
   if (v < best) best = v;
@@ -607,10 +709,41 @@ RBG_D bool tube_reached(d3 o, d3 d, double rmin, double rmax, double dz) {
   return false;
 }
 
+// FP32 screen of the bounding tube, enlarged so that it never rejects a ray
+// the exact test accepts: slab in z, then the outer cylinder
+RBG_D bool tube_reached_f32(d3 o, d3 d, double rmin, double rmax, double dz) {
+  const float pad = 1e-4f + 1e-5f * (float)(rmax + dz);
+  const float R = (float)rmax + pad, Z = (float)dz + pad;
+  const float ox = (float)o.x, oy = (float)o.y, oz = (float)o.z;
+  const float dx = (float)d.x, dy = (float)d.y, dzz = (float)d.z;
+  float t0 = 0.f, t1 = 3.0e38f;
+  if (dzz != 0.f) {
+    float ta = (-Z - oz) / dzz, tb = (Z - oz) / dzz;
+    t0 = fmaxf(t0, fminf(ta, tb));
+    t1 = fminf(t1, fmaxf(ta, tb));
+  } else if (fabsf(oz) > Z) {
+    return false;
+  }
+  if (t0 > t1) return false;
+  float A = dx * dx + dy * dy, B = ox * dx + oy * dy, C = ox * ox + oy * oy - R * R;
+  if (A == 0.f) return C <= 0.f;
+  float disc = B * B - A * C;
+  if (disc < 0.f) return false;
+  float sq = sqrtf(disc);
+  float c0 = (-B - sq) / A, c1 = (-B + sq) / A;
+  return fmaxf(t0, c0) <= fminf(t1, c1) + pad;
+  (void)rmin;
+}
+
+template <bool MIXED = false>
 RBG_D double asph_dist_out(const Asph& a, d3 p, d3 d) {
   d3 pp = mk(p.x, p.y, p.z - a.P[RBG_ASPH_ORIGIN_Z]);
-  if (!tube_reached(pp, d, a.rmin(), a.rmax(), a.P[RBG_ASPH_DZ])) return kBig;
-  return asph_dist4(a, p, d);
+  if (MIXED) {
+    if (!tube_reached_f32(pp, d, a.rmin(), a.rmax(), a.P[RBG_ASPH_DZ])) return kBig;
+  } else {
+    if (!tube_reached(pp, d, a.rmin(), a.rmax(), a.P[RBG_ASPH_DZ])) return kBig;
+  }
+  return asph_dist4<MIXED>(a, p, d);
 }
 
 // ComputeNormal (:246-327)
@@ -803,11 +936,12 @@ RBG_D bool shape_contains(const DevScene& S, int shape, d3 p) {
   return csg_contains(S, shape, p);
 }
 
+template <bool MIXED = false>
 RBG_D double shape_dist(const DevScene& S, int shape, d3 p, d3 d, bool exit, d3& nrm, unsigned& err) {
   const int type = S.shapes[shape].type;
   if (type == RBG_SHAPE_ASPHERIC_DISK) {
     Asph a{SP(S, shape)};
-    return exit ? asph_dist4(a, p, d) : asph_dist_out(a, p, d);
+    return exit ? asph_dist4<MIXED>(a, p, d) : asph_dist_out<MIXED>(a, p, d);
   }
   if (type == RBG_SHAPE_WINSTON_POLY) {
     Win w = win_load(SP(S, shape));

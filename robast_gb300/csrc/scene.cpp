@@ -293,6 +293,19 @@ struct Builder {
         asph_bbox(q.data(), &oz, &dz, steps, repeat);
         q[RBG_ASPH_ORIGIN_Z] = oz;
         q[RBG_ASPH_DZ] = dz;
+        {
+          const double* k1 = q.data() + RBG_ASPH_K;
+          const double* k2 = k1 + n1;
+          const double nan = std::numeric_limits<double>::quiet_NaN();
+          double f;
+          const double rr[2] = {q[RBG_ASPH_RMIN], q[RBG_ASPH_RMAX]};
+          for (int w = 0; w < 2; ++w) {
+            q[RBG_ASPH_F1RMIN + 2 * w] =
+                asph_sag(rr[w], q[RBG_ASPH_Z1], q[RBG_ASPH_C1], q[RBG_ASPH_KAPPA1], n1, k1, &f) ? f : nan;
+            q[RBG_ASPH_F2RMIN + 2 * w] =
+                asph_sag(rr[w], q[RBG_ASPH_Z2], q[RBG_ASPH_C2], q[RBG_ASPH_KAPPA2], n2, k2, &f) ? f : nan;
+          }
+        }
         double r = q[RBG_ASPH_RMAX];
         // conservative box for culling only: the sampled extremum can miss
         // the true one by a grid step, so pad generously

@@ -96,11 +96,12 @@ RBG_D int locate_from_top(const DevScene& S, d3 p) {
 }
 
 // candidate daughter test shared by the scan and the BVH walk
+template <bool MIXED>
 RBG_D void try_child(const DevScene& S, int k, d3 p, d3 d, double& best, int& xnode, bool& enter, d3& nbest,
                      unsigned& err) {
   const rbg_node& K = S.nodes[k];
   d3 nrm = mk(0, 0, 1);
-  double s = shape_dist(S, K.shape, to_local(K.m, p), dir_to_local(K.m, d), false, nrm, err);
+  double s = shape_dist<MIXED>(S, K.shape, to_local(K.m, p), dir_to_local(K.m, d), false, nrm, err);
   // ties: leaving the mother first, then the lowest node id (placement order)
   if (s < best || (s == best && enter && k < xnode)) {
     best = s;
@@ -111,6 +112,7 @@ RBG_D void try_child(const DevScene& S, int k, d3 p, d3 d, double& best, int& xn
 }
 
 // TGeoNavigator::FindNextBoundaryAndStep
+template <bool MIXED>
 RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, unsigned& err) {
   const int c = nv.node;
   double best;
@@ -119,7 +121,7 @@ RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, 
   bool enter;
   if (c < 0) {
     const rbg_node& T = S.nodes[0];
-    best = shape_dist(S, T.shape, to_local(T.m, nv.p), dir_to_local(T.m, nv.d), false, nbest, err);
+    best = shape_dist<MIXED>(S, T.shape, to_local(T.m, nv.p), dir_to_local(T.m, nv.d), false, nbest, err);
     if (best >= kBig) {
       step = 0;
       nv.xnode = -1;
@@ -129,7 +131,7 @@ RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, 
     enter = true;
   } else {
     const rbg_node& N = S.nodes[c];
-    best = shape_dist(S, N.shape, to_local(N.m, nv.p), dir_to_local(N.m, nv.d), true, nbest, err);
+    best = shape_dist<MIXED>(S, N.shape, to_local(N.m, nv.p), dir_to_local(N.m, nv.d), true, nbest, err);
     xnode = c;
     enter = false;
     d3 inv = mk(1.0 / nv.d.x, 1.0 / nv.d.y, 1.0 / nv.d.z);
@@ -138,7 +140,7 @@ RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, 
         int k = S.children[N.child_begin + i];
         const rbg_node& K = S.nodes[k];
         if (!seg_box(nv.p, inv, nv.d, best, K.lo, K.hi)) continue;
-        try_child(S, k, nv.p, nv.d, best, xnode, enter, nbest, err);
+        try_child<MIXED>(S, k, nv.p, nv.d, best, xnode, enter, nbest, err);
       }
     } else {
       int stack[32];
@@ -152,7 +154,7 @@ RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, 
             int k = S.bvh_items[b.item_begin + i];
             const rbg_node& K = S.nodes[k];
             if (!seg_box(nv.p, inv, nv.d, best, K.lo, K.hi)) continue;
-            try_child(S, k, nv.p, nv.d, best, xnode, enter, nbest, err);
+            try_child<MIXED>(S, k, nv.p, nv.d, best, xnode, enter, nbest, err);
           }
         } else if (sp + 2 <= 32) {
           stack[sp++] = b.right;
@@ -200,113 +202,133 @@ RBG_D d3 find_normal(const DevScene& S, const Nav& nv) {
 // --------------------------------------------------------------------
 // complex arithmetic for the transfer matrices
 // --------------------------------------------------------------------
-struct cplx {
-  double re, im;
+template <typename T>
+struct cplxT {
+  T re, im;
 };
-RBG_D cplx cx(double r, double i = 0) { return cplx{r, i}; }
-RBG_D cplx operator+(cplx a, cplx b) { return cplx{a.re + b.re, a.im + b.im}; }
-RBG_D cplx operator-(cplx a, cplx b) { return cplx{a.re - b.re, a.im - b.im}; }
-RBG_D cplx operator*(cplx a, cplx b) { return cplx{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
-RBG_D cplx operator*(double s, cplx a) { return cplx{s * a.re, s * a.im}; }
-RBG_D cplx cdiv(cplx a, cplx b) {
+template <typename T>
+RBG_D cplxT<T> cx(T r, T i = 0) { return cplxT<T>{r, i}; }
+template <typename T>
+RBG_D cplxT<T> operator+(cplxT<T> a, cplxT<T> b) { return cplxT<T>{a.re + b.re, a.im + b.im}; }
+template <typename T>
+RBG_D cplxT<T> operator-(cplxT<T> a, cplxT<T> b) { return cplxT<T>{a.re - b.re, a.im - b.im}; }
+template <typename T>
+RBG_D cplxT<T> operator*(cplxT<T> a, cplxT<T> b) {
+  return cplxT<T>{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <typename T>
+RBG_D cplxT<T> operator*(T s, cplxT<T> a) { return cplxT<T>{s * a.re, s * a.im}; }
+template <typename T>
+RBG_D cplxT<T> cdiv(cplxT<T> a, cplxT<T> b) {
   // Smith's algorithm
   if (fabs(b.re) >= fabs(b.im)) {
-    double r = b.im / b.re, den = b.re + b.im * r;
-    return cplx{(a.re + a.im * r) / den, (a.im - a.re * r) / den};
+    T r = b.im / b.re, den = b.re + b.im * r;
+    return cplxT<T>{(a.re + a.im * r) / den, (a.im - a.re * r) / den};
   }
-  double r = b.re / b.im, den = b.re * r + b.im;
-  return cplx{(a.re * r + a.im) / den, (a.im * r - a.re) / den};
+  T r = b.re / b.im, den = b.re * r + b.im;
+  return cplxT<T>{(a.re * r + a.im) / den, (a.im * r - a.re) / den};
 }
-RBG_D double cabs_(cplx a) { return hypot(a.re, a.im); }
-RBG_D cplx cexp_(cplx a) {
-  double e = exp(a.re);
-  double s, c;
+template <typename T>
+RBG_D T cabs_(cplxT<T> a) { return hypot(a.re, a.im); }
+template <typename T>
+RBG_D cplxT<T> cexp_(cplxT<T> a) {
+  T e = exp(a.re), s, c;
   sincos(a.im, &s, &c);
-  return cplx{e * c, e * s};
+  return cplxT<T>{e * c, e * s};
 }
-RBG_D cplx ccos_(cplx a) {
-  double s, c;
+template <typename T>
+RBG_D cplxT<T> ccos_(cplxT<T> a) {
+  T s, c;
   sincos(a.re, &s, &c);
-  return cplx{c * cosh(a.im), -s * sinh(a.im)};
+  return cplxT<T>{c * cosh(a.im), -s * sinh(a.im)};
 }
-RBG_D cplx csin_(cplx a) {
-  double s, c;
+template <typename T>
+RBG_D cplxT<T> csin_(cplxT<T> a) {
+  T s, c;
   sincos(a.re, &s, &c);
-  return cplx{s * cosh(a.im), c * sinh(a.im)};
+  return cplxT<T>{s * cosh(a.im), c * sinh(a.im)};
 }
-RBG_D cplx csqrt_(cplx a) {
+template <typename T>
+RBG_D cplxT<T> csqrt_(cplxT<T> a) {
   // principal square root
-  if (a.re == 0 && a.im == 0) return cplx{0, a.im};
-  double m = hypot(a.re, a.im);
-  double t = sqrt(0.5 * (m + fabs(a.re)));
-  if (a.re >= 0) return cplx{t, a.im / (2 * t)};
-  return cplx{fabs(a.im) / (2 * t), copysign(t, a.im)};
+  if (a.re == 0 && a.im == 0) return cplxT<T>{0, a.im};
+  T m = hypot(a.re, a.im);
+  T t = sqrt(T(0.5) * (m + fabs(a.re)));
+  if (a.re >= 0) return cplxT<T>{t, a.im / (2 * t)};
+  return cplxT<T>{fabs(a.im) / (2 * t), copysign(t, a.im)};
 }
-RBG_D cplx clog_(cplx a) { return cplx{log(hypot(a.re, a.im)), atan2(a.im, a.re)}; }
+template <typename T>
+RBG_D cplxT<T> clog_(cplxT<T> a) { return cplxT<T>{log(hypot(a.re, a.im)), atan2(a.im, a.re)}; }
 // principal arcsine: -i log(i z + sqrt(1 - z^2))
-RBG_D cplx casin_(cplx z) {
-  cplx one_m = cx(1) - z * z;
-  cplx w = cplx{-z.im, z.re} + csqrt_(one_m);
-  cplx l = clog_(w);
-  return cplx{l.im, -l.re};
+template <typename T>
+RBG_D cplxT<T> casin_(cplxT<T> z) {
+  cplxT<T> one_m = cx<T>(1) - z * z;
+  cplxT<T> w = cplxT<T>{-z.im, z.re} + csqrt_(one_m);
+  cplxT<T> l = clog_(w);
+  return cplxT<T>{l.im, -l.re};
 }
 
-RBG_D bool is_forward_angle(cplx n, cplx th) {
-  const double eps = 2.220446049250313e-16;
-  cplx nc = n * ccos_(th);
+template <typename T>
+RBG_D bool is_forward_angle(cplxT<T> n, cplxT<T> th) {
+  // 100 machine epsilons of the working precision
+  const T eps = sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-07);
+  cplxT<T> nc = n * ccos_(th);
   if (fabs(nc.im) > 100 * eps) return nc.im > 0;
   return nc.re > 0;
 }
 
-// AMultilayer::CoherentTMM (src/AMultilayer.cxx:240-481), pol 0 = s, 1 = p
-RBG_D void coherent_tmm(const DevScene& S, int ml, int pol, double th0r, double lam, double& R, double& T) {
+// AMultilayer::CoherentTMM (src/AMultilayer.cxx:240-481), pol 0 = s, 1 = p,
+// evaluated in precision T; the stack is walked front to back, building the
+// transfer-matrix product on the fly
+template <typename T>
+RBG_D void coherent_tmm(const DevScene& S, int ml, int pol, double th0r, double lam, double& R, double& Tr) {
+  typedef cplxT<T> C;
   const rbg_multilayer_desc M = S.multilayers[ml];
   const int N = M.n_layers;
-  // pass 1: first and last media and forward angles
   auto nidx = [&](int i) {
     const rbg_layer_desc& L = S.layers[M.layer_offset + i];
-    return cx(index_n(S, L.index, lam), index_k(S, L.index, lam));
+    return cx<T>((T)index_n(S, L.index, lam), (T)index_k(S, L.index, lam));
   };
-  cplx th0 = cx(th0r);
-  cplx n0 = nidx(0);
-  cplx n0s = n0 * csin_(th0);
-  cplx th_first = casin_(cdiv(n0s, n0));
-  if (!is_forward_angle(n0, th_first)) th_first = cx(kPi) - th_first;
-  // running transfer-matrix product over layers 1..N-2, built front to back
-  cplx a = cx(1), b = cx(0), c = cx(0), d = cx(1);
-  cplx n_prev = n0, ct_prev = ccos_(th_first);
-  cplx r0 = cx(0), t0 = cx(1);
+  const T pi = T(kPi);
+  C th0 = cx<T>((T)th0r);
+  C n0 = nidx(0);
+  C n0s = n0 * csin_(th0);
+  C th_first = casin_(cdiv(n0s, n0));
+  if (!is_forward_angle(n0, th_first)) th_first = cx<T>(pi) - th_first;
+  C a = cx<T>(1), b = cx<T>(0), c = cx<T>(0), d = cx<T>(1);
+  C n_prev = n0, ct_prev = ccos_(th_first);
+  C r0 = cx<T>(0), t0 = cx<T>(1);
   for (int i = 1; i < N; ++i) {
-    cplx ni = nidx(i);
-    cplx thi = casin_(cdiv(n0s, ni));
-    if (i == N - 1 && !is_forward_angle(ni, thi)) thi = cx(kPi) - thi;
-    cplx cti = ccos_(thi);
+    C ni = nidx(i);
+    C thi = casin_(cdiv(n0s, ni));
+    if (i == N - 1 && !is_forward_angle(ni, thi)) thi = cx<T>(pi) - thi;
+    C cti = ccos_(thi);
     // interface (i-1) -> i
-    cplx ii = n_prev * ct_prev, r, t;
+    C ii = n_prev * ct_prev, r, t;
     if (pol == 0) {
-      cplx ff = ni * cti;
+      C ff = ni * cti;
       r = cdiv(ii - ff, ii + ff);
-      t = cdiv(2.0 * ii, ii + ff);
+      t = cdiv(T(2) * ii, ii + ff);
     } else {
-      cplx fi = ni * ct_prev, iff = n_prev * cti;
+      C fi = ni * ct_prev, iff = n_prev * cti;
       r = cdiv(fi - iff, fi + iff);
-      t = cdiv(2.0 * ii, fi + iff);
+      t = cdiv(T(2) * ii, fi + iff);
     }
     if (i == 1) {
       r0 = r;
       t0 = t;
     } else {
-      // layer i-1 matrix: (1/t) diag(e^{-i delta}, e^{i delta}) [[1, r],[r, 1]]
+      // layer i-1: (1/t) diag(e^{-i delta}, e^{i delta}) [[1, r],[r, 1]]
       const rbg_layer_desc& L = S.layers[M.layer_offset + i - 1];
-      cplx kz = (2 * kPi / lam) * (n_prev * ct_prev);
-      cplx delta = L.thickness * kz;
+      C kz = (T(2) * pi / (T)lam) * (n_prev * ct_prev);
+      C delta = (T)L.thickness * kz;
       if (delta.im > 35) delta.im = 35;
-      cplx em = cexp_(cplx{delta.im, -delta.re});
-      cplx ep = cexp_(cplx{-delta.im, delta.re});
-      cplx it = cdiv(cx(1), t);
-      cplx m00 = em * it, m01 = em * r * it, m10 = ep * r * it, m11 = ep * it;
-      cplx na = a * m00 + b * m10, nb = a * m01 + b * m11;
-      cplx nc = c * m00 + d * m10, nd = c * m01 + d * m11;
+      C em = cexp_(C{delta.im, -delta.re});
+      C ep = cexp_(C{-delta.im, delta.re});
+      C it = cdiv(cx<T>(1), t);
+      C m00 = em * it, m01 = em * r * it, m10 = ep * r * it, m11 = ep * it;
+      C na = a * m00 + b * m10, nb = a * m01 + b * m11;
+      C nc = c * m00 + d * m10, nd = c * m01 + d * m11;
       a = na;
       b = nb;
       c = nc;
@@ -316,22 +338,28 @@ RBG_D void coherent_tmm(const DevScene& S, int ml, int pol, double th0r, double 
     ct_prev = cti;
   }
   // prepend the first interface: (1/t0) [[1, r0],[r0, 1]] * Mtilde
-  cplx it0 = cdiv(cx(1), t0);
-  cplx A = (a + r0 * c) * it0, Cc = (r0 * a + c) * it0;
-  cplx rr = cdiv(Cc, A), tt = cdiv(cx(1), A);
-  double ar = cabs_(rr);
-  R = ar * ar;
-  cplx ct0 = ccos_(th0);
-  cplx nf = n_prev, ctf = ct_prev;
-  double tt2 = cabs_(tt * tt);
-  if (pol == 0) T = tt2 * ((nf * ctf).re / (n0 * ct0).re);
-  else T = tt2 * ((nf * cx(ctf.re, -ctf.im)).re / (n0 * cx(ct0.re, -ct0.im)).re);
+  C it0 = cdiv(cx<T>(1), t0);
+  C A = (a + r0 * c) * it0, Cc = (r0 * a + c) * it0;
+  C rr = cdiv(Cc, A), tt = cdiv(cx<T>(1), A);
+  T ar = cabs_(rr);
+  R = (double)(ar * ar);
+  C ct0 = ccos_(th0);
+  C nf = n_prev, ctf = ct_prev;
+  T tt2 = cabs_(tt * tt);
+  if (pol == 0) Tr = (double)(tt2 * ((nf * ctf).re / (n0 * ct0).re));
+  else Tr = (double)(tt2 * ((nf * C{ctf.re, -ctf.im}).re / (n0 * C{ct0.re, -ct0.im}).re));
 }
 
+template <bool MIXED>
 RBG_D void coherent_tmm_mixed(const DevScene& S, int ml, double th0, double lam, double& R, double& T) {
   double rp, tp, rs, ts;
-  coherent_tmm(S, ml, 1, th0, lam, rp, tp);
-  coherent_tmm(S, ml, 0, th0, lam, rs, ts);
+  if (MIXED) {
+    coherent_tmm<float>(S, ml, 1, th0, lam, rp, tp);
+    coherent_tmm<float>(S, ml, 0, th0, lam, rs, ts);
+  } else {
+    coherent_tmm<double>(S, ml, 1, th0, lam, rp, tp);
+    coherent_tmm<double>(S, ml, 0, th0, lam, rs, ts);
+  }
   R = (rp + rs) / 2.;
   T = (tp + ts) / 2.;
 }
@@ -414,6 +442,7 @@ RBG_D d3 rotate_uz(d3 v, d3 u) {
 }
 
 // GetFacetNormal (:250-301)
+template <bool MIXED>
 RBG_D d3 get_facet_normal(const DevScene& S, const Nav& nv, Ray& r, int cur, int next) {
   d3 normal = find_normal(S, nv);
   int bi = find_border(S, cur, next);
@@ -461,9 +490,10 @@ RBG_D d3 euler_apply(double phi, double theta, double psi, d3 v) {
 }
 
 // DoReflection (:170-247); `normal` may be null (computed here)
+template <bool MIXED>
 RBG_D void do_reflection(const DevScene& S, Nav& nv, Ray& r, double n1, double step, int cur, int next,
                          const d3* normal) {
-  d3 n = normal ? *normal : get_facet_normal(S, nv, r, cur, next);
+  d3 n = normal ? *normal : get_facet_normal<MIXED>(S, nv, r, cur, next);
   const d3 d1 = r.d;
   double cos1 = dot(d1, n);
   int bi = find_border(S, cur, next);
@@ -473,7 +503,7 @@ RBG_D void do_reflection(const DevScene& S, Nav& nv, Ray& r, double n1, double s
     double ref;
     if (bi >= 0 && S.borders[bi].multilayer >= 0) {
       double tr;
-      coherent_tmm_mixed(S, S.borders[bi].multilayer, angle, r.lambda, ref, tr);
+      coherent_tmm_mixed<MIXED>(S, S.borders[bi].multilayer, angle, r.lambda, ref, tr);
     } else {
       const rbg_volume_desc& v = S.volumes[S.nodes[next].volume];
       if (v.refl_table >= 0)
@@ -510,10 +540,37 @@ RBG_D void do_reflection(const DevScene& S, Nav& nv, Ray& r, double n1, double s
   add_node(r, next);
 }
 
+// Fresnel reflectance for unpolarised light (:103-136) in precision T
+template <typename T>
+RBG_D double fresnel_R(T n1, T n2, T k2, T cos1, T sin1, T cos2) {
+  T Rs, Rp;
+  if (k2 <= T(0)) {
+    T eta1S = n1 * cos1, eta2S = n2 * cos2, eta1P = n1 / cos1, eta2P = n2 / cos2;
+    T a = (eta1S - eta2S) / (eta1S + eta2S), b = (eta1P - eta2P) / (eta1P + eta2P);
+    Rs = a * a;
+    Rp = b * b;
+  } else {
+    T x1S = n1 * cos1, x1P = n1 / cos1;
+    T u = n2 * n2 - k2 * k2 - (n1 * sin1) * (n1 * sin1);
+    T v = 2 * n2 * k2;
+    T tmp = sqrt(u * u + v * v);
+    T cosxi2 = sqrt(1 + u / tmp) / sqrt(T(2));
+    T sinxi2 = sqrt(1 - u / tmp) / sqrt(T(2));
+    T x2S = sqrt(tmp) * cosxi2, y2S = sqrt(tmp) * sinxi2;
+    tmp = x2S * x2S + y2S * y2S;
+    T x2P = (2 * n2 * k2 * y2S + (n2 * n2 - k2 * k2) * x2S) / tmp;
+    T y2P = (2 * n2 * k2 * x2S - (n2 * n2 - k2 * k2) * y2S) / tmp;
+    Rs = ((x1S - x2S) * (x1S - x2S) + y2S * y2S) / ((x1S + x2S) * (x1S + x2S) + y2S * y2S);
+    Rp = ((x1P - x2P) * (x1P - x2P) + y2P * y2P) / ((x1P + x2P) * (x1P + x2P) + y2P * y2P);
+  }
+  return (double)((Rs + Rp) / 2);
+}
+
 // DoFresnel (:52-167)
+template <bool MIXED>
 RBG_D void do_fresnel(const DevScene& S, Nav& nv, Ray& r, double n1, double n2, double k2, double step, int cur,
                       int next, bool disable_fresnel) {
-  d3 n = get_facet_normal(S, nv, r, cur, next);
+  d3 n = get_facet_normal<MIXED>(S, nv, r, cur, next);
   const d3 d1 = r.d;
   double cos1 = dot(d1, n);
   double sin1 = sqrt(1 - cos1 * cos1);
@@ -524,10 +581,10 @@ RBG_D void do_fresnel(const DevScene& S, Nav& nv, Ray& r, double n1, double n2, 
   bool transmit = false;
   if (bi >= 0 && S.borders[bi].multilayer >= 0) {
     double refl, trans;
-    coherent_tmm_mixed(S, S.borders[bi].multilayer, acos(cos1), r.lambda, refl, trans);
+    coherent_tmm_mixed<MIXED>(S, S.borders[bi].multilayer, acos(cos1), r.lambda, refl, trans);
     double rnd = rng_u(r);
     if (rnd < refl) {
-      do_reflection(S, nv, r, n1, step, cur, next, &n);
+      do_reflection<MIXED>(S, nv, r, n1, step, cur, next, &n);
       return;
     }
     absorbed = !(rnd < refl + trans);
@@ -535,33 +592,14 @@ RBG_D void do_fresnel(const DevScene& S, Nav& nv, Ray& r, double n1, double n2, 
   }
   if (!transmit) {
     if (sin2 > 1.) {
-      do_reflection(S, nv, r, n1, step, cur, next, &n);
+      do_reflection<MIXED>(S, nv, r, n1, step, cur, next, &n);
       return;
     }
     if (!disable_fresnel) {
-      double Rs, Rp;
-      if (k2 <= 0.) {
-        double eta1S = n1 * cos1, eta2S = n2 * cos2, eta1P = n1 / cos1, eta2P = n2 / cos2;
-        double a = (eta1S - eta2S) / (eta1S + eta2S), b = (eta1P - eta2P) / (eta1P + eta2P);
-        Rs = a * a;
-        Rp = b * b;
-      } else {
-        double x1S = n1 * cos1, x1P = n1 / cos1;
-        double u = n2 * n2 - k2 * k2 - (n1 * sin1) * (n1 * sin1);
-        double v = 2 * n2 * k2;
-        double tmp = sqrt(u * u + v * v);
-        double cosxi2 = sqrt(1 + u / tmp) / sqrt(2.0);
-        double sinxi2 = sqrt(1 - u / tmp) / sqrt(2.0);
-        double x2S = sqrt(tmp) * cosxi2, y2S = sqrt(tmp) * sinxi2;
-        tmp = x2S * x2S + y2S * y2S;
-        double x2P = (2 * n2 * k2 * y2S + (n2 * n2 - k2 * k2) * x2S) / tmp;
-        double y2P = (2 * n2 * k2 * x2S - (n2 * n2 - k2 * k2) * y2S) / tmp;
-        Rs = ((x1S - x2S) * (x1S - x2S) + y2S * y2S) / ((x1S + x2S) * (x1S + x2S) + y2S * y2S);
-        Rp = ((x1P - x2P) * (x1P - x2P) + y2P * y2P) / ((x1P + x2P) * (x1P + x2P) + y2P * y2P);
-      }
-      double R = (Rs + Rp) / 2.;
+      double R = MIXED ? fresnel_R<float>((float)n1, (float)n2, (float)k2, (float)cos1, (float)sin1, (float)cos2)
+                       : fresnel_R<double>(n1, n2, k2, cos1, sin1, cos2);
       if (rng_u(r) < R) {
-        do_reflection(S, nv, r, n1, step, cur, next, &n);
+        do_reflection<MIXED>(S, nv, r, n1, step, cur, next, &n);
         return;
       }
     }
@@ -578,81 +616,149 @@ RBG_D void do_fresnel(const DevScene& S, Nav& nv, Ray& r, double n1, double n2, 
   }
 }
 
-// TraceNonSequential(TObjArray*) body for one ray (:346-518)
-RBG_D void trace_ray(const DevScene& S, Ray& r, int limit, bool disable_fresnel) {
-  Nav nv;
+// TraceNonSequential(TObjArray*) body for one ray (:346-518), split into
+// InitTrack and one iteration of the while (ray->IsRunning()) loop so that
+// a persistent kernel can interleave rays
+RBG_D void trace_begin(const DevScene& S, Ray& r, Nav& nv) {
   nv.p = r.x;
   nv.d = r.d;
   nv.node = locate_from_top(S, nv.p);
   nv.xnode = -1;
   nv.xn = mk(0, 0, 1);
+}
+
+template <bool MIXED>
+RBG_D void trace_step(const DevScene& S, Ray& r, Nav& nv, int limit, bool disable_fresnel) {
   const double lambda = r.lambda;
-  while (r.status == RBG_RUN) {
-    const d3 x1 = r.x;
-    const double t1 = r.t;
-    const d3 d1 = r.d;
-    const int cur = nv.node;
-    double step;
-    const int next = find_next_boundary_and_step(S, nv, step, r.err);
-    const int tc = kind_of(S, cur), tn = kind_of(S, next);
+  const d3 x1 = r.x;
+  const double t1 = r.t;
+  const d3 d1 = r.d;
+  const int cur = nv.node;
+  double step;
+  const int next = find_next_boundary_and_step<MIXED>(S, nv, step, r.err);
+  const int tc = kind_of(S, cur), tn = kind_of(S, next);
 
-    if (tc == kLens) {
-      int idx = S.volumes[S.nodes[cur].volume].index;
-      double k = index_k(S, idx, lambda);
-      double abs_len = k <= 0. ? INFINITY : lambda / (4 * kPi * k);
-      if (abs_len > 0 && abs_len != INFINITY) {
-        double abs_step = -abs_len * log(1.0 - rng_u(r));
-        if (abs_step < step) {
-          double n1 = index_n(S, idx, lambda);
-          add_point(r, x1 + abs_step * d1, t1 + abs_step / (RBG_SPEED_OF_LIGHT_CM / n1));
-          add_node(r, next);
-          r.status = RBG_ABSORB;
-          continue;
-        }
+  if (tc == kLens) {
+    int idx = S.volumes[S.nodes[cur].volume].index;
+    double k = index_k(S, idx, lambda);
+    double abs_len = k <= 0. ? INFINITY : lambda / (4 * kPi * k);
+    if (abs_len > 0 && abs_len != INFINITY) {
+      double abs_step = -abs_len * log(1.0 - rng_u(r));
+      if (abs_step < step) {
+        double n1 = index_n(S, idx, lambda);
+        add_point(r, x1 + abs_step * d1, t1 + abs_step / (RBG_SPEED_OF_LIGHT_CM / n1));
+        add_node(r, next);
+        r.status = RBG_ABSORB;
+        return;
       }
     }
-
-    if ((tc == kNull || tc == kOpt || tc == kLens || tc == kOther) && tn == kMirror) {
-      double n1 = tc == kLens ? lens_n(S, cur, lambda) : 1.;
-      do_reflection(S, nv, r, n1, step, cur, next, nullptr);
-    } else if ((tc == kNull || tc == kOpt || tc == kOther) && tn == kLens) {
-      int idx = S.volumes[S.nodes[next].volume].index;
-      do_fresnel(S, nv, r, 1, index_n(S, idx, lambda), index_k(S, idx, lambda), step, cur, next, disable_fresnel);
-    } else if ((tc == kNull || tc == kLens || tc == kOpt || tc == kOther) && (tn == kObs || tn == kFocus)) {
-      double speed = tc == kLens ? RBG_SPEED_OF_LIGHT_CM / lens_n(S, cur, lambda) : RBG_SPEED_OF_LIGHT_CM;
-      add_point(r, nv.p, t1 + step / speed);
-      add_node(r, next);
-    } else if ((tc == kNull || tc == kOpt || tc == kOther) && (tn == kOther || tn == kOpt)) {
-      add_point(r, nv.p, t1 + step / RBG_SPEED_OF_LIGHT_CM);
-      add_node(r, next);
-    } else if (tc == kLens && tn == kLens) {
-      int idx = S.volumes[S.nodes[next].volume].index;
-      do_fresnel(S, nv, r, lens_n(S, cur, lambda), index_n(S, idx, lambda), index_k(S, idx, lambda), step, cur,
-                 next, disable_fresnel);
-    } else if (tc == kLens && (tn == kNull || tn == kOpt || tn == kOther)) {
-      do_fresnel(S, nv, r, lens_n(S, cur, lambda), 1, 0, step, cur, next, disable_fresnel);
-    }
-
-    if (tn == kNull) {
-      add_point(r, nv.p, t1 + step / RBG_SPEED_OF_LIGHT_CM);
-      add_node(r, next);
-      r.status = RBG_EXIT;
-    } else if (tc == kFocus || tc == kObs || tc == kMirror || tn == kObs) {
-      r.status = RBG_STOP;
-    } else if (tn == kFocus) {
-      const rbg_volume_desc& v = S.volumes[S.nodes[next].volume];
-      double angle = 0.;
-      if (v.qe_angle_table >= 0) {
-        d3 n = get_facet_normal(S, nv, r, cur, next);
-        angle = acos(dot(r.d, n));
-      }
-      double qe = v.qe_lambda_table >= 0 ? table1d(S, v.qe_lambda_table, lambda) : 1.;
-      if (v.qe_angle_table >= 0) qe *= table1d(S, v.qe_angle_table, angle);
-      if (qe == 1 || rng_u(r) < qe) r.status = RBG_FOCUS;
-      else r.status = RBG_STOP;
-    }
-    if (r.status == RBG_RUN && r.npoints >= limit) r.status = RBG_SUSPEND;
   }
+
+  if ((tc == kNull || tc == kOpt || tc == kLens || tc == kOther) && tn == kMirror) {
+    double n1 = tc == kLens ? lens_n(S, cur, lambda) : 1.;
+    do_reflection<MIXED>(S, nv, r, n1, step, cur, next, nullptr);
+  } else if ((tc == kNull || tc == kOpt || tc == kOther) && tn == kLens) {
+    int idx = S.volumes[S.nodes[next].volume].index;
+    do_fresnel<MIXED>(S, nv, r, 1, index_n(S, idx, lambda), index_k(S, idx, lambda), step, cur, next,
+                      disable_fresnel);
+  } else if ((tc == kNull || tc == kLens || tc == kOpt || tc == kOther) && (tn == kObs || tn == kFocus)) {
+    double speed = tc == kLens ? RBG_SPEED_OF_LIGHT_CM / lens_n(S, cur, lambda) : RBG_SPEED_OF_LIGHT_CM;
+    add_point(r, nv.p, t1 + step / speed);
+    add_node(r, next);
+  } else if ((tc == kNull || tc == kOpt || tc == kOther) && (tn == kOther || tn == kOpt)) {
+    add_point(r, nv.p, t1 + step / RBG_SPEED_OF_LIGHT_CM);
+    add_node(r, next);
+  } else if (tc == kLens && tn == kLens) {
+    int idx = S.volumes[S.nodes[next].volume].index;
+    do_fresnel<MIXED>(S, nv, r, lens_n(S, cur, lambda), index_n(S, idx, lambda), index_k(S, idx, lambda), step,
+                      cur, next, disable_fresnel);
+  } else if (tc == kLens && (tn == kNull || tn == kOpt || tn == kOther)) {
+    do_fresnel<MIXED>(S, nv, r, lens_n(S, cur, lambda), 1, 0, step, cur, next, disable_fresnel);
+  }
+
+  if (tn == kNull) {
+    add_point(r, nv.p, t1 + step / RBG_SPEED_OF_LIGHT_CM);
+    add_node(r, next);
+    r.status = RBG_EXIT;
+  } else if (tc == kFocus || tc == kObs || tc == kMirror || tn == kObs) {
+    r.status = RBG_STOP;
+  } else if (tn == kFocus) {
+    const rbg_volume_desc& v = S.volumes[S.nodes[next].volume];
+    double angle = 0.;
+    if (v.qe_angle_table >= 0) {
+      d3 n = get_facet_normal<MIXED>(S, nv, r, cur, next);
+      angle = acos(dot(r.d, n));
+    }
+    double qe = v.qe_lambda_table >= 0 ? table1d(S, v.qe_lambda_table, lambda) : 1.;
+    if (v.qe_angle_table >= 0) qe *= table1d(S, v.qe_angle_table, angle);
+    if (qe == 1 || rng_u(r) < qe) r.status = RBG_FOCUS;
+    else r.status = RBG_STOP;
+  }
+  if (r.status == RBG_RUN && r.npoints >= limit) r.status = RBG_SUSPEND;
+}
+
+template <bool MIXED>
+RBG_D void trace_ray(const DevScene& S, Ray& r, int limit, bool disable_fresnel) {
+  Nav nv;
+  trace_begin(S, r, nv);
+  while (r.status == RBG_RUN) trace_step<MIXED>(S, r, nv, limit, disable_fresnel);
+}
+
+// ---------------------------------------------------------------------
+// kernel-side ray I/O (structure of arrays)
+// ---------------------------------------------------------------------
+struct KernelRays {
+  const double *x, *y, *z, *t, *dx, *dy, *dz, *lambda;
+};
+struct KernelOut {
+  uint8_t* status;
+  int32_t *npoints, *last_node;
+  double *x, *y, *z, *t, *dx, *dy, *dz;
+  int32_t hist_cap;
+  double* hist_xyzt;
+  int32_t* hist_node;
+};
+
+// Read ray i, record its start point, normalise the direction as
+// ARay::SetDirection does.  Returns false (and flags the error) for a ray
+// that cannot be traced: NaN origin or a zero/NaN direction.
+RBG_D bool load_ray(const KernelRays& in, const KernelOut& out, int64_t i, uint64_t seed, uint64_t id_offset,
+                    Ray& r) {
+  r.x = mk(in.x[i], in.y[i], in.z[i]);
+  r.t = in.t ? in.t[i] : 0.0;
+  r.lambda = in.lambda[i];
+  d3 dd = mk(in.dx[i], in.dy[i], in.dz[i]);
+  r.status = RBG_RUN;
+  r.npoints = 0;
+  r.last_node = -2;
+  r.err = 0;
+  r.hist_cap = out.hist_cap;
+  r.hist_xyzt = out.hist_cap ? out.hist_xyzt + (size_t)i * out.hist_cap * 4 : nullptr;
+  r.hist_node = out.hist_cap ? out.hist_node + (size_t)i * out.hist_cap : nullptr;
+  r.rng.init(seed, id_offset + (uint64_t)i, 0);
+  add_point(r, r.x, r.t);
+  double mag = sqrt(dot(dd, dd));
+  bool bad = !(mag > 0) || !isfinite(mag) || !isfinite(r.x.x) || !isfinite(r.x.y) || !isfinite(r.x.z);
+  if (bad) {
+    r.d = dd;
+    r.err |= ERR_BIT_NAN;
+    return false;
+  }
+  set_direction(r, dd);
+  return true;
+}
+
+RBG_D void store_ray(const KernelOut& out, int64_t i, const Ray& r) {
+  if (out.status) out.status[i] = (uint8_t)r.status;
+  if (out.npoints) out.npoints[i] = r.npoints;
+  if (out.last_node) out.last_node[i] = r.last_node;
+  if (out.x) out.x[i] = r.x.x;
+  if (out.y) out.y[i] = r.x.y;
+  if (out.z) out.z[i] = r.x.z;
+  if (out.t) out.t[i] = r.t;
+  if (out.dx) out.dx[i] = r.d.x;
+  if (out.dy) out.dy[i] = r.d.y;
+  if (out.dz) out.dz[i] = r.d.z;
 }
 
 }  // namespace rbg

@@ -101,3 +101,28 @@ def test_config_parity(name, kw):
     g = np.bincount(gpu["status"], minlength=6)
     r = np.bincount(ref["status"], minlength=6)
     assert np.abs(g - r).max() <= max(5, 0.002 * len(batch["x"]))
+
+
+MIXED_CASES = [
+    ("paraboloid", dict(n_rays=20000)),
+    ("schwarzschild_couder", dict(n_rays=20000)),
+    ("davies_cotton", dict(n_rays=22000)),
+    ("light_guide", dict(n_rays=16000, n_variants=4)),
+    ("schmidt_cassegrain", dict(n_rays=16000, n_samples=4)),
+]
+
+
+@pytest.mark.parametrize("name,kw", MIXED_CASES)
+def test_mixed_precision_parity(name, kw):
+    """The mixed-precision persistent tracer against the FP64 oracle: the
+    accepted intersections are polished in FP64, so fates and final points
+    agree like the plain FP64 tracer's; FP32 reflectances (thin-film
+    matrices, Fresnel) can flip a random draw on a handful of rays."""
+    from robast_gb300 import _native as N
+
+    man, batch = configs.CONFIGS[name](**kw)
+    st, gpu = _gpu_trace(man, batch, precision=N.PREC_MIXED)
+    assert st == 0
+    ost, ref = oracle_ref.trace(man, configs.to_array(batch), threads=8)
+    assert ost == 0
+    compare(gpu, ref, min_agree=0.999)
