@@ -108,6 +108,63 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def grad_bench(batch, rays, steps, device, N, torch):
+    """Gradient evaluations per second of the summed per-field RMS spot
+    radius w.r.t. the 22 Schwarzschild-Couder parameters: adjoint (mixed
+    forward with hit records + one backward) vs central finite differences
+    with the plain FP64 tracer (2 x 22 traces), same rays."""
+    from robast_gb300 import adjoint as A
+
+    build = A.sc_builder()
+    p0 = A.sc_parameters()
+    group = rays["group"]
+    n_groups = int(batch["group"].max()) + 1
+    TF = A.make_trace_function()
+
+    def loss_of(x, y, focused):
+        return sum(A.rms_spot(x, y, focused & (group == g)) for g in range(n_groups))
+
+    def adjoint_eval():
+        params = torch.tensor(p0, dtype=torch.float64, requires_grad=True)
+        x, y, f = TF.apply(params, build, rays)
+        loss_of(x, y, f).backward()
+        return params.grad.clone()
+
+    g_adj = adjoint_eval()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        g_adj = adjoint_eval()
+    torch.cuda.synchronize()
+    t_adj = (time.perf_counter() - t0) / steps
+
+    h = A.fd_steps(p0)
+    res = device.alloc_result(rays["x"].numel(), rays["x"].device)
+
+    def loss_fp64(p):
+        man, _ = build(p)
+        device.trace(man, rays, res, precision=N.PREC_FP64)
+        return float(loss_of(res["x"], res["y"], res["status"] == N.RBG_FOCUS))
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fd = np.zeros_like(p0)
+    for k in range(len(p0)):
+        pp, pm = p0.copy(), p0.copy()
+        pp[k] += h[k]
+        pm[k] -= h[k]
+        fd[k] = (loss_fp64(pp) - loss_fp64(pm)) / (2 * h[k])
+    torch.cuda.synchronize()
+    t_fd = time.perf_counter() - t0
+    ga = g_adj.cpu().numpy()
+    scale = np.abs(fd * h).max()
+    rel = np.abs((ga - fd) * h) / np.maximum(np.abs(fd * h), 1e-3 * scale)
+    return {"unit": "grad-evals/s", "params": len(p0), "rays": int(rays["x"].numel()),
+            "adjoint": 1.0 / t_adj, "finite_differences_fp64": 1.0 / t_fd, "speedup": t_fd / t_adj,
+            "max_rel_err_vs_fd": float(rel.max()),
+            "loss": "sum over the 5 field angles of the RMS spot radius"}
+
+
 def cpu_baseline(man, batch, sample):
     import oracle_ref
 
@@ -159,6 +216,7 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-compare", action="store_true", help="skip the plain FP64 comparison run")
+    ap.add_argument("--no-grad", action="store_true", help="skip the gradient benchmark")
     ap.add_argument("--rays", type=int, default=N_RAYS)
     ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE)
     args = ap.parse_args()
@@ -293,6 +351,8 @@ def main():
                          "frac": achieved / hbm, "traffic": None, "peak_source": how,
                          "note": "algorithmic ray-state bytes; the kernel is FP64-pipe bound, see profiles/"},
             "e2e": e2e, "clocks": clocks, "vs_plain_fp64": compare}
+    if not args.no_grad and ws == 1:
+        line["grad"] = grad_bench(batch, rays, max(1, min(args.steps, 3)), device, N, torch)
     cb, _ = cpu_baseline(man, batch, args.cpu_sample)
     line["cpu_baseline"] = cb
     print(json.dumps(line))

@@ -1,0 +1,184 @@
+"""Gradients of focal-plane figures of merit through the GPU tracer.
+
+``TraceFunction`` is a ``torch.autograd.Function``: its forward traces a
+ray batch (recording each ray's hit points) in a scene built from a
+parameter vector, and its backward calls the hand-written adjoint kernel
+``rbg_trace_adjoint`` (vector-Jacobian product of the final ray points with
+respect to the parameters).  Losses are ordinary torch code on the focal
+points, so ``loss.backward()`` gives d loss / d parameters in one forward +
+one backward pass -- the gradient step that replaces the Minuit scans of
+tutorials/Optimize.C:60-205.
+
+The reference has no gradients; effective area (a count of focused rays)
+is piecewise constant in the parameters, so its pathwise gradient is zero
+and it is reported, not differentiated.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+from typing import Callable, List, Sequence
+
+import numpy as np
+
+from . import _native as N
+from . import device
+
+ADJ_ASPH_COEF, ADJ_NODE_SHIFT, ADJ_NODE_ROTATE = 1, 2, 3
+
+
+class AdjointParam(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("node", C.c_int32), ("index", C.c_int32), ("faces", C.c_int32),
+                ("pivot", C.c_double * 3)]
+
+
+def _declare():
+    L = N.lib()
+    if not getattr(L, "_adj_declared", False):
+        L.rbg_trace_adjoint.argtypes = [C.c_void_p, C.c_int64, C.POINTER(N.Result), C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_int32, C.POINTER(AdjointParam), C.c_void_p,
+                                        C.POINTER(C.c_int64), C.c_void_p]
+        L._adj_declared = True
+    return L
+
+
+@dataclass
+class ParamSpec:
+    """One differentiable parameter: kind, physical node id, index (K_j or
+    axis), face mask for coefficients, pivot for rotations."""
+    kind: int
+    node: int
+    index: int
+    faces: int = 3
+    pivot: Sequence[float] = (0.0, 0.0, 0.0)
+
+    def as_c(self):
+        return AdjointParam(self.kind, self.node, self.index, self.faces, (C.c_double * 3)(*self.pivot))
+
+
+def trace_with_history(manager, rays, precision=N.PREC_MIXED, history=8, stream=None):
+    n = rays["x"].numel()
+    res = device.alloc_result(n, rays["x"].device, history)
+    res, st = device.trace(manager, rays, res, precision=precision, stream=stream)
+    return res, st
+
+
+def vjp(manager, res, specs: List[ParamSpec], gx, gy, gz=None, stream=None):
+    """dL/dp for cotangents (gx, gy, gz) of the final points (device tensors)."""
+    import torch
+
+    L = _declare()
+    n = res["x"].numel()
+    rr = device._result_struct(res)
+    arr = (AdjointParam * max(1, len(specs)))(*[s.as_c() for s in specs])
+    out = torch.zeros(len(specs), dtype=torch.float64, device=res["x"].device)
+    skipped = C.c_int64(0)
+    st = (stream if stream is not None else torch.cuda.current_stream()).cuda_stream
+    N.check(L.rbg_trace_adjoint(manager.scene.handle, n, C.byref(rr), device._ptr(gx), device._ptr(gy),
+                                device._ptr(gz), len(specs), arr, device._ptr(out), C.byref(skipped),
+                                C.c_void_p(st)), "rbg_trace_adjoint")
+    return out, skipped.value
+
+
+def make_trace_function():
+    import torch
+
+    class TraceFunction(torch.autograd.Function):
+        """forward(params, build, rays, precision) -> (x, y, focused).
+
+        ``build(params_numpy) -> (manager, [ParamSpec])`` constructs the
+        scene at the given parameter values."""
+
+        @staticmethod
+        def forward(ctx, params, build: Callable, rays, precision=N.PREC_MIXED):
+            man, specs = build(params.detach().cpu().numpy())
+            res, st = trace_with_history(man, rays, precision)
+            if st not in (N.RBG_OK,):
+                N.check(st, "rbg_trace")
+            focused = res["status"] == N.RBG_FOCUS
+            ctx.man, ctx.specs, ctx.res = man, specs, res
+            ctx.mark_non_differentiable(focused)
+            return res["x"].clone(), res["y"].clone(), focused
+
+        @staticmethod
+        def backward(ctx, gx, gy, _gf):
+            g, skipped = vjp(ctx.man, ctx.res, ctx.specs, gx.contiguous(), gy.contiguous())
+            ctx.skipped = skipped
+            return g.to(gx.dtype), None, None, None
+
+    return TraceFunction
+
+
+def rms_spot(x, y, mask):
+    """RMS spot radius of the focused rays: sqrt(<|p - <p>|^2>)."""
+    xs, ys = x[mask], y[mask]
+    return ((xs - xs.mean()) ** 2 + (ys - ys.mean()) ** 2).mean().sqrt()
+
+
+def r80_smooth(x, y, mask, width_frac=0.05, fraction=0.8):
+    """Differentiable 80 % containment radius about the centroid: the root
+    r of F(r) = <sigmoid((r - rho_i) / h)> = fraction, h = width_frac * r.
+    Found by bisection without gradient, then one implicit-function step
+    (r - (F(r) - f) / F'(r) with F'(r) held fixed) carries d r / d x."""
+    import torch
+
+    xs, ys = x[mask], y[mask]
+    cx, cy = xs.mean(), ys.mean()
+    rho = torch.sqrt((xs - cx) ** 2 + (ys - cy) ** 2 + 1e-30)
+    with torch.no_grad():
+        r_hard = torch.quantile(rho, fraction)
+        h = width_frac * r_hard
+        lo, hi = torch.zeros_like(r_hard), rho.max() + 10 * h
+        for _ in range(80):
+            mid = 0.5 * (lo + hi)
+            f = torch.sigmoid((mid - rho) / h).mean()
+            lo, hi = torch.where(f < fraction, mid, lo), torch.where(f < fraction, hi, mid)
+        r0 = 0.5 * (lo + hi)
+        s = torch.sigmoid((r0 - rho) / h)
+        dF = (s * (1 - s)).mean() / h
+    F = torch.sigmoid((r0 - rho) / h).mean()
+    return r0 - (F - fraction) / dF
+
+
+# ---------------------------------------------------------------------------
+# Schwarzschild-Couder parameterisation: 8 + 8 aspheric coefficients and
+# the secondary's shift (3) and rotation (3) about its vertex
+# ---------------------------------------------------------------------------
+def sc_parameters(primary_k=None, secondary_k=None):
+    from .configs import SC_PRIMARY_K, SC_SECONDARY_K
+
+    kp = np.array(SC_PRIMARY_K if primary_k is None else primary_k, dtype=float)
+    ks = np.array(SC_SECONDARY_K if secondary_k is None else secondary_k, dtype=float)
+    return np.concatenate([kp, ks, np.zeros(6)])
+
+
+def sc_builder(n_rays=0):
+    """build(params) for the Schwarzschild-Couder telescope of configs.py."""
+    from .configs import SC_ZS, schwarzschild_couder
+
+    def build(p):
+        man, _ = schwarzschild_couder(n_rays=5, primary_k=p[0:8], secondary_k=p[8:16], perturb=0.0,
+                                      secondary_shift=tuple(p[16:19]), secondary_tilt=tuple(p[19:22]))
+        names = man.scene.node_names()
+        prim = names.index("primaryMirror")
+        sec = names.index("secondaryMirror")
+        specs = [ParamSpec(ADJ_ASPH_COEF, prim, j, 3) for j in range(8)]
+        specs += [ParamSpec(ADJ_ASPH_COEF, sec, j, 3) for j in range(8)]
+        specs += [ParamSpec(ADJ_NODE_SHIFT, sec, a) for a in range(3)]
+        pivot = (float(p[16]), float(p[17]), SC_ZS + float(p[18]))
+        specs += [ParamSpec(ADJ_NODE_ROTATE, sec, a, pivot=pivot) for a in range(3)]
+        return man, specs
+
+    return build
+
+
+def fd_steps(params):
+    """Central-difference steps: coefficient steps that move the sag by
+    ~1e-5 cm at r = 4.85 m, 1e-4 cm shifts, 1e-6 rad rotations."""
+    h = np.empty_like(params)
+    for j in range(8):
+        h[j] = h[8 + j] = 1e-5 / (485.0 ** (2 * (j + 1)))
+    h[16:19] = 1e-4
+    h[19:22] = 1e-6
+    return h

@@ -130,6 +130,8 @@ def schwarzschild_couder(n_rays: int = 10_000_000, angles=(0.0, 1.0, 2.0, 3.0, 4
         rot = TGeoRotation("", 0, 0, 0)
         rot.RotateX(secondary_tilt[0] / deg)
         rot.RotateY(secondary_tilt[1] / deg)
+        if len(secondary_tilt) > 2:
+            rot.RotateZ(secondary_tilt[2] / deg)
         # rotate about the mirror vertex (z = SC_ZS)
         c = np.array([0.0, 0.0, SC_ZS])
         t = c - rot.R @ c + np.asarray(secondary_shift, dtype=float)
