@@ -92,7 +92,7 @@ enum { RBG_OP_UNION = 0, RBG_OP_INTERSECTION = 1, RBG_OP_SUBTRACTION = 2 };
  *   WINSTON_POLY   r1 r2 n
  *   COMPOSITE      (no params; op/left/right/left_matrix/right_matrix fields)
  * The flattened scene (rbg_flat_scene) holds a canonical layout that adds
- * derived quantities; it is documented in robast_gb300/csrc/scene_layout.h.
+ * derived quantities; it is documented in include/robast_gb_layout.h.
  */
 typedef struct {
   int32_t type;
@@ -309,9 +309,8 @@ int rbg_trace(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
 int rbg_trace_host(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
                    const rbg_trace_opts* opts);
 
-/* Number of kernel launches the last rbg_trace on this scene issued, and the
- * device time of its dominant kernel in ms measured with events on the
- * launching stream (NaN when not measured). */
+/* Number of tracer kernel launches the last rbg_trace on this scene issued
+ * (1 for either precision: the whole batch is one launch). */
 int rbg_last_launch_count(const rbg_scene* scene);
 
 /* ---- spot reductions ---------------------------------------------------- */

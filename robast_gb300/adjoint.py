@@ -98,6 +98,7 @@ def make_trace_function():
                 N.check(st, "rbg_trace")
             focused = res["status"] == N.RBG_FOCUS
             ctx.man, ctx.specs, ctx.res = man, specs, res
+            ctx.param_device, ctx.param_dtype = params.device, params.dtype
             ctx.mark_non_differentiable(focused)
             return res["x"].clone(), res["y"].clone(), focused
 
@@ -105,7 +106,7 @@ def make_trace_function():
         def backward(ctx, gx, gy, _gf):
             g, skipped = vjp(ctx.man, ctx.res, ctx.specs, gx.contiguous(), gy.contiguous())
             ctx.skipped = skipped
-            return g.to(gx.dtype), None, None, None
+            return g.to(device=ctx.param_device, dtype=ctx.param_dtype), None, None, None
 
     return TraceFunction
 
@@ -117,28 +118,29 @@ def rms_spot(x, y, mask):
 
 
 def r80_smooth(x, y, mask, width_frac=0.05, fraction=0.8):
-    """Differentiable 80 % containment radius about the centroid: the root
-    r of F(r) = <sigmoid((r - rho_i) / h)> = fraction, h = width_frac * r.
-    Found by bisection without gradient, then one implicit-function step
-    (r - (F(r) - f) / F'(r) with F'(r) held fixed) carries d r / d x."""
+    """Differentiable 80 % containment radius about the centroid: the root r
+    of G(r) = <sigmoid((r - rho_i) / (w r))> - fraction = 0 with w =
+    width_frac (the sigmoid's width scales with r itself, so G is smooth in
+    the ray positions and strictly increasing in r).  The root is found by
+    bisection without gradient; one implicit-function step
+    r0 - G(r0) / G'(r0), with G'(r0) = <s (1 - s) rho_i / (w r0^2)> held
+    fixed, carries dr/dx = -(dG/dx) / G'(r)."""
     import torch
 
     xs, ys = x[mask], y[mask]
     cx, cy = xs.mean(), ys.mean()
     rho = torch.sqrt((xs - cx) ** 2 + (ys - cy) ** 2 + 1e-30)
     with torch.no_grad():
-        r_hard = torch.quantile(rho, fraction)
-        h = width_frac * r_hard
-        lo, hi = torch.zeros_like(r_hard), rho.max() + 10 * h
-        for _ in range(80):
+        lo, hi = torch.zeros_like(rho[0]), 2 * rho.max() + 1e-30
+        for _ in range(100):
             mid = 0.5 * (lo + hi)
-            f = torch.sigmoid((mid - rho) / h).mean()
-            lo, hi = torch.where(f < fraction, mid, lo), torch.where(f < fraction, hi, mid)
+            g = torch.sigmoid((mid - rho) / (width_frac * mid)).mean()
+            lo, hi = torch.where(g < fraction, mid, lo), torch.where(g < fraction, hi, mid)
         r0 = 0.5 * (lo + hi)
-        s = torch.sigmoid((r0 - rho) / h)
-        dF = (s * (1 - s)).mean() / h
-    F = torch.sigmoid((r0 - rho) / h).mean()
-    return r0 - (F - fraction) / dF
+        s = torch.sigmoid((r0 - rho) / (width_frac * r0))
+        dG = (s * (1 - s) * rho).mean() / (width_frac * r0 * r0)
+    G = torch.sigmoid((r0 - rho) / (width_frac * r0)).mean() - fraction
+    return r0 - G / dG
 
 
 # ---------------------------------------------------------------------------

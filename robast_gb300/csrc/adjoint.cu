@@ -93,7 +93,7 @@ RBG_D bool surface_at(const DevScene& S, int node, d3 P, Surf& out) {
     double H2 = p.x * p.x + p.y * p.y;
     double best = kBig;
     int face = 0;
-    double F = 0, dF = 0, d2F = 0;
+    double dF = 0, d2F = 0;
     for (int f = 1; f <= 2; ++f) {
       double Ff, dFf, d2Ff;
       if (!asph_sag2(a, f, H2, Ff, dFf, d2Ff)) continue;
@@ -101,7 +101,6 @@ RBG_D bool surface_at(const DevScene& S, int node, d3 P, Surf& out) {
       if (dist < best) {
         best = dist;
         face = f;
-        F = Ff;
         dF = dFf;
         d2F = d2Ff;
       }

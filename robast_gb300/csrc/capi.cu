@@ -90,6 +90,7 @@ int ensure_device(rbg_scene* s) {
   v.n_borders = (int32_t)s->borders.size();
   v.n_multilayers = (int32_t)s->multilayers.size();
   v.n_tables = (int32_t)s->tables.size();
+  v.features = s->features;
   s->dev = d;
   s->dev_id = dev;
   return RBG_OK;

@@ -3,6 +3,7 @@
 #pragma once
 #include <cstdint>
 
+#include "trace_features.h"
 #include "philox.h"
 #include "robast_gb.h"
 #include "robast_gb_layout.h"
@@ -25,7 +26,10 @@ struct DevScene {
   const rbg_border_desc* borders;
   const double* params;
   int32_t n_nodes, n_borders, n_multilayers, n_tables;
+  uint32_t features;  // kFeat* bits present in the scene
 };
+
+
 
 // error bits raised by kernels (read back by the C ABI)
 enum : unsigned { ERR_BIT_NAN = 1u, ERR_BIT_CAP = 2u };

@@ -666,15 +666,123 @@ RBG_D double asph_dist_surface_mixed(const Asph& a, int n, d3 point, d3 dir) {
   return sqrt(dot(dv, dv));
 }
 
-template <bool MIXED>
+// Sag F(H2) and dF/dH2 of face s in FP64 without the conic square roots
+// when the curvature is zero (the SC and light-guide surfaces); the values
+// equal CalcF1/CalcF2 to rounding.
+RBG_D bool asph_sag_fast(const Asph& a, int s, double H2, double& F, double& dF) {
+  const double c = a.c(s);
+  const int n = a.npol(s);
+  const double* K = a.K(s);
+  double p = 0, dp = 0;
+  for (int j = n - 1; j >= 0; --j) {
+    p = (p + K[j]) * H2;
+    dp = dp * H2 + (j + 1) * K[j];
+  }
+  if (c == 0) {
+    F = a.z(s) + p;
+    dF = dp;
+    return true;
+  }
+  double chk = 1 - a.kap(s) * c * c * H2;
+  if (chk < 0) return false;
+  double sq = sqrt(chk);
+  F = a.z(s) + H2 * c / (1 + sq) + p;
+  dF = chk > 0 ? c / (2 * sq) + dp : dp;
+  return true;
+}
+
+// Contains without the radius square root (H2 against rmin^2, rmax^2)
+RBG_D bool asph_contains_fast(const Asph& a, d3 p) {
+  double H2 = p.x * p.x + p.y * p.y;
+  if (H2 > a.rmax() * a.rmax() || H2 < a.rmin() * a.rmin()) return false;
+  double f1, f2, d;
+  if (!asph_sag_fast(a, 1, H2, f1, d) || !asph_sag_fast(a, 2, H2, f2, d)) return false;
+  return !(p.z < f1 || f2 < p.z);
+}
+
+// ComputeNormal of the mixed path: the same closest-surface choice, but the
+// normal of a face is its exact gradient (-2x F', -2y F', 1) (no atan2 /
+// RotateZ) and the face residuals are FP64 while the comparisons are FP32.
+RBG_D d3 asph_normal_fast(const Asph& a, d3 point, d3 dir) {
+  const double H2 = point.x * point.x + point.y * point.y;
+  const float r = sqrtf((float)H2);
+  float saf[4];
+  saf[0] = a.rseg() ? fabsf(r - (float)a.rmin()) : 3e38f;
+  saf[1] = fabsf(r - (float)a.rmax());
+  double F1, F2, dF1 = 0, dF2 = 0;
+  bool ok1 = asph_sag_fast(a, 1, H2, F1, dF1), ok2 = asph_sag_fast(a, 2, H2, F2, dF2);
+  // |dF/dr| = 2 r |F'|
+  saf[2] = ok1 ? (float)fabs(F1 - point.z) / sqrtf(1.f + 4.f * (float)H2 * (float)(dF1 * dF1)) : 3e38f;
+  saf[3] = ok2 ? (float)fabs(F2 - point.z) / sqrtf(1.f + 4.f * (float)H2 * (float)(dF2 * dF2)) : 3e38f;
+  int i = 0;
+  for (int k = 1; k < 4; ++k)
+    if (saf[k] < saf[i]) i = k;
+  d3 n;
+  if (i <= 1) {
+    if (H2 > 0) {
+      double inv = 1.0 / sqrt(H2);
+      n = mk(point.x * inv, point.y * inv, 0);
+    } else {
+      n = mk(1, 0, 0);
+    }
+  } else {
+    double dF = i == 2 ? dF1 : dF2;
+    if (dF == 0) n = mk(0, 0, 1);
+    else n = normalized(mk(-2 * point.x * dF, -2 * point.y * dF, 1));
+  }
+  if (dot(n, dir) < 0) n = neg(n);
+  return n;
+}
+
+// FP32 screen of DistToInner/DistToOuter: could the wall be hit at a
+// distance <= limit?  Conservative (enlarged z window and radius).
+RBG_D bool asph_wall_maybe(const Asph& a, bool outer, d3 point, d3 dir, double limit) {
+  if (!outer && !a.rseg()) return false;
+  const float R = (float)(outer ? a.rmax() : a.rmin());
+  const float px = (float)point.x, py = (float)point.y, pz = (float)point.z;
+  const float dx = (float)dir.x, dy = (float)dir.y, dz = (float)dir.z;
+  float nsq = dx * dx + dy * dy;
+  if (nsq < 1e-20f) return false;
+  float rsq = px * px + py * py, rdotn = px * dx + py * dy;
+  float b = rdotn / nsq, delta = b * b - (rsq - R * R) / nsq;
+  const float pad = 1e-3f + 1e-5f * (R + fabsf(pz));
+  if (delta < -pad) return false;
+  float sq = sqrtf(fmaxf(delta, 0.f));
+  float t1 = -b + sq, t2 = -b - sq;
+  if (t1 < -pad && t2 < -pad) return false;
+  double zlo = a.P[outer ? RBG_ASPH_F1RMAX : RBG_ASPH_F1RMIN], zhi = a.P[outer ? RBG_ASPH_F2RMAX : RBG_ASPH_F2RMIN];
+  if (isnan(zlo) || isnan(zhi)) return false;
+  float lim = (float)limit + pad;
+  for (int k = 0; k < 2; ++k) {
+    float t = k == 0 ? t1 : t2;
+    if (t < -pad || t > lim) continue;
+    float z = pz + t * dz;
+    if (z >= (float)zlo - pad && z <= (float)zhi + pad) return true;
+  }
+  return false;
+}
+
+template <bool MIXED, unsigned F = kFeatAll>
 RBG_D double asph_surface(const Asph& a, int n, d3 p, d3 d) {
   return MIXED ? asph_dist_surface_mixed(a, n, p, d) : asph_dist_surface(a, n, p, d);
 }
 
-template <bool MIXED = false>
+template <bool MIXED = false, unsigned F = kFeatAll>
 RBG_D double asph_dist4(const Asph& a, d3 p, d3 d) {
   double best = asph_surface<MIXED>(a, 1, p, d);
   double v = asph_surface<MIXED>(a, 2, p, d);
+  if (MIXED) {
+    if (v < best) best = v;
+    if (asph_wall_maybe(a, false, p, d, best)) {
+      v = asph_dist_wall(a, false, p, d);
+      if (v < best) best = v;
+    }
+    if (asph_wall_maybe(a, true, p, d, best)) {
+      v = asph_dist_wall(a, true, p, d);
+      if (v < best) best = v;
+    }
+    return best;
+  }
   if (v < best) best = v;
   v = asph_dist_wall(a, false, p, d);
   if (v < best) best = v;
@@ -735,7 +843,7 @@ RBG_D bool tube_reached_f32(d3 o, d3 d, double rmin, double rmax, double dz) {
   (void)rmin;
 }
 
-template <bool MIXED = false>
+template <bool MIXED = false, unsigned F = kFeatAll>
 RBG_D double asph_dist_out(const Asph& a, d3 p, d3 d) {
   d3 pp = mk(p.x, p.y, p.z - a.P[RBG_ASPH_ORIGIN_Z]);
   if (MIXED) {
@@ -929,14 +1037,71 @@ RBG_D d3 win_normal(const Win& w, d3 point, d3 dir) {
 // --------------------------------------------------------------------
 // dispatch
 // --------------------------------------------------------------------
-RBG_D bool shape_contains(const DevScene& S, int shape, d3 p) {
-  const int type = S.shapes[shape].type;
-  if (type == RBG_SHAPE_ASPHERIC_DISK) return asph_contains(Asph{SP(S, shape)}, p);
-  if (type == RBG_SHAPE_WINSTON_POLY) return win_contains(win_load(SP(S, shape)), p);
-  return csg_contains(S, shape, p);
+// Reciprocal seeded in FP32 and refined by one FP64 Newton step (relative
+// error ~1e-14): the mixed path's replacement for FP64 divisions by the
+// direction cosines.
+RBG_D double rcp_refined(double v) {
+  double r = (double)(1.0f / (float)v);
+  return r * (2.0 - v * r);
 }
 
-template <bool MIXED = false>
+// TGeoBBox distances for the mixed path (slabs; the same crossings the
+// exact-solid method finds for a box).
+RBG_D double box_dist_fast(const double* P, d3 p, d3 d, bool exit, d3& nrm) {
+  const double o[3] = {p.x - P[RBG_BOX_OX], p.y - P[RBG_BOX_OY], p.z - P[RBG_BOX_OZ]};
+  const double dd[3] = {d.x, d.y, d.z};
+  if (exit) {
+    double best = kBig;
+    int axis = -1;
+    for (int k = 0; k < 3; ++k) {
+      if (dd[k] == 0) continue;
+      double plane = dd[k] > 0 ? P[k] : -P[k];
+      double t = (plane - o[k]) * rcp_refined(dd[k]);
+      if (t < best) {
+        best = t;
+        axis = k;
+      }
+    }
+    if (axis < 0 || best <= 0) return kBig;
+    nrm = mk(axis == 0, axis == 1, axis == 2);
+    return best;
+  }
+  double tnear = -kBig, tfar = kBig;
+  int axis = -1;
+  for (int k = 0; k < 3; ++k) {
+    if (dd[k] == 0) {
+      if (fabs(o[k]) > P[k]) return kBig;
+      continue;
+    }
+    double inv = rcp_refined(dd[k]);
+    double ta = (-P[k] - o[k]) * inv, tb = (P[k] - o[k]) * inv;
+    if (ta > tb) {
+      double s = ta;
+      ta = tb;
+      tb = s;
+    }
+    if (ta > tnear) {
+      tnear = ta;
+      axis = k;
+    }
+    tfar = fmin(tfar, tb);
+  }
+  if (axis < 0 || tnear > tfar || tnear <= 0) return kBig;
+  nrm = mk(axis == 0, axis == 1, axis == 2);
+  return tnear;
+}
+
+template <bool MIXED = false, unsigned F = kFeatAll>
+RBG_D bool shape_contains(const DevScene& S, int shape, d3 p) {
+  const int type = S.shapes[shape].type;
+  if (type == RBG_SHAPE_ASPHERIC_DISK)
+    return MIXED ? asph_contains_fast(Asph{SP(S, shape)}, p) : asph_contains(Asph{SP(S, shape)}, p);
+  if (type == RBG_SHAPE_WINSTON_POLY) return (F & kFeatWinston) ? win_contains(win_load(SP(S, shape)), p) : false;
+  if (!(F & kFeatCSG) && type == RBG_SHAPE_BOX) return prim_contains(RBG_SHAPE_BOX, SP(S, shape), p);
+  return (F & kFeatCSG) ? csg_contains(S, shape, p) : false;
+}
+
+template <bool MIXED = false, unsigned F = kFeatAll>
 RBG_D double shape_dist(const DevScene& S, int shape, d3 p, d3 d, bool exit, d3& nrm, unsigned& err) {
   const int type = S.shapes[shape].type;
   if (type == RBG_SHAPE_ASPHERIC_DISK) {
@@ -944,10 +1109,12 @@ RBG_D double shape_dist(const DevScene& S, int shape, d3 p, d3 d, bool exit, d3&
     return exit ? asph_dist4<MIXED>(a, p, d) : asph_dist_out<MIXED>(a, p, d);
   }
   if (type == RBG_SHAPE_WINSTON_POLY) {
+    if (!(F & kFeatWinston)) return kBig;
     Win w = win_load(SP(S, shape));
     return exit ? win_dist_in(w, p, d) : win_dist_out(w, p, d);
   }
-  return csg_dist(S, shape, p, d, exit, nrm, err);
+  if (MIXED && type == RBG_SHAPE_BOX) return box_dist_fast(SP(S, shape), p, d, exit, nrm);
+  return (F & kFeatCSG) ? csg_dist(S, shape, p, d, exit, nrm, err) : kBig;
 }
 
 RBG_D bool is_ageo(int type) { return type == RBG_SHAPE_ASPHERIC_DISK || type == RBG_SHAPE_WINSTON_POLY; }

@@ -12,6 +12,7 @@
 #include <new>
 #include <vector>
 
+#include "trace_features.h"
 #include "scene_internal.h"
 
 namespace {
@@ -584,7 +585,18 @@ struct Builder {
         std::vector<int> items(s->children.begin() + n.child_begin,
                                s->children.begin() + n.child_begin + n.child_count);
         n.bvh_root = bvh_build(items, 0, (int)items.size());
+        s->features |= rbg::kFeatBVH;
       }
+    }
+    for (const auto& sh : s->shapes) {
+      if (sh.type == RBG_SHAPE_WINSTON_POLY) s->features |= rbg::kFeatWinston;
+      else if (sh.type != RBG_SHAPE_BOX && sh.type != RBG_SHAPE_ASPHERIC_DISK) s->features |= rbg::kFeatCSG;
+    }
+    for (const auto& v : s->volumes)
+      if (v.kind == RBG_KIND_LENS) s->features |= rbg::kFeatLens;
+    for (const auto& b : s->borders) {
+      if (b.multilayer >= 0) s->features |= rbg::kFeatMultilayer;
+      if (b.sigma != 0 || b.lambertian) s->features |= rbg::kFeatRough;
     }
     return RBG_OK;
   }

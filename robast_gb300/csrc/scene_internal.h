@@ -6,7 +6,7 @@
 #include "robast_gb.h"
 #include "robast_gb_layout.h"
 
-struct rbg_device_scene;  // defined in trace_common.cuh
+struct rbg_device_scene;  // defined in device_state.cuh
 
 struct rbg_scene {
   // canonical description tables (ids identical to the user description)
@@ -25,6 +25,8 @@ struct rbg_scene {
   std::vector<int32_t> bvh_items;
   // local bounding boxes per shape: lo[3], hi[3]
   std::vector<double> shape_box;
+  // kFeat* bits (trace_features.h) the scene uses
+  uint32_t features = 0;
 
   // device mirror, owned by the CUDA side (capi.cu)
   rbg_device_scene* dev = nullptr;

@@ -20,6 +20,10 @@ namespace rbg {
 
 constexpr int kMixedBlock = 128;
 
+// Instances: F = kFeatAll runs any scene; F = 0 (boxes and aspheric disks,
+// mirrors, obscurations and focal surfaces only, e.g. two-mirror
+// telescopes) compiles every other code path out, which frees registers.
+template <unsigned F>
 __global__ void __launch_bounds__(kMixedBlock) trace_mixed_kernel(DevScene S, KernelRays in, KernelOut out,
                                                                   int64_t n, int limit, int disable_fresnel,
                                                                   uint64_t seed, uint64_t id_offset,
@@ -48,7 +52,7 @@ __global__ void __launch_bounds__(kMixedBlock) trace_mixed_kernel(DevScene S, Ke
         if (mine < (unsigned long long)n) {
           idx = (int64_t)mine;
           if (load_ray(in, out, idx, seed, id_offset, r)) {
-            trace_begin(S, r, nv);
+            trace_begin<true, F>(S, r, nv);
             active = true;
           } else {
             err |= r.err;
@@ -62,7 +66,7 @@ __global__ void __launch_bounds__(kMixedBlock) trace_mixed_kernel(DevScene S, Ke
       continue;
     }
     if (active) {
-      trace_step<true>(S, r, nv, limit, disable_fresnel != 0);
+      trace_step<true, F>(S, r, nv, limit, disable_fresnel != 0);
       if (r.status != RBG_RUN) {
         err |= r.err;
         store_ray(out, idx, r);
@@ -75,23 +79,25 @@ __global__ void __launch_bounds__(kMixedBlock) trace_mixed_kernel(DevScene S, Ke
 
 int launch_mixed(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o,
                  cudaStream_t st, unsigned* err_flags, unsigned long long* counter, int* launches) {
-  static int blocks_per_sm = 0;
+  const bool lean = S.features == 0;
+  auto kernel = lean ? trace_mixed_kernel<0u> : trace_mixed_kernel<kFeatAll>;
+  static int blocks_per_sm[2] = {0, 0};
   static int sms = 0;
-  if (blocks_per_sm == 0) {
+  int& bps = blocks_per_sm[lean ? 1 : 0];
+  if (bps == 0) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return RBG_ERR_CUDA;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return RBG_ERR_CUDA;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, trace_mixed_kernel, kMixedBlock, 0) !=
-        cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, kMixedBlock, 0) != cudaSuccess)
       return RBG_ERR_CUDA;
-    if (blocks_per_sm < 1) blocks_per_sm = 1;
+    if (bps < 1) bps = 1;
   }
   int64_t want = (n + kMixedBlock - 1) / kMixedBlock;
-  int64_t grid = (int64_t)sms * blocks_per_sm;
+  int64_t grid = (int64_t)sms * bps;
   if (want < grid) grid = want;
   if (cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st) != cudaSuccess) return RBG_ERR_CUDA;
-  trace_mixed_kernel<<<(int)grid, kMixedBlock, 0, st>>>(S, in, out, n, o.limit, o.disable_fresnel, o.seed,
-                                                        o.ray_id_offset, err_flags, counter);
+  kernel<<<(int)grid, kMixedBlock, 0, st>>>(S, in, out, n, o.limit, o.disable_fresnel, o.seed, o.ray_id_offset,
+                                            err_flags, counter);
   if (cudaGetLastError() != cudaSuccess) return RBG_ERR_CUDA;
   *launches = 1;
   return RBG_OK;

@@ -22,10 +22,37 @@ RBG_D bool in_fbox(const float* lo, const float* hi, d3 p) {
   return !(p.x < lo[0] || p.x > hi[0] || p.y < lo[1] || p.y > hi[1] || p.z < lo[2] || p.z > hi[2]);
 }
 
+template <bool MIXED = false, unsigned F = kFeatAll>
 RBG_D bool node_contains(const DevScene& S, int k, d3 p) {
   const rbg_node& N = S.nodes[k];
   if (!in_box(N.lo, N.hi, p)) return false;
-  return shape_contains(S, N.shape, to_local(N.m, p));
+  return shape_contains<MIXED, F>(S, N.shape, to_local(N.m, p));
+}
+
+// FP32 segment/box test for the mixed path, enlarged so that it never
+// rejects a box the FP64 test accepts
+template <typename T>
+RBG_D bool seg_box_f32(float ox, float oy, float oz, float ix, float iy, float iz, bool zx, bool zy, bool zz,
+                       float smax, const T* lo, const T* hi) {
+  float t0 = 0.f, t1 = smax;
+  const float o3[3] = {ox, oy, oz}, i3[3] = {ix, iy, iz};
+  const bool z3[3] = {zx, zy, zz};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float l = (float)lo[a], h = (float)hi[a];
+    float pad = 1e-4f + 2e-6f * fmaxf(fabsf(l), fabsf(h));
+    l -= pad;
+    h += pad;
+    if (z3[a]) {
+      if (o3[a] < l || o3[a] > h) return false;
+      continue;
+    }
+    float ta = (l - o3[a]) * i3[a], tb = (h - o3[a]) * i3[a];
+    t0 = fmaxf(t0, fminf(ta, tb));
+    t1 = fminf(t1, fmaxf(ta, tb));
+    if (t0 > t1 * 1.000001f + 1e-4f) return false;
+  }
+  return true;
 }
 
 // segment [0, smax] of the ray against a box
@@ -53,12 +80,13 @@ RBG_D bool seg_box(d3 o, d3 inv, d3 d, double smax, const T* lo, const T* hi) {
 }
 
 // first child (in placement order) of node k containing p, or -1
+template <bool MIXED = false, unsigned F = kFeatAll>
 RBG_D int first_child_containing(const DevScene& S, int k, d3 p) {
   const rbg_node& N = S.nodes[k];
-  if (N.bvh_root < 0) {
+  if (!(F & kFeatBVH) || N.bvh_root < 0) {
     for (int i = 0; i < N.child_count; ++i) {
       int c = S.children[N.child_begin + i];
-      if (node_contains(S, c, p)) return c;
+      if (node_contains<MIXED, F>(S, c, p)) return c;
     }
     return -1;
   }
@@ -72,7 +100,7 @@ RBG_D int first_child_containing(const DevScene& S, int k, d3 p) {
     if (b.left < 0) {
       for (int i = 0; i < b.right; ++i) {
         int c = S.bvh_items[b.item_begin + i];
-        if ((best < 0 || c < best) && node_contains(S, c, p)) best = c;
+        if ((best < 0 || c < best) && node_contains<MIXED, F>(S, c, p)) best = c;
       }
     } else if (sp + 2 <= 32) {
       stack[sp++] = b.left;
@@ -82,26 +110,28 @@ RBG_D int first_child_containing(const DevScene& S, int k, d3 p) {
   return best;
 }
 
+template <bool MIXED = false, unsigned F = kFeatAll>
 RBG_D int locate_down(const DevScene& S, int k, d3 p) {
   for (int depth = 0; depth < 64; ++depth) {
-    int c = first_child_containing(S, k, p);
+    int c = first_child_containing<MIXED, F>(S, k, p);
     if (c < 0) return k;
     k = c;
   }
   return k;
 }
+template <bool MIXED = false, unsigned F = kFeatAll>
 RBG_D int locate_from_top(const DevScene& S, d3 p) {
-  if (!node_contains(S, 0, p)) return -1;
-  return locate_down(S, 0, p);
+  if (!node_contains<MIXED, F>(S, 0, p)) return -1;
+  return locate_down<MIXED, F>(S, 0, p);
 }
 
 // candidate daughter test shared by the scan and the BVH walk
-template <bool MIXED>
+template <bool MIXED, unsigned F = kFeatAll>
 RBG_D void try_child(const DevScene& S, int k, d3 p, d3 d, double& best, int& xnode, bool& enter, d3& nbest,
                      unsigned& err) {
   const rbg_node& K = S.nodes[k];
   d3 nrm = mk(0, 0, 1);
-  double s = shape_dist<MIXED>(S, K.shape, to_local(K.m, p), dir_to_local(K.m, d), false, nrm, err);
+  double s = shape_dist<MIXED, F>(S, K.shape, to_local(K.m, p), dir_to_local(K.m, d), false, nrm, err);
   // ties: leaving the mother first, then the lowest node id (placement order)
   if (s < best || (s == best && enter && k < xnode)) {
     best = s;
@@ -112,7 +142,7 @@ RBG_D void try_child(const DevScene& S, int k, d3 p, d3 d, double& best, int& xn
 }
 
 // TGeoNavigator::FindNextBoundaryAndStep
-template <bool MIXED>
+template <bool MIXED, unsigned F = kFeatAll>
 RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, unsigned& err) {
   const int c = nv.node;
   double best;
@@ -121,7 +151,7 @@ RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, 
   bool enter;
   if (c < 0) {
     const rbg_node& T = S.nodes[0];
-    best = shape_dist<MIXED>(S, T.shape, to_local(T.m, nv.p), dir_to_local(T.m, nv.d), false, nbest, err);
+    best = shape_dist<MIXED, F>(S, T.shape, to_local(T.m, nv.p), dir_to_local(T.m, nv.d), false, nbest, err);
     if (best >= kBig) {
       step = 0;
       nv.xnode = -1;
@@ -131,16 +161,33 @@ RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, 
     enter = true;
   } else {
     const rbg_node& N = S.nodes[c];
-    best = shape_dist<MIXED>(S, N.shape, to_local(N.m, nv.p), dir_to_local(N.m, nv.d), true, nbest, err);
+    best = shape_dist<MIXED, F>(S, N.shape, to_local(N.m, nv.p), dir_to_local(N.m, nv.d), true, nbest, err);
     xnode = c;
     enter = false;
-    d3 inv = mk(1.0 / nv.d.x, 1.0 / nv.d.y, 1.0 / nv.d.z);
-    if (N.bvh_root < 0) {
+    d3 inv = mk(0, 0, 0);
+    float fo[3], fi[3];
+    bool fz[3];
+    if (MIXED) {
+      const double dd[3] = {nv.d.x, nv.d.y, nv.d.z}, pp[3] = {nv.p.x, nv.p.y, nv.p.z};
+      for (int a = 0; a < 3; ++a) {
+        fo[a] = (float)pp[a];
+        fz[a] = dd[a] == 0;
+        fi[a] = fz[a] ? 0.f : 1.0f / (float)dd[a];
+      }
+    } else {
+      inv = mk(1.0 / nv.d.x, 1.0 / nv.d.y, 1.0 / nv.d.z);
+    }
+    auto culled = [&](auto lo, auto hi) {
+      if (MIXED) return !seg_box_f32(fo[0], fo[1], fo[2], fi[0], fi[1], fi[2], fz[0], fz[1], fz[2],
+                                     best >= kBig ? 3e38f : (float)best, lo, hi);
+      return !seg_box(nv.p, inv, nv.d, best, lo, hi);
+    };
+    if (!(F & kFeatBVH) || N.bvh_root < 0) {
       for (int i = 0; i < N.child_count; ++i) {
         int k = S.children[N.child_begin + i];
         const rbg_node& K = S.nodes[k];
-        if (!seg_box(nv.p, inv, nv.d, best, K.lo, K.hi)) continue;
-        try_child<MIXED>(S, k, nv.p, nv.d, best, xnode, enter, nbest, err);
+        if (culled(K.lo, K.hi)) continue;
+        try_child<MIXED, F>(S, k, nv.p, nv.d, best, xnode, enter, nbest, err);
       }
     } else {
       int stack[32];
@@ -148,13 +195,13 @@ RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, 
       stack[sp++] = N.bvh_root;
       while (sp > 0) {
         const rbg_bvh_node& b = S.bvh[stack[--sp]];
-        if (!seg_box(nv.p, inv, nv.d, best, b.lo, b.hi)) continue;
+        if (culled(b.lo, b.hi)) continue;
         if (b.left < 0) {
           for (int i = 0; i < b.right; ++i) {
             int k = S.bvh_items[b.item_begin + i];
             const rbg_node& K = S.nodes[k];
-            if (!seg_box(nv.p, inv, nv.d, best, K.lo, K.hi)) continue;
-            try_child<MIXED>(S, k, nv.p, nv.d, best, xnode, enter, nbest, err);
+            if (culled(K.lo, K.hi)) continue;
+            try_child<MIXED, F>(S, k, nv.p, nv.d, best, xnode, enter, nbest, err);
           }
         } else if (sp + 2 <= 32) {
           stack[sp++] = b.right;
@@ -170,11 +217,11 @@ RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, 
   nv.xn = nbest;
   int next;
   if (enter) {
-    next = locate_down(S, xnode, nv.p);
+    next = locate_down<MIXED, F>(S, xnode, nv.p);
   } else {
     int q = S.nodes[c].parent;
-    while (q >= 0 && !node_contains(S, q, nv.p)) q = S.nodes[q].parent;
-    next = q < 0 ? -1 : locate_down(S, q, nv.p);
+    while (q >= 0 && !node_contains<MIXED, F>(S, q, nv.p)) q = S.nodes[q].parent;
+    next = q < 0 ? -1 : locate_down<MIXED, F>(S, q, nv.p);
   }
   nv.node = next;
   step = best;
@@ -182,13 +229,16 @@ RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, 
 }
 
 // TGeoNavigator::FindNormal: master-frame normal, n . d >= 0
+template <bool MIXED = false, unsigned F = kFeatAll>
 RBG_D d3 find_normal(const DevScene& S, const Nav& nv) {
   if (nv.xnode < 0) return mk(0, 0, 1);
   const rbg_node& N = S.nodes[nv.xnode];
   const int type = S.shapes[N.shape].type;
   d3 nl;
   if (type == RBG_SHAPE_ASPHERIC_DISK) {
-    nl = asph_normal(Asph{SP(S, N.shape)}, to_local(N.m, nv.p), dir_to_local(N.m, nv.d));
+    Asph a{SP(S, N.shape)};
+    d3 pl = to_local(N.m, nv.p), dl = dir_to_local(N.m, nv.d);
+    nl = MIXED ? asph_normal_fast(a, pl, dl) : asph_normal(a, pl, dl);
   } else if (type == RBG_SHAPE_WINSTON_POLY) {
     nl = win_normal(win_load(SP(S, N.shape)), to_local(N.m, nv.p), dir_to_local(N.m, nv.d));
   } else {
@@ -350,7 +400,7 @@ RBG_D void coherent_tmm(const DevScene& S, int ml, int pol, double th0r, double 
   else Tr = (double)(tt2 * ((nf * C{ctf.re, -ctf.im}).re / (n0 * C{ct0.re, -ct0.im}).re));
 }
 
-template <bool MIXED>
+template <bool MIXED, unsigned F = kFeatAll>
 RBG_D void coherent_tmm_mixed(const DevScene& S, int ml, double th0, double lam, double& R, double& T) {
   double rp, tp, rs, ts;
   if (MIXED) {
@@ -413,6 +463,17 @@ RBG_D void set_direction(Ray& r, d3 v) {
   double mag = sqrt(dot(v, v));
   if (mag > 0) r.d = mk(v.x / mag, v.y / mag, v.z / mag);
 }
+// ARay::SetDirection for a vector that is unit to ~1e-8 (a reflected unit
+// vector): first-order inverse square root, no FP64 sqrt or division
+RBG_D void set_direction_fast(Ray& r, d3 v) {
+  double m2 = dot(v, v);
+  if (fabs(m2 - 1.0) < 1e-8) {
+    double s = 1.5 - 0.5 * m2;
+    r.d = mk(v.x * s, v.y * s, v.z * s);
+  } else {
+    set_direction(r, v);
+  }
+}
 
 enum { kLens = 0, kObs = 1, kMirror = 2, kFocus = 3, kOpt = 4, kOther = 5, kNull = 6 };
 RBG_D int kind_of(const DevScene& S, int node) { return node < 0 ? kNull : S.nodes[node].kind; }
@@ -442,9 +503,10 @@ RBG_D d3 rotate_uz(d3 v, d3 u) {
 }
 
 // GetFacetNormal (:250-301)
-template <bool MIXED>
+template <bool MIXED, unsigned F = kFeatAll>
 RBG_D d3 get_facet_normal(const DevScene& S, const Nav& nv, Ray& r, int cur, int next) {
-  d3 normal = find_normal(S, nv);
+  d3 normal = find_normal<MIXED, F>(S, nv);
+  if (!(F & kFeatRough)) return normal;
   int bi = find_border(S, cur, next);
   if (bi < 0) return normal;
   const rbg_border_desc B = S.borders[bi];
@@ -490,18 +552,23 @@ RBG_D d3 euler_apply(double phi, double theta, double psi, d3 v) {
 }
 
 // DoReflection (:170-247); `normal` may be null (computed here)
-template <bool MIXED>
+template <bool MIXED, unsigned F = kFeatAll>
 RBG_D void do_reflection(const DevScene& S, Nav& nv, Ray& r, double n1, double step, int cur, int next,
                          const d3* normal) {
-  d3 n = normal ? *normal : get_facet_normal<MIXED>(S, nv, r, cur, next);
+  d3 n = normal ? *normal : get_facet_normal<MIXED, F>(S, nv, r, cur, next);
   const d3 d1 = r.d;
   double cos1 = dot(d1, n);
-  int bi = find_border(S, cur, next);
+  int bi = (F & (kFeatMultilayer | kFeatRough)) ? find_border(S, cur, next) : -1;
   bool absorbed = false;
   if (kind_of(S, next) == kMirror) {
-    double angle = acos(cos1);
+    const rbg_volume_desc& mv = S.volumes[S.nodes[next].volume];
+    // the incidence angle only matters for 2D tables and thin films
+    const bool need_angle =
+        !MIXED || (bi >= 0 && S.borders[bi].multilayer >= 0) ||
+        (mv.refl_table >= 0 && S.tables[mv.refl_table].kind == RBG_TABLE_2D);
+    double angle = need_angle ? acos(cos1) : 0.0;
     double ref;
-    if (bi >= 0 && S.borders[bi].multilayer >= 0) {
+    if ((F & kFeatMultilayer) && bi >= 0 && S.borders[bi].multilayer >= 0) {
       double tr;
       coherent_tmm_mixed<MIXED>(S, S.borders[bi].multilayer, angle, r.lambda, ref, tr);
     } else {
@@ -520,7 +587,7 @@ RBG_D void do_reflection(const DevScene& S, Nav& nv, Ray& r, double n1, double s
     }
   }
   d3 d2;
-  if (bi >= 0 && S.borders[bi].lambertian) {
+  if ((F & kFeatRough) && bi >= 0 && S.borders[bi].lambertian) {
     double y = 0.5 * rng_u(r);
     double theta = asin(sqrt(2 * y));
     double phi = 2 * kPi * rng_u(r);
@@ -531,10 +598,13 @@ RBG_D void do_reflection(const DevScene& S, Nav& nv, Ray& r, double n1, double s
   } else {
     d2 = d1 - (2 * cos1) * n;
   }
-  if (!absorbed) set_direction(r, d2);
-  double t = r.t + step / (RBG_SPEED_OF_LIGHT_CM / n1);
+  if (!absorbed) {
+    if (MIXED) set_direction_fast(r, d2);
+    else set_direction(r, d2);
+  }
+  double t = MIXED ? r.t + step * (n1 * (1.0 / RBG_SPEED_OF_LIGHT_CM)) : r.t + step / (RBG_SPEED_OF_LIGHT_CM / n1);
   nv.p = nv.p - RBG_REFLECT_BACKSTEP * d1;
-  nv.node = locate_from_top(S, nv.p);
+  nv.node = locate_from_top<MIXED, F>(S, nv.p);
   nv.d = d2;
   add_point(r, nv.p, t);
   add_node(r, next);
@@ -567,10 +637,10 @@ RBG_D double fresnel_R(T n1, T n2, T k2, T cos1, T sin1, T cos2) {
 }
 
 // DoFresnel (:52-167)
-template <bool MIXED>
+template <bool MIXED, unsigned F = kFeatAll>
 RBG_D void do_fresnel(const DevScene& S, Nav& nv, Ray& r, double n1, double n2, double k2, double step, int cur,
                       int next, bool disable_fresnel) {
-  d3 n = get_facet_normal<MIXED>(S, nv, r, cur, next);
+  d3 n = get_facet_normal<MIXED, F>(S, nv, r, cur, next);
   const d3 d1 = r.d;
   double cos1 = dot(d1, n);
   double sin1 = sqrt(1 - cos1 * cos1);
@@ -584,7 +654,7 @@ RBG_D void do_fresnel(const DevScene& S, Nav& nv, Ray& r, double n1, double n2, 
     coherent_tmm_mixed<MIXED>(S, S.borders[bi].multilayer, acos(cos1), r.lambda, refl, trans);
     double rnd = rng_u(r);
     if (rnd < refl) {
-      do_reflection<MIXED>(S, nv, r, n1, step, cur, next, &n);
+      do_reflection<MIXED, F>(S, nv, r, n1, step, cur, next, &n);
       return;
     }
     absorbed = !(rnd < refl + trans);
@@ -592,14 +662,14 @@ RBG_D void do_fresnel(const DevScene& S, Nav& nv, Ray& r, double n1, double n2, 
   }
   if (!transmit) {
     if (sin2 > 1.) {
-      do_reflection<MIXED>(S, nv, r, n1, step, cur, next, &n);
+      do_reflection<MIXED, F>(S, nv, r, n1, step, cur, next, &n);
       return;
     }
     if (!disable_fresnel) {
       double R = MIXED ? fresnel_R<float>((float)n1, (float)n2, (float)k2, (float)cos1, (float)sin1, (float)cos2)
                        : fresnel_R<double>(n1, n2, k2, cos1, sin1, cos2);
       if (rng_u(r) < R) {
-        do_reflection<MIXED>(S, nv, r, n1, step, cur, next, &n);
+        do_reflection<MIXED, F>(S, nv, r, n1, step, cur, next, &n);
         return;
       }
     }
@@ -619,15 +689,16 @@ RBG_D void do_fresnel(const DevScene& S, Nav& nv, Ray& r, double n1, double n2, 
 // TraceNonSequential(TObjArray*) body for one ray (:346-518), split into
 // InitTrack and one iteration of the while (ray->IsRunning()) loop so that
 // a persistent kernel can interleave rays
+template <bool MIXED = false, unsigned F = kFeatAll>
 RBG_D void trace_begin(const DevScene& S, Ray& r, Nav& nv) {
   nv.p = r.x;
   nv.d = r.d;
-  nv.node = locate_from_top(S, nv.p);
+  nv.node = locate_from_top<MIXED, F>(S, nv.p);
   nv.xnode = -1;
   nv.xn = mk(0, 0, 1);
 }
 
-template <bool MIXED>
+template <bool MIXED, unsigned F = kFeatAll>
 RBG_D void trace_step(const DevScene& S, Ray& r, Nav& nv, int limit, bool disable_fresnel) {
   const double lambda = r.lambda;
   const d3 x1 = r.x;
@@ -635,10 +706,10 @@ RBG_D void trace_step(const DevScene& S, Ray& r, Nav& nv, int limit, bool disabl
   const d3 d1 = r.d;
   const int cur = nv.node;
   double step;
-  const int next = find_next_boundary_and_step<MIXED>(S, nv, step, r.err);
+  const int next = find_next_boundary_and_step<MIXED, F>(S, nv, step, r.err);
   const int tc = kind_of(S, cur), tn = kind_of(S, next);
 
-  if (tc == kLens) {
+  if ((F & kFeatLens) && tc == kLens) {
     int idx = S.volumes[S.nodes[cur].volume].index;
     double k = index_k(S, idx, lambda);
     double abs_len = k <= 0. ? INFINITY : lambda / (4 * kPi * k);
@@ -655,25 +726,25 @@ RBG_D void trace_step(const DevScene& S, Ray& r, Nav& nv, int limit, bool disabl
   }
 
   if ((tc == kNull || tc == kOpt || tc == kLens || tc == kOther) && tn == kMirror) {
-    double n1 = tc == kLens ? lens_n(S, cur, lambda) : 1.;
-    do_reflection<MIXED>(S, nv, r, n1, step, cur, next, nullptr);
-  } else if ((tc == kNull || tc == kOpt || tc == kOther) && tn == kLens) {
+    double n1 = ((F & kFeatLens) && tc == kLens) ? lens_n(S, cur, lambda) : 1.;
+    do_reflection<MIXED, F>(S, nv, r, n1, step, cur, next, nullptr);
+  } else if ((F & kFeatLens) && (tc == kNull || tc == kOpt || tc == kOther) && tn == kLens) {
     int idx = S.volumes[S.nodes[next].volume].index;
-    do_fresnel<MIXED>(S, nv, r, 1, index_n(S, idx, lambda), index_k(S, idx, lambda), step, cur, next,
+    do_fresnel<MIXED, F>(S, nv, r, 1, index_n(S, idx, lambda), index_k(S, idx, lambda), step, cur, next,
                       disable_fresnel);
   } else if ((tc == kNull || tc == kLens || tc == kOpt || tc == kOther) && (tn == kObs || tn == kFocus)) {
-    double speed = tc == kLens ? RBG_SPEED_OF_LIGHT_CM / lens_n(S, cur, lambda) : RBG_SPEED_OF_LIGHT_CM;
+    double speed = ((F & kFeatLens) && tc == kLens) ? RBG_SPEED_OF_LIGHT_CM / lens_n(S, cur, lambda) : RBG_SPEED_OF_LIGHT_CM;
     add_point(r, nv.p, t1 + step / speed);
     add_node(r, next);
   } else if ((tc == kNull || tc == kOpt || tc == kOther) && (tn == kOther || tn == kOpt)) {
     add_point(r, nv.p, t1 + step / RBG_SPEED_OF_LIGHT_CM);
     add_node(r, next);
-  } else if (tc == kLens && tn == kLens) {
+  } else if ((F & kFeatLens) && tc == kLens && tn == kLens) {
     int idx = S.volumes[S.nodes[next].volume].index;
-    do_fresnel<MIXED>(S, nv, r, lens_n(S, cur, lambda), index_n(S, idx, lambda), index_k(S, idx, lambda), step,
+    do_fresnel<MIXED, F>(S, nv, r, lens_n(S, cur, lambda), index_n(S, idx, lambda), index_k(S, idx, lambda), step,
                       cur, next, disable_fresnel);
-  } else if (tc == kLens && (tn == kNull || tn == kOpt || tn == kOther)) {
-    do_fresnel<MIXED>(S, nv, r, lens_n(S, cur, lambda), 1, 0, step, cur, next, disable_fresnel);
+  } else if ((F & kFeatLens) && tc == kLens && (tn == kNull || tn == kOpt || tn == kOther)) {
+    do_fresnel<MIXED, F>(S, nv, r, lens_n(S, cur, lambda), 1, 0, step, cur, next, disable_fresnel);
   }
 
   if (tn == kNull) {
@@ -686,7 +757,7 @@ RBG_D void trace_step(const DevScene& S, Ray& r, Nav& nv, int limit, bool disabl
     const rbg_volume_desc& v = S.volumes[S.nodes[next].volume];
     double angle = 0.;
     if (v.qe_angle_table >= 0) {
-      d3 n = get_facet_normal<MIXED>(S, nv, r, cur, next);
+      d3 n = get_facet_normal<MIXED, F>(S, nv, r, cur, next);
       angle = acos(dot(r.d, n));
     }
     double qe = v.qe_lambda_table >= 0 ? table1d(S, v.qe_lambda_table, lambda) : 1.;
@@ -697,11 +768,11 @@ RBG_D void trace_step(const DevScene& S, Ray& r, Nav& nv, int limit, bool disabl
   if (r.status == RBG_RUN && r.npoints >= limit) r.status = RBG_SUSPEND;
 }
 
-template <bool MIXED>
+template <bool MIXED, unsigned F = kFeatAll>
 RBG_D void trace_ray(const DevScene& S, Ray& r, int limit, bool disable_fresnel) {
   Nav nv;
-  trace_begin(S, r, nv);
-  while (r.status == RBG_RUN) trace_step<MIXED>(S, r, nv, limit, disable_fresnel);
+  trace_begin<MIXED, F>(S, r, nv);
+  while (r.status == RBG_RUN) trace_step<MIXED, F>(S, r, nv, limit, disable_fresnel);
 }
 
 // ---------------------------------------------------------------------
