@@ -39,7 +39,8 @@ enum {
   RBG_ERR_CAP = 5,         /* a bounded device loop hit its iteration cap */
   RBG_ERR_UNSUPPORTED = 6, /* feature outside this build (e.g. AGeo shape in CSG) */
   RBG_ERR_NOMEM = 7,       /* allocation failed */
-  RBG_ERR_NODEVICE = 8     /* no CUDA device visible */
+  RBG_ERR_NODEVICE = 8,    /* no CUDA device visible */
+  RBG_ERR_TOO_LARGE = 9    /* scene exceeds rbg_trace_noalloc's fixed array */
 };
 
 /* ---- per-ray fate: same values and order as ARay's private enum
@@ -308,6 +309,22 @@ int rbg_trace(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
  * src/AOpticsManager.cxx:523). */
 int rbg_trace_host(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
                    const rbg_trace_opts* opts);
+
+/* rbg_trace without any device allocation (no counterpart in the reference:
+ * ROBAST traces on host threads).  For callers that cannot let a library
+ * allocate or free device memory -- a real-time camera trigger or DAQ chain
+ * or a serving process that owns all device memory in a fixed budget, where
+ * cudaMalloc may fail and cudaFree would synchronise the whole device.  The
+ * scene tables, the error word and the ray-queue counter live in one
+ * statically allocated device array of 4 MiB (held by every GPU that loads
+ * the library until exit); scenes whose flattened tables exceed it return
+ * RBG_ERR_TOO_LARGE.  Buffers as rbg_trace (DEVICE rays and results); only
+ * opts->precision == RBG_PREC_MIXED is accepted.  Calls share the array and
+ * it keeps the last call's contents: calls that overlap on the GPU race.
+ * The first call on a device looks up the array's address with that device
+ * current; make it before any stream capture begins. */
+int rbg_trace_noalloc(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
+                      const rbg_trace_opts* opts, void* stream);
 
 /* Number of tracer kernel launches the last rbg_trace on this scene issued
  * (1 for either precision: the whole batch is one launch). */

@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(BUILD_DIR, "librobast_gb.so")
 # ---- constants (robast_gb.h) -------------------------------------------
 RBG_OK, RBG_ERR_ARG, RBG_ERR_SCENE, RBG_ERR_CUDA, RBG_ERR_NAN = 0, 1, 2, 3, 4
 RBG_ERR_CAP, RBG_ERR_UNSUPPORTED, RBG_ERR_NOMEM, RBG_ERR_NODEVICE = 5, 6, 7, 8
+RBG_ERR_TOO_LARGE = 9
 
 RBG_RUN, RBG_STOP, RBG_EXIT, RBG_FOCUS, RBG_SUSPEND, RBG_ABSORB = range(6)
 

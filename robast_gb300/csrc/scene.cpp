@@ -619,6 +619,7 @@ const char* rbg_status_string(int status) {
     case RBG_ERR_UNSUPPORTED: return "unsupported feature";
     case RBG_ERR_NOMEM: return "out of memory";
     case RBG_ERR_NODEVICE: return "no CUDA device";
+    case RBG_ERR_TOO_LARGE: return "scene larger than the no-allocation trace array (4 MiB)";
     default: return "unknown status";
   }
 }
