@@ -72,7 +72,9 @@ int ensure_device(rbg_scene* s) {
       (rc = upload(d->allocations, s->layers, &v.layers)) ||
       (rc = upload(d->allocations, s->multilayers, &v.multilayers)) ||
       (rc = upload(d->allocations, s->borders, &v.borders)) ||
-      (rc = upload(d->allocations, s->params, &v.params))) {
+      (rc = upload(d->allocations, s->params, &v.params)) ||
+      (rc = upload(d->allocations, s->node_aux, &v.aux)) ||
+      (rc = upload(d->allocations, s->fparams, &v.fparams))) {
     for (void* p : d->allocations) cudaFree(p);
     delete d;
     return rc;

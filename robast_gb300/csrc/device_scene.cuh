@@ -7,6 +7,7 @@
 #include "philox.h"
 #include "robast_gb.h"
 #include "robast_gb_layout.h"
+#include "node_aux.h"
 
 #define RBG_D __device__ __forceinline__
 
@@ -25,6 +26,10 @@ struct DevScene {
   const rbg_multilayer_desc* multilayers;
   const rbg_border_desc* borders;
   const double* params;
+  // mixed-precision tracer only: per-node float boxes and transform kind,
+  // float copy of params (same offsets)
+  const rbg_node_aux* aux;
+  const float* fparams;
   int32_t n_nodes, n_borders, n_multilayers, n_tables;
   uint32_t features;  // kFeat* bits present in the scene
 };

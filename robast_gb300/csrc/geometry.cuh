@@ -745,7 +745,7 @@ RBG_D bool asph_wall_maybe(const Asph& a, bool outer, d3 point, d3 dir, double l
   if (nsq < 1e-20f) return false;
   float rsq = px * px + py * py, rdotn = px * dx + py * dy;
   float b = rdotn / nsq, delta = b * b - (rsq - R * R) / nsq;
-  const float pad = 1e-3f + 1e-5f * (R + fabsf(pz));
+  const float pad = 1e-3f + 1e-5f * (R + fabsf(px) + fabsf(py) + fabsf(pz));
   if (delta < -pad) return false;
   float sq = sqrtf(fmaxf(delta, 0.f));
   float t1 = -b + sq, t2 = -b - sq;
@@ -1118,5 +1118,349 @@ RBG_D double shape_dist(const DevScene& S, int shape, d3 p, d3 d, bool exit, d3&
 }
 
 RBG_D bool is_ageo(int type) { return type == RBG_SHAPE_ASPHERIC_DISK || type == RBG_SHAPE_WINSTON_POLY; }
+
+// ====================================================================
+// Mixed-precision fast paths.
+//
+// The mixed tracer spends its time in the FP64 pipe, which on this part
+// runs at 1/64 of the FP32 rate, and in instruction fetch.  The functions
+// below keep every decision the FP64 algorithm makes, but take it with an
+// FP32 screen where the screen's error bound leaves no doubt, and fall back
+// to the exact FP64 test (compiled once, out of line) where it does.  The
+// ray's float position and direction are converted once per step and
+// passed along with the FP64 ones.
+// ====================================================================
+#define RBG_NOINLINE static __device__ __noinline__
+
+struct f3 {
+  float x, y, z;
+};
+RBG_D f3 to_f3(d3 a) { return f3{(float)a.x, (float)a.y, (float)a.z}; }
+
+// a ray (or point, with d unused) in a node's local frame, FP64 and FP32
+struct LRay {
+  d3 p, d;
+  f3 pf, df;
+};
+
+// master -> local for node k, using its transform kind.  The float local
+// point is always converted from the FP64 local point, so its error stays
+// relative to the local coordinates the screens compare.
+RBG_D LRay local_ray(const DevScene& S, int k, d3 p, d3 d, f3 pf, f3 df) {
+  const int xf = S.aux[k].xform;
+  if (xf == RBG_XFORM_IDENTITY) return LRay{p, d, pf, df};
+  const rbg_node& N = S.nodes[k];
+  if (xf == RBG_XFORM_TRANSLATION) {
+    d3 lp = mk(p.x - N.m[9], p.y - N.m[10], p.z - N.m[11]);
+    return LRay{lp, d, to_f3(lp), df};
+  }
+  d3 lp = to_local(N.m, p), ld = dir_to_local(N.m, d);
+  return LRay{lp, ld, to_f3(lp), to_f3(ld)};
+}
+RBG_D LRay local_point(const DevScene& S, int k, d3 p, f3 pf) {
+  const int xf = S.aux[k].xform;
+  if (xf == RBG_XFORM_IDENTITY) return LRay{p, p, pf, pf};
+  const rbg_node& N = S.nodes[k];
+  d3 lp = xf == RBG_XFORM_TRANSLATION ? mk(p.x - N.m[9], p.y - N.m[10], p.z - N.m[11]) : to_local(N.m, p);
+  f3 lpf = to_f3(lp);
+  return LRay{lp, lp, lpf, lpf};
+}
+
+// 1/sqrt(m2) for m2 >= ~1e-30: FP32 seed, two FP64 Newton steps
+// (relative error 2^-23 -> ~1e-14 -> FP64 rounding)
+RBG_D double rsqrt_refined(double m2) {
+  double r = (double)rsqrtf((float)m2);
+  double h = 0.5 * m2;
+  r = r * (1.5 - h * r * r);
+  r = r * (1.5 - h * r * r);
+  return r;
+}
+
+// sum_{j<n} K_j h^(j+1) (the polynomial part of CalcF1/CalcF2) with FMAs
+RBG_D double asph_poly(const double* K, int n, double h) {
+  if (n <= 0) return 0.0;
+  double q = K[n - 1];
+  for (int j = n - 2; j >= 0; --j) q = fma(q, h, K[j]);
+  return q * h;
+}
+// sum_{j<n} (j+1) K_j h^j = d poly / d h
+RBG_D double asph_dpoly(const double* K, int n, double h) {
+  if (n <= 0) return 0.0;
+  double q = n * K[n - 1];
+  for (int j = n - 2; j >= 0; --j) q = fma(q, h, (j + 1) * K[j]);
+  return q;
+}
+// FP32 sag of a face with c == 0 and the sum of its terms' magnitudes
+// (the scale of its rounding error)
+RBG_D float asph_poly_f(const float* K, int n, float h, float& mag) {
+  float q = 0.f, m = 0.f;
+  for (int j = n - 1; j >= 0; --j) {
+    q = (q + K[j]) * h;
+    m = (m + fabsf(K[j])) * h;
+  }
+  mag = m;
+  return q;
+}
+
+// the FP64 reference algorithms, out of line: taken only when a screen
+// cannot decide or the FP32 iteration breaks down
+RBG_NOINLINE double asph_dist_surface_exact(const double* P, int n, d3 point, d3 dir) {
+  return asph_dist_surface(Asph{P}, n, point, dir);
+}
+RBG_NOINLINE double asph_dist_wall_exact(const double* P, bool outer, d3 point, d3 dir) {
+  return asph_dist_wall(Asph{P}, outer, point, dir);
+}
+RBG_NOINLINE bool asph_contains_exact(const double* P, d3 p) { return asph_contains_fast(Asph{P}, p); }
+RBG_NOINLINE d3 asph_normal_exact(const double* P, d3 point, d3 dir) {
+  return asph_normal_fast(Asph{P}, point, dir);
+}
+
+// DistToAsphere (src/AGeoAsphericDisk.cxx:415-526), mixed precision: the
+// reference's iteration (spherical first guess, Newton along the ray) in
+// FP32 from the float parameters, relative to the face vertex, tracking the
+// distance t; then FP64 polish steps t += s (x(h2) - z) with the FP32 slope
+// s until |step| < 1e-10 (the reference's stopping rule).  The distance is
+// t itself (the reference's |np - point| for a unit direction), rejected
+// when t < 0 (its dot(dir, np - point) < 0) or when the hit radius lies
+// outside [rmin, rmax] (compared squared).
+RBG_D double asph_dist_surface_f(const double* P, const float* Pf, int n, const LRay& L) {
+  const int npol1 = (int)Pf[RBG_ASPH_NPOL1];
+  const int npol = n == 1 ? npol1 : (int)Pf[RBG_ASPH_NPOL2];
+  const float* Kf = Pf + RBG_ASPH_K + (n == 1 ? 0 : npol1);
+  const float curve = Pf[n == 1 ? RBG_ASPH_C1 : RBG_ASPH_C2], kappa = Pf[n == 1 ? RBG_ASPH_KAPPA1 : RBG_ASPH_KAPPA2];
+  const float px = L.pf.x, py = L.pf.y, pz = L.pf.z - Pf[n == 1 ? RBG_ASPH_Z1 : RBG_ASPH_Z2];
+  const float dx = L.df.x, dy = L.df.y, dz = L.df.z;
+  float H2 = px * px + py * py;
+  float p = -(pz * dz + px * dx + py * dy);
+  float M = p * dz + pz;
+  float M2 = pz * pz + H2 - p * p;
+  float check = 1.f - (M2 * curve - 2.f * M) * curve / dz / dz;
+  if (!(check >= 0.f)) return asph_dist_surface_exact(P, n, L.p, L.d);
+  float tf = p + (M2 * curve - 2.f * M) / (dz * (1.f + sqrtf(check)));
+  float nx = px + tf * dx, ny = py + tf * dy, nz = pz + tf * dz;
+  float scale = 1.f;
+  bool ok = false;
+  for (int i = 0; i < 40; i++) {
+    H2 = nx * nx + ny * ny;
+    check = 1.f - kappa * H2 * curve * curve;
+    if (check < 0) break;
+    float l = sqrtf(check);
+    float x = 0.f, v = 0.f;
+    for (int j = npol - 1; j >= 0; --j) {
+      x = (x + Kf[j]) * H2;
+      v = v * H2 + 2.f * (j + 1) * Kf[j];
+    }
+    if (curve != 0.f) x += (1.f - l) / curve / kappa;
+    v = curve * kappa + l * v;
+    float m = -nx * v, nn = -ny * v;
+    float norm = sqrtf(l * l + m * m + nn * nn);
+    l /= norm;
+    m /= norm;
+    nn /= norm;
+    check = dz * l + dx * m + dy * nn;
+    if (check == 0.f) break;
+    scale = l / check;  // dt per unit sag residual
+    float e = scale * (x - nz);
+    tf += e;
+    nx += e * dx;
+    ny += e * dy;
+    nz += e * dz;
+    if (fabsf(e) < 4e-6f * (1.f + fabsf(nz) + sqrtf(H2))) {
+      ok = true;
+      break;
+    }
+  }
+  if (!ok || !isfinite(tf)) return asph_dist_surface_exact(P, n, L.p, L.d);
+  const int s1 = n == 1;
+  const double* K = P + RBG_ASPH_K + (s1 ? 0 : npol1);
+  const double c64 = P[s1 ? RBG_ASPH_C1 : RBG_ASPH_C2];
+  const double kap64 = P[s1 ? RBG_ASPH_KAPPA1 : RBG_ASPH_KAPPA2];
+  const double pz0 = L.p.z - P[s1 ? RBG_ASPH_Z1 : RBG_ASPH_Z2];
+  const double sc = (double)scale;
+  double t = (double)tf;
+  bool conv = false;
+  for (int it = 0; it < 8; ++it) {
+    double qx = fma(t, L.d.x, L.p.x), qy = fma(t, L.d.y, L.p.y), qz = fma(t, L.d.z, pz0);
+    double h2 = fma(qx, qx, qy * qy);
+    double x = asph_poly(K, npol, h2);
+    if (c64 != 0) {
+      double chk = 1 - kap64 * h2 * c64 * c64;
+      if (chk < 0) return asph_dist_surface_exact(P, n, L.p, L.d);
+      x += (1 - sqrt(chk)) / c64 / kap64;
+    }
+    double e = sc * (x - qz);
+    t += e;
+    if (fabs(e) < 1e-10) {
+      conv = true;
+      break;
+    }
+  }
+  if (!conv) return asph_dist_surface_exact(P, n, L.p, L.d);
+  if (t < 0) return kBig;
+  double qx = fma(t, L.d.x, L.p.x), qy = fma(t, L.d.y, L.p.y);
+  double h2 = fma(qx, qx, qy * qy);
+  const double rmin = P[RBG_ASPH_RMIN], rmax = P[RBG_ASPH_RMAX];
+  if (h2 < rmin * rmin || h2 > rmax * rmax) return kBig;
+  return t;
+}
+
+// FP32 screen of DistToInner/DistToOuter from the float parameters (the
+// test asph_wall_maybe makes, without conversions)
+RBG_D bool asph_wall_maybe_f(const float* Pf, bool outer, const LRay& L, float limit) {
+  if (!outer && Pf[RBG_ASPH_RSEG] == 0.f) return false;
+  const float R = outer ? Pf[RBG_ASPH_RMAX] : Pf[RBG_ASPH_RMIN];
+  const float px = L.pf.x, py = L.pf.y, pz = L.pf.z;
+  const float dx = L.df.x, dy = L.df.y, dz = L.df.z;
+  float nsq = dx * dx + dy * dy;
+  if (nsq < 1e-20f) return false;
+  float rsq = px * px + py * py, rdotn = px * dx + py * dy;
+  float b = rdotn / nsq, delta = b * b - (rsq - R * R) / nsq;
+  const float pad = 1e-3f + 1e-5f * (R + fabsf(pz));
+  if (delta < -pad) return false;
+  float sq = sqrtf(fmaxf(delta, 0.f));
+  float t1 = -b + sq, t2 = -b - sq;
+  if (t1 < -pad && t2 < -pad) return false;
+  const float zlo = Pf[outer ? RBG_ASPH_F1RMAX : RBG_ASPH_F1RMIN];
+  const float zhi = Pf[outer ? RBG_ASPH_F2RMAX : RBG_ASPH_F2RMIN];
+  if (isnan(zlo) || isnan(zhi)) return false;
+  float lim = limit + pad + 1e-5f * limit;
+  for (int k = 0; k < 2; ++k) {
+    float t = k == 0 ? t1 : t2;
+    if (t < -pad - 1e-5f * fabsf(t) || t > lim) continue;
+    float z = pz + t * dz;
+    if (z >= zlo - pad && z <= zhi + pad) return true;
+  }
+  return false;
+}
+
+// DistFromInside (:363-380): nearest of the two faces and the two walls;
+// `face` = 1, 2 (faces), 3 (inner wall), 4 (outer wall) of the minimum
+RBG_D double asph_dist4_f(const double* P, const float* Pf, const LRay& L, int& face) {
+  double best = asph_dist_surface_f(P, Pf, 1, L);
+  face = 1;
+  double v = asph_dist_surface_f(P, Pf, 2, L);
+  if (v < best) {
+    best = v;
+    face = 2;
+  }
+  const float lim = best >= kBig ? 3e38f : (float)best;
+  if (asph_wall_maybe_f(Pf, false, L, lim)) {
+    v = asph_dist_wall_exact(P, false, L.p, L.d);
+    if (v < best) {
+      best = v;
+      face = 3;
+    }
+  }
+  if (asph_wall_maybe_f(Pf, true, L, best >= kBig ? 3e38f : (float)best)) {
+    v = asph_dist_wall_exact(P, true, L.p, L.d);
+    if (v < best) {
+      best = v;
+      face = 4;
+    }
+  }
+  return best;
+}
+
+// DistFromOutside (:383-412): the bounding-tube screen in FP32 (enlarged,
+// never rejecting a ray the exact TGeoTube test accepts), then the faces
+RBG_D double asph_dist_out_f(const double* P, const float* Pf, const LRay& L, int& face) {
+  // pad: 1e-4 cm, plus 1e-5 of the tube size and 1e-6 of the coordinates
+  // (the float position and origin carry ~6e-8 relative error each)
+  const float pad = 1e-4f + 1e-5f * (Pf[RBG_ASPH_RMAX] + Pf[RBG_ASPH_DZ]) +
+                    1e-6f * (fabsf(L.pf.x) + fabsf(L.pf.y) + fabsf(L.pf.z) + fabsf(Pf[RBG_ASPH_ORIGIN_Z]));
+  const float R = Pf[RBG_ASPH_RMAX] + pad, Z = Pf[RBG_ASPH_DZ] + pad;
+  const float ox = L.pf.x, oy = L.pf.y, oz = L.pf.z - Pf[RBG_ASPH_ORIGIN_Z];
+  const float dx = L.df.x, dy = L.df.y, dzz = L.df.z;
+  float t0 = 0.f, t1 = 3.0e38f;
+  if (dzz != 0.f) {
+    float ta = (-Z - oz) / dzz, tb = (Z - oz) / dzz;
+    t0 = fmaxf(t0, fminf(ta, tb));
+    t1 = fminf(t1, fmaxf(ta, tb));
+  } else if (fabsf(oz) > Z) {
+    return kBig;
+  }
+  if (t0 > t1) return kBig;
+  float A = dx * dx + dy * dy, B = ox * dx + oy * dy, C = ox * ox + oy * oy - R * R;
+  if (A == 0.f) {
+    if (C > 0.f) return kBig;
+  } else {
+    float disc = B * B - A * C;
+    if (disc < 0.f) return kBig;
+    float sq = sqrtf(disc);
+    float c0 = (-B - sq) / A, c1 = (-B + sq) / A;
+    const float lo = fmaxf(t0, c0), hi = fminf(t1, c1);
+    if (lo > hi + pad + 1e-5f * (fabsf(lo) + fabsf(hi))) return kBig;
+  }
+  return asph_dist4_f(P, Pf, L, face);
+}
+
+// Contains (:330-347) behind FP32 screens of the radius and of both sags
+// (faces with c == 0; the screen margin is 2e-5 of the sum of the sag's term
+// magnitudes plus the coordinates, >10x the FP32 rounding of the sums)
+RBG_D bool asph_contains_f(const double* P, const float* Pf, const LRay& L) {
+  const float h = L.pf.x * L.pf.x + L.pf.y * L.pf.y;
+  const float rmax = Pf[RBG_ASPH_RMAX], rmin = Pf[RBG_ASPH_RMIN];
+  const float hr = 4e-6f * h + 1e-12f;
+  if (h > rmax * rmax * (1.f + 4e-6f) + hr) return false;
+  if (h < rmin * rmin * (1.f - 4e-6f) - hr) return false;
+  const bool radial_in = h < rmax * rmax * (1.f - 4e-6f) - hr && h > rmin * rmin * (1.f + 4e-6f) + hr;
+  if (Pf[RBG_ASPH_C1] == 0.f && Pf[RBG_ASPH_C2] == 0.f) {
+    const int n1 = (int)Pf[RBG_ASPH_NPOL1], n2 = (int)Pf[RBG_ASPH_NPOL2];
+    float m1, m2;
+    const float f1 = Pf[RBG_ASPH_Z1] + asph_poly_f(Pf + RBG_ASPH_K, n1, h, m1);
+    const float f2 = Pf[RBG_ASPH_Z2] + asph_poly_f(Pf + RBG_ASPH_K + n1, n2, h, m2);
+    const float z = L.pf.z;
+    const float e1 = 2e-5f * (m1 + fabsf(Pf[RBG_ASPH_Z1]) + fabsf(z)) + 1e-7f;
+    const float e2 = 2e-5f * (m2 + fabsf(Pf[RBG_ASPH_Z2]) + fabsf(z)) + 1e-7f;
+    if (z < f1 - e1 || z > f2 + e2) return false;
+    if (radial_in && z > f1 + e1 && z < f2 - e2) return true;
+  }
+  return asph_contains_exact(P, L.p);
+}
+
+// TGeoBBox::Contains behind an FP32 screen
+RBG_D bool box_contains_f(const double* P, const float* Pf, const LRay& L) {
+  const float ax = fabsf(L.pf.x - Pf[RBG_BOX_OX]), ay = fabsf(L.pf.y - Pf[RBG_BOX_OY]),
+              az = fabsf(L.pf.z - Pf[RBG_BOX_OZ]);
+  const float ex = 1e-6f * (fabsf(L.pf.x) + fabsf(Pf[RBG_BOX_OX]) + Pf[RBG_BOX_DX]) + 1e-30f;
+  const float ey = 1e-6f * (fabsf(L.pf.y) + fabsf(Pf[RBG_BOX_OY]) + Pf[RBG_BOX_DY]) + 1e-30f;
+  const float ez = 1e-6f * (fabsf(L.pf.z) + fabsf(Pf[RBG_BOX_OZ]) + Pf[RBG_BOX_DZ]) + 1e-30f;
+  if (ax > Pf[RBG_BOX_DX] + ex || ay > Pf[RBG_BOX_DY] + ey || az > Pf[RBG_BOX_DZ] + ez) return false;
+  if (ax < Pf[RBG_BOX_DX] - ex && ay < Pf[RBG_BOX_DY] - ey && az < Pf[RBG_BOX_DZ] - ez) return true;
+  return prim_contains(RBG_SHAPE_BOX, P, L.p);
+}
+
+// Node-local normal of an aspheric disk at a point just past face `face`
+// (1 or 2) of a crossing.  ComputeNormal (:246-327) takes the surface with
+// the smallest safety distance: the crossed face is within the 1e-9 cm
+// push, so a wall can only win when the point lies that close to a rim.
+// When both faces share their polynomial with c == 0 (a thin shell), both
+// faces have the same gradient (-2x F', -2y F', 1), and a point clearly away
+// from both rims (FP32 radius test, 1e-4 cm + 1e-5 relative margin) takes
+// it directly; anything else runs the full FP64 choice.
+RBG_D d3 asph_normal_f(const DevScene& S, int node, const double* P, const float* Pf, const LRay& L, int face) {
+  if ((face == 1 || face == 2) && (S.aux[node].flags & RBG_AUX_ASPH_TWIN_FACES) && Pf[RBG_ASPH_C1] == 0.f) {
+    const float r = sqrtf(L.pf.x * L.pf.x + L.pf.y * L.pf.y);
+    const float rmax = Pf[RBG_ASPH_RMAX], rmin = Pf[RBG_ASPH_RMIN];
+    const float pad = 1e-4f + 1e-5f * rmax;
+    const bool rim = fabsf(r - rmax) < pad || (Pf[RBG_ASPH_RSEG] != 0.f && fabsf(r - rmin) < pad);
+    if (!rim) {
+      const int n1 = (int)Pf[RBG_ASPH_NPOL1];
+      const double H2 = L.p.x * L.p.x + L.p.y * L.p.y;
+      const double dF = asph_dpoly(P + RBG_ASPH_K, n1, H2);
+      d3 n;
+      if (dF == 0) {
+        n = mk(0, 0, 1);
+      } else {
+        const double gx = -2 * L.p.x * dF, gy = -2 * L.p.y * dF;
+        const double inv = rsqrt_refined(fma(gx, gx, fma(gy, gy, 1.0)));
+        n = mk(gx * inv, gy * inv, inv);
+      }
+      if (dot(n, L.d) < 0) n = neg(n);
+      return n;
+    }
+  }
+  return asph_normal_exact(P, L.p, L.d);
+}
 
 }  // namespace rbg

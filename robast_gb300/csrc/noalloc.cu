@@ -98,7 +98,8 @@ extern "C" int rbg_trace_noalloc(rbg_scene* s, const rbg_rays* in, rbg_result* o
   const size_t need = kHeader + table_bytes(s->nodes) + table_bytes(s->children) + table_bytes(s->bvh) +
                       table_bytes(s->bvh_items) + table_bytes(s->shapes) + table_bytes(s->volumes) +
                       table_bytes(s->tables) + table_bytes(s->indices) + table_bytes(s->layers) +
-                      table_bytes(s->multilayers) + table_bytes(s->borders) + table_bytes(s->params);
+                      table_bytes(s->multilayers) + table_bytes(s->borders) + table_bytes(s->params) +
+                      table_bytes(s->node_aux) + table_bytes(s->fparams);
   if (need > RBG_NOALLOC_SCRATCH_BYTES) return RBG_ERR_TOO_LARGE;
   unsigned char* base = nullptr;
   int rc = scratch_address(&base);
@@ -114,7 +115,8 @@ extern "C" int rbg_trace_noalloc(rbg_scene* s, const rbg_rays* in, rbg_result* o
       (rc = place(s->tables, base, &off, st, &v.tables)) || (rc = place(s->indices, base, &off, st, &v.indices)) ||
       (rc = place(s->layers, base, &off, st, &v.layers)) ||
       (rc = place(s->multilayers, base, &off, st, &v.multilayers)) ||
-      (rc = place(s->borders, base, &off, st, &v.borders)) || (rc = place(s->params, base, &off, st, &v.params)))
+      (rc = place(s->borders, base, &off, st, &v.borders)) || (rc = place(s->params, base, &off, st, &v.params)) ||
+      (rc = place(s->node_aux, base, &off, st, &v.aux)) || (rc = place(s->fparams, base, &off, st, &v.fparams)))
     return rc;
   v.n_nodes = (int32_t)s->nodes.size();
   v.n_borders = (int32_t)s->borders.size();

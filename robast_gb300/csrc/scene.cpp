@@ -598,11 +598,48 @@ struct Builder {
       if (b.multilayer >= 0) s->features |= rbg::kFeatMultilayer;
       if (b.sigma != 0 || b.lambertian) s->features |= rbg::kFeatRough;
     }
+    rbg::build_node_aux(s);
     return RBG_OK;
   }
 };
 
+// largest float <= v (smallest float >= v when up)
+float round_to_float(double v, bool up) {
+  float f = (float)v;
+  if (std::isnan(v)) return f;
+  if (up && (double)f < v) f = std::nextafter(f, std::numeric_limits<float>::infinity());
+  if (!up && (double)f > v) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
+  return f;
+}
+
 }  // namespace
+
+void rbg::build_node_aux(rbg_scene* s) {
+  s->fparams.resize(s->params.size());
+  for (size_t i = 0; i < s->params.size(); ++i) s->fparams[i] = (float)s->params[i];
+  s->node_aux.assign(s->nodes.size(), rbg_node_aux{});
+  for (size_t i = 0; i < s->nodes.size(); ++i) {
+    const rbg_node& n = s->nodes[i];
+    rbg_node_aux& a = s->node_aux[i];
+    for (int k = 0; k < 3; ++k) {
+      a.lo[k] = round_to_float(n.lo[k], false);
+      a.hi[k] = round_to_float(n.hi[k], true);
+    }
+    const bool rot_identity = n.m[0] == 1 && n.m[1] == 0 && n.m[2] == 0 && n.m[3] == 0 && n.m[4] == 1 &&
+                              n.m[5] == 0 && n.m[6] == 0 && n.m[7] == 0 && n.m[8] == 1;
+    const bool no_shift = n.m[9] == 0 && n.m[10] == 0 && n.m[11] == 0;
+    a.xform = !rot_identity ? RBG_XFORM_GENERAL : (no_shift ? RBG_XFORM_IDENTITY : RBG_XFORM_TRANSLATION);
+    a.flags = 0;
+    const rbg_shape_desc& sh = s->shapes[n.shape];
+    if (sh.type == RBG_SHAPE_ASPHERIC_DISK) {
+      const double* P = s->params.data() + sh.param_offset;
+      const int n1 = (int)P[RBG_ASPH_NPOL1], n2 = (int)P[RBG_ASPH_NPOL2];
+      bool twin = n1 == n2 && P[RBG_ASPH_C1] == P[RBG_ASPH_C2] && P[RBG_ASPH_KAPPA1] == P[RBG_ASPH_KAPPA2];
+      for (int j = 0; twin && j < n1; ++j) twin = P[RBG_ASPH_K + j] == P[RBG_ASPH_K + n1 + j];
+      if (twin) a.flags |= RBG_AUX_ASPH_TWIN_FACES;
+    }
+  }
+}
 
 extern "C" {
 

@@ -5,6 +5,7 @@
 
 #include "robast_gb.h"
 #include "robast_gb_layout.h"
+#include "node_aux.h"
 
 struct rbg_device_scene;  // defined in device_state.cuh
 
@@ -27,6 +28,9 @@ struct rbg_scene {
   std::vector<double> shape_box;
   // kFeat* bits (trace_features.h) the scene uses
   uint32_t features = 0;
+  // device-only tables of the mixed-precision tracer (node_aux.h)
+  std::vector<rbg_node_aux> node_aux;
+  std::vector<float> fparams;
 
   // device mirror, owned by the CUDA side (capi.cu)
   rbg_device_scene* dev = nullptr;

@@ -13,6 +13,7 @@ struct Nav {
   d3 p, d;    // navigator point and direction (master frame)
   int xnode;  // node whose surface the last step crossed
   d3 xn;      // its normal for TGeo primitives (node frame)
+  int xface;  // mixed path: face of an aspheric disk the step crossed
 };
 
 RBG_D bool in_box(const double* lo, const double* hi, d3 p) {
@@ -125,6 +126,97 @@ RBG_D int locate_from_top(const DevScene& S, d3 p) {
   return locate_down<MIXED, F>(S, 0, p);
 }
 
+// ---- mixed-precision navigation: the same tree walks with FP32 screens
+// in front of every containment test (geometry.cuh fast paths) ----------
+RBG_D bool in_fbox3(const float* lo, const float* hi, f3 p) {
+  return !(p.x < lo[0] || p.x > hi[0] || p.y < lo[1] || p.y > hi[1] || p.z < lo[2] || p.z > hi[2]);
+}
+
+template <unsigned F>
+RBG_D bool shape_contains_f(const DevScene& S, int shape, const LRay& L) {
+  const rbg_shape_desc& sh = S.shapes[shape];
+  const double* P = S.params + sh.param_offset;
+  const float* Pf = S.fparams + sh.param_offset;
+  if (sh.type == RBG_SHAPE_ASPHERIC_DISK) return asph_contains_f(P, Pf, L);
+  if (sh.type == RBG_SHAPE_BOX) return box_contains_f(P, Pf, L);
+  if (sh.type == RBG_SHAPE_WINSTON_POLY) return (F & kFeatWinston) ? win_contains(win_load(P), L.p) : false;
+  return (F & kFeatCSG) ? csg_contains(S, shape, L.p) : false;
+}
+
+// node k contains p: float box (rounded outward, so it never rejects a
+// point of the FP64 box) and the shape's own test in the local frame
+template <unsigned F>
+RBG_D bool node_contains_f(const DevScene& S, int k, d3 p, f3 pf) {
+  const rbg_node_aux& A = S.aux[k];
+  if (!in_fbox3(A.lo, A.hi, pf)) return false;
+  return shape_contains_f<F>(S, S.nodes[k].shape, local_point(S, k, p, pf));
+}
+
+template <unsigned F>
+RBG_D int first_child_containing_f(const DevScene& S, int k, d3 p, f3 pf) {
+  const rbg_node& N = S.nodes[k];
+  if (!(F & kFeatBVH) || N.bvh_root < 0) {
+    for (int i = 0; i < N.child_count; ++i) {
+      int c = S.children[N.child_begin + i];
+      if (node_contains_f<F>(S, c, p, pf)) return c;
+    }
+    return -1;
+  }
+  int best = -1;
+  int stack[32];
+  int sp = 0;
+  stack[sp++] = N.bvh_root;
+  while (sp > 0) {
+    const rbg_bvh_node& b = S.bvh[stack[--sp]];
+    if (!in_fbox3(b.lo, b.hi, pf)) continue;
+    if (b.left < 0) {
+      for (int i = 0; i < b.right; ++i) {
+        int c = S.bvh_items[b.item_begin + i];
+        if ((best < 0 || c < best) && node_contains_f<F>(S, c, p, pf)) best = c;
+      }
+    } else if (sp + 2 <= 32) {
+      stack[sp++] = b.left;
+      stack[sp++] = b.right;
+    }
+  }
+  return best;
+}
+
+template <unsigned F>
+RBG_D int locate_down_f(const DevScene& S, int k, d3 p, f3 pf) {
+  for (int depth = 0; depth < 64; ++depth) {
+    int c = first_child_containing_f<F>(S, k, p, pf);
+    if (c < 0) return k;
+    k = c;
+  }
+  return k;
+}
+template <unsigned F>
+RBG_D int locate_from_top_f(const DevScene& S, d3 p) {
+  const f3 pf = to_f3(p);
+  if (!node_contains_f<F>(S, 0, p, pf)) return -1;
+  return locate_down_f<F>(S, 0, p, pf);
+}
+
+// shape distance in the mixed path; `face` receives the aspheric face
+template <unsigned F>
+RBG_D double shape_dist_f(const DevScene& S, int shape, const LRay& L, bool exit, d3& nrm, int& face, unsigned& err) {
+  const rbg_shape_desc& sh = S.shapes[shape];
+  const double* P = S.params + sh.param_offset;
+  face = 0;
+  if (sh.type == RBG_SHAPE_ASPHERIC_DISK) {
+    const float* Pf = S.fparams + sh.param_offset;
+    return exit ? asph_dist4_f(P, Pf, L, face) : asph_dist_out_f(P, Pf, L, face);
+  }
+  if (sh.type == RBG_SHAPE_WINSTON_POLY) {
+    if (!(F & kFeatWinston)) return kBig;
+    Win w = win_load(P);
+    return exit ? win_dist_in(w, L.p, L.d) : win_dist_out(w, L.p, L.d);
+  }
+  if (sh.type == RBG_SHAPE_BOX) return box_dist_fast(P, L.p, L.d, exit, nrm);
+  return (F & kFeatCSG) ? csg_dist(S, shape, L.p, L.d, exit, nrm, err) : kBig;
+}
+
 // candidate daughter test shared by the scan and the BVH walk
 template <bool MIXED, unsigned F = kFeatAll>
 RBG_D void try_child(const DevScene& S, int k, d3 p, d3 d, double& best, int& xnode, bool& enter, d3& nbest,
@@ -228,6 +320,89 @@ RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, 
   return next;
 }
 
+// TGeoNavigator::FindNextBoundaryAndStep for the mixed path: the same
+// candidates, tie rules and relocation as find_next_boundary_and_step, with
+// the ray converted to FP32 once for every screen, the daughters culled
+// against their float boxes, and the crossed aspheric face recorded for
+// find_normal
+template <unsigned F>
+RBG_D int find_next_boundary_and_step_f(const DevScene& S, Nav& nv, double& step, unsigned& err) {
+  const int c = nv.node;
+  const f3 pf = to_f3(nv.p), df = to_f3(nv.d);
+  double best;
+  d3 nbest = mk(0, 0, 1);
+  int xnode, face = 0, xface = 0;
+  bool enter;
+  if (c < 0) {
+    best = shape_dist_f<F>(S, S.nodes[0].shape, local_ray(S, 0, nv.p, nv.d, pf, df), false, nbest, xface, err);
+    if (best >= kBig) {
+      step = 0;
+      nv.xnode = -1;
+      return -1;
+    }
+    xnode = 0;
+    enter = true;
+  } else {
+    const rbg_node& N = S.nodes[c];
+    best = shape_dist_f<F>(S, N.shape, local_ray(S, c, nv.p, nv.d, pf, df), true, nbest, xface, err);
+    xnode = c;
+    enter = false;
+    const bool zx = df.x == 0.f, zy = df.y == 0.f, zz = df.z == 0.f;
+    const float ix = zx ? 0.f : 1.0f / df.x, iy = zy ? 0.f : 1.0f / df.y, iz = zz ? 0.f : 1.0f / df.z;
+    auto visit = [&](int k) {
+      const rbg_node_aux& A = S.aux[k];
+      if (!seg_box_f32(pf.x, pf.y, pf.z, ix, iy, iz, zx, zy, zz, best >= kBig ? 3e38f : (float)best, A.lo, A.hi))
+        return;
+      d3 nrm = mk(0, 0, 1);
+      double s = shape_dist_f<F>(S, S.nodes[k].shape, local_ray(S, k, nv.p, nv.d, pf, df), false, nrm, face, err);
+      // ties: leaving the mother first, then the lowest node id (placement order)
+      if (s < best || (s == best && enter && k < xnode)) {
+        best = s;
+        xnode = k;
+        enter = true;
+        nbest = nrm;
+        xface = face;
+      }
+    };
+    if (!(F & kFeatBVH) || N.bvh_root < 0) {
+      for (int i = 0; i < N.child_count; ++i) visit(S.children[N.child_begin + i]);
+    } else {
+      int stack[32];
+      int sp = 0;
+      stack[sp++] = N.bvh_root;
+      while (sp > 0) {
+        const rbg_bvh_node& b = S.bvh[stack[--sp]];
+        if (!seg_box_f32(pf.x, pf.y, pf.z, ix, iy, iz, zx, zy, zz, best >= kBig ? 3e38f : (float)best, b.lo, b.hi))
+          continue;
+        if (b.left < 0) {
+          for (int i = 0; i < b.right; ++i) visit(S.bvh_items[b.item_begin + i]);
+        } else if (sp + 2 <= 32) {
+          stack[sp++] = b.right;
+          stack[sp++] = b.left;
+        } else {
+          err |= ERR_BIT_CAP;
+        }
+      }
+    }
+  }
+  nv.p = nv.p + (best + RBG_BOUNDARY_PUSH) * nv.d;
+  nv.xnode = xnode;
+  nv.xn = nbest;
+  nv.xface = xface;
+  const f3 qf = to_f3(nv.p);
+  int next;
+  if (enter) {
+    next = locate_down_f<F>(S, xnode, nv.p, qf);
+  } else {
+    int q = S.nodes[c].parent;
+    while (q >= 0 && !node_contains_f<F>(S, q, nv.p, qf)) q = S.nodes[q].parent;
+    next = q < 0 ? -1 : locate_down_f<F>(S, q, nv.p, qf);
+  }
+  nv.node = next;
+  step = best;
+  return next;
+}
+
 // TGeoNavigator::FindNormal: master-frame normal, n . d >= 0
 template <bool MIXED = false, unsigned F = kFeatAll>
 RBG_D d3 find_normal(const DevScene& S, const Nav& nv) {
@@ -235,10 +410,19 @@ RBG_D d3 find_normal(const DevScene& S, const Nav& nv) {
   const rbg_node& N = S.nodes[nv.xnode];
   const int type = S.shapes[N.shape].type;
   d3 nl;
-  if (type == RBG_SHAPE_ASPHERIC_DISK) {
+  if (MIXED && type == RBG_SHAPE_ASPHERIC_DISK) {
+    const int off = S.shapes[N.shape].param_offset;
+    const LRay L = local_ray(S, nv.xnode, nv.p, nv.d, to_f3(nv.p), to_f3(nv.d));
+    nl = asph_normal_f(S, nv.xnode, S.params + off, S.fparams + off, L, nv.xface);
+    const int xf = S.aux[nv.xnode].xform;
+    // a rotation keeps the unit length (to rounding); no renormalisation
+    d3 n = xf == RBG_XFORM_GENERAL ? dir_to_master(N.m, nl) : nl;
+    if (dot(n, nv.d) < 0) n = neg(n);
+    return n;
+  } else if (type == RBG_SHAPE_ASPHERIC_DISK) {
     Asph a{SP(S, N.shape)};
     d3 pl = to_local(N.m, nv.p), dl = dir_to_local(N.m, nv.d);
-    nl = MIXED ? asph_normal_fast(a, pl, dl) : asph_normal(a, pl, dl);
+    nl = asph_normal(a, pl, dl);
   } else if (type == RBG_SHAPE_WINSTON_POLY) {
     nl = win_normal(win_load(SP(S, N.shape)), to_local(N.m, nv.p), dir_to_local(N.m, nv.d));
   } else {
@@ -604,7 +788,7 @@ RBG_D void do_reflection(const DevScene& S, Nav& nv, Ray& r, double n1, double s
   }
   double t = MIXED ? r.t + step * (n1 * (1.0 / RBG_SPEED_OF_LIGHT_CM)) : r.t + step / (RBG_SPEED_OF_LIGHT_CM / n1);
   nv.p = nv.p - RBG_REFLECT_BACKSTEP * d1;
-  nv.node = locate_from_top<MIXED, F>(S, nv.p);
+  nv.node = MIXED ? locate_from_top_f<F>(S, nv.p) : locate_from_top<MIXED, F>(S, nv.p);
   nv.d = d2;
   add_point(r, nv.p, t);
   add_node(r, next);
@@ -693,9 +877,10 @@ template <bool MIXED = false, unsigned F = kFeatAll>
 RBG_D void trace_begin(const DevScene& S, Ray& r, Nav& nv) {
   nv.p = r.x;
   nv.d = r.d;
-  nv.node = locate_from_top<MIXED, F>(S, nv.p);
+  nv.node = MIXED ? locate_from_top_f<F>(S, nv.p) : locate_from_top<MIXED, F>(S, nv.p);
   nv.xnode = -1;
   nv.xn = mk(0, 0, 1);
+  nv.xface = 0;
 }
 
 template <bool MIXED, unsigned F = kFeatAll>
@@ -706,7 +891,8 @@ RBG_D void trace_step(const DevScene& S, Ray& r, Nav& nv, int limit, bool disabl
   const d3 d1 = r.d;
   const int cur = nv.node;
   double step;
-  const int next = find_next_boundary_and_step<MIXED, F>(S, nv, step, r.err);
+  const int next = MIXED ? find_next_boundary_and_step_f<F>(S, nv, step, r.err)
+                         : find_next_boundary_and_step<MIXED, F>(S, nv, step, r.err);
   const int tc = kind_of(S, cur), tn = kind_of(S, next);
 
   if ((F & kFeatLens) && tc == kLens) {
