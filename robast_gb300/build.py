@@ -24,7 +24,7 @@ ORACLE = os.path.join(ROOT, "oracle")
 ORACLE_BUILD = os.path.join(ORACLE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["capi.cu", "trace_mixed.cu", "adjoint.cu", "noalloc.cu"]
+CU_SOURCES = ["trace_fp64.cu", "trace_mixed_all.cu", "capi.cu", "trace_mixed.cu", "adjoint.cu", "noalloc.cu"]
 CPP_SOURCES = ["scene.cpp", "shoot.cpp"]
 
 

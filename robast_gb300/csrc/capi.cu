@@ -1,5 +1,5 @@
-// capi.cu -- C ABI of the tracer: device upload of a flattened scene, the
-// plain FP64 trace kernel, host-buffer tracing and focal-plane reductions.
+// capi.cu -- C ABI of the tracer: device upload of a flattened scene,
+// device- and host-buffer tracing and focal-plane reductions.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -41,6 +41,8 @@ void release_device(rbg_scene* s) {
   int prev = -1;
   cudaGetDevice(&prev);
   if (s->dev_id >= 0) cudaSetDevice(s->dev_id);
+  for (cudaStream_t& st : s->dev->host_streams)
+    if (st) cudaStreamDestroy(st);
   for (void* p : s->dev->allocations) cudaFree(p);
   if (s->workspace) cudaFree(s->workspace);
   if (prev >= 0) cudaSetDevice(prev);
@@ -98,20 +100,6 @@ int ensure_device(rbg_scene* s) {
   return RBG_OK;
 }
 
-// ---------------------------------------------------------------------
-// plain FP64 kernel: one thread per ray, whole path in registers
-// ---------------------------------------------------------------------
-__global__ void __launch_bounds__(128) trace_fp64_kernel(DevScene S, KernelRays in, KernelOut out, int64_t n,
-                                                         int limit, int disable_fresnel, uint64_t seed,
-                                                         uint64_t id_offset, unsigned* err_flags) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    Ray r;
-    if (load_ray(in, out, i, seed, id_offset, r)) trace_ray<false>(S, r, limit, disable_fresnel != 0);
-    if (r.err) atomicOr(err_flags, r.err);
-    store_ray(out, i, r);
-  }
-}
-
 int sm_count() {
   static int cached = 0;
   if (cached == 0) {
@@ -152,10 +140,12 @@ extern "C" int rbg_scene_upload(rbg_scene* s) {
 
 extern "C" int rbg_last_launch_count(const rbg_scene* s) { return s ? s->last_launches : -1; }
 
-// forward declaration of the mixed-precision entry (trace_mixed.cu)
+// the two tracer launchers (trace_mixed.cu, trace_fp64.cu)
 namespace rbg {
 int launch_mixed(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o,
                  cudaStream_t st, unsigned* err_flags, unsigned long long* counter, int* launches);
+int launch_fp64(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o,
+                cudaStream_t st, unsigned* err_flags, int* launches);
 }
 
 extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, const rbg_trace_opts* opts,
@@ -180,15 +170,10 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
     if (rc) return rc;
     s->last_launches = launches;
   } else {
-    int block = opts->block_size > 0 ? opts->block_size : 128;
-    if (block > 128) block = 128;
-    int64_t blocks64 = (in->n + block - 1) / block;
-    int64_t cap = (int64_t)sm_count() * 64;
-    int blocks = (int)(blocks64 < cap ? blocks64 : cap);
-    trace_fp64_kernel<<<blocks, block, 0, st>>>(s->dev->view, kr, ko, in->n, opts->limit, opts->disable_fresnel,
-                                                opts->seed, opts->ray_id_offset, s->dev->err_flags);
-    if (cudaGetLastError() != cudaSuccess) return RBG_ERR_CUDA;
-    s->last_launches = 1;
+    int launches = 0;
+    rc = launch_fp64(s->dev->view, kr, ko, in->n, *opts, st, s->dev->err_flags, &launches);
+    if (rc) return rc;
+    s->last_launches = launches;
   }
   unsigned bits = 0;
   if ((rc = read_errors(s, st, &bits))) return rc;
@@ -197,77 +182,161 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
   return RBG_OK;
 }
 
+namespace rbg {
 namespace {
-struct DevBuf {
-  void* p = nullptr;
-  ~DevBuf() {
-    if (p) cudaFree(p);
-  }
-};
-}  // namespace
 
+constexpr int kHostStreams = 2;
+constexpr int64_t kHostChunk = int64_t(1) << 21;  // rays per pipeline stage
+
+int launch_trace(rbg_scene* s, const KernelRays& kr, const KernelOut& ko, int64_t n, const rbg_trace_opts& o,
+                 cudaStream_t st, unsigned* err, unsigned long long* counter, int* launches) {
+  if (o.precision == RBG_PREC_MIXED) return launch_mixed(s->dev->view, kr, ko, n, o, st, err, counter, launches);
+  return launch_fp64(s->dev->view, kr, ko, n, o, st, err, launches);
+}
+
+// the scene's device workspace, grown to at least `bytes`; it is kept
+// between calls (freed with the scene), so repeated calls allocate nothing
+int grow_workspace(rbg_scene* s, size_t bytes, char** out) {
+  if (s->workspace_bytes < bytes) {
+    if (s->workspace) cudaFree(s->workspace);
+    s->workspace = nullptr;
+    s->workspace_bytes = 0;
+    if (cudaMalloc(&s->workspace, bytes) != cudaSuccess) {
+      s->workspace = nullptr;
+      return RBG_ERR_NOMEM;
+    }
+    s->workspace_bytes = bytes;
+  }
+  *out = static_cast<char*>(s->workspace);
+  return RBG_OK;
+}
+
+// One pipeline slot: its own queue head and error word (a 256-byte
+// header), the chunk's 8 input and 7 output arrays, fates, point counts,
+// last nodes and optional histories, for up to `cap` rays.
+struct Slot {
+  unsigned* err;
+  unsigned long long* counter;
+  double* in[8];
+  double* out[7];
+  int32_t* npoints;
+  int32_t* last_node;
+  uint8_t* status;
+  double* hist;
+  int32_t* hist_node;
+};
+
+size_t slot_bytes(int64_t cap, int hist_cap) {
+  return 256 + (size_t)cap * (15 * 8 + 2 * 4 + 8) + (size_t)cap * hist_cap * (4 * 8 + 4);
+}
+
+Slot slot_at(char* base, int64_t cap, int hist_cap) {
+  Slot sl;
+  sl.err = reinterpret_cast<unsigned*>(base);
+  sl.counter = reinterpret_cast<unsigned long long*>(base + 8);
+  char* p = base + 256;
+  for (int k = 0; k < 8; ++k, p += cap * 8) sl.in[k] = reinterpret_cast<double*>(p);
+  for (int k = 0; k < 7; ++k, p += cap * 8) sl.out[k] = reinterpret_cast<double*>(p);
+  sl.npoints = reinterpret_cast<int32_t*>(p);
+  p += cap * 4;
+  sl.last_node = reinterpret_cast<int32_t*>(p);
+  p += cap * 4;
+  sl.status = reinterpret_cast<uint8_t*>(p);
+  p += cap * 8;
+  sl.hist = hist_cap ? reinterpret_cast<double*>(p) : nullptr;
+  p += (size_t)cap * hist_cap * 32;
+  sl.hist_node = hist_cap ? reinterpret_cast<int32_t*>(p) : nullptr;
+  return sl;
+}
+
+}  // namespace
+}  // namespace rbg
+
+// The call a host-side AOpticsManager::TraceNonSequential makes: host
+// arrays in and out.  The batch runs as a pipeline of chunks of 2^21 rays
+// over two streams, so that the copies of one chunk overlap the tracing of
+// the other; each chunk has its own queue head and error word, and its ray
+// ids continue the batch's (opts->ray_id_offset + index), so the Philox
+// draws -- and the results -- are those of one rbg_trace over the batch.
+// Device memory is the scene's workspace, reused across calls.  Host arrays
+// in page-locked memory overlap best; pageable ones work, staged by CUDA.
 extern "C" int rbg_trace_host(rbg_scene* s, const rbg_rays* in, rbg_result* out, const rbg_trace_opts* opts) {
-  if (!s || !in || !out || !opts || in->n < 0) return RBG_ERR_ARG;
+  if (!s || !in || !out || !opts || in->n < 0 || opts->limit <= 0) return RBG_ERR_ARG;
   if (in->n > 0 && (!in->x || !in->y || !in->z || !in->dx || !in->dy || !in->dz || !in->lambda)) return RBG_ERR_ARG;
+  if (out->hist_cap < 0 || (out->hist_cap > 0 && (!out->hist_xyzt || !out->hist_node))) return RBG_ERR_ARG;
   int rc = ensure_device(s);
   if (rc) return rc;
+  if ((rc = stack_ready())) return rc;
   const int64_t n = in->n;
+  s->last_launches = 0;
   if (n == 0) return RBG_OK;
-  // one device block holding every input and output array
-  const size_t d8 = (size_t)n * sizeof(double);
-  const size_t hist = out->hist_cap > 0 ? (size_t)n * out->hist_cap : 0;
-  size_t bytes = 8 * d8 + 7 * d8 + (size_t)n * (sizeof(int32_t) * 2 + 8) + hist * (4 * sizeof(double) + sizeof(int32_t));
-  DevBuf buf;
-  if (cudaMalloc(&buf.p, bytes) != cudaSuccess) return RBG_ERR_NOMEM;
-  char* base = static_cast<char*>(buf.p);
-  double* din[8];
-  for (int k = 0; k < 8; ++k) din[k] = reinterpret_cast<double*>(base + k * d8);
-  double* dout[7];
-  for (int k = 0; k < 7; ++k) dout[k] = reinterpret_cast<double*>(base + (8 + k) * d8);
-  char* tail = base + 15 * d8;
-  int32_t* dnp = reinterpret_cast<int32_t*>(tail);
-  int32_t* dln = dnp + n;
-  uint8_t* dst = reinterpret_cast<uint8_t*>(dln + n);
-  char* htail = reinterpret_cast<char*>(dst) + ((n + 7) / 8) * 8;
-  double* dhist = hist ? reinterpret_cast<double*>(htail) : nullptr;
-  int32_t* dhnode = hist ? reinterpret_cast<int32_t*>(htail + hist * 4 * sizeof(double)) : nullptr;
+  const int hcap = out->hist_cap;
+  const int64_t cap = ((n < kHostChunk ? n : kHostChunk) + 255) / 256 * 256;
+  const int64_t chunks = (n + cap - 1) / cap;
+  const int nslots = chunks < kHostStreams ? (int)chunks : kHostStreams;
+  const size_t sb = slot_bytes(cap, hcap);
+  char* ws = nullptr;
+  if ((rc = grow_workspace(s, sb * nslots, &ws))) return rc;
+  Slot slots[kHostStreams];
+  for (int k = 0; k < nslots; ++k) {
+    cudaStream_t& st = s->dev->host_streams[k];
+    if (!st && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return RBG_ERR_CUDA;
+    slots[k] = slot_at(ws + sb * k, cap, hcap);
+    if (cudaMemsetAsync(slots[k].err, 0, 16, st) != cudaSuccess) return RBG_ERR_CUDA;
+  }
   const double* src[8] = {in->x, in->y, in->z, in->t, in->dx, in->dy, in->dz, in->lambda};
-  cudaStream_t st = 0;
-  for (int k = 0; k < 8; ++k) {
-    if (!src[k]) continue;
-    if (cudaMemcpyAsync(din[k], src[k], d8, cudaMemcpyHostToDevice, st) != cudaSuccess) return RBG_ERR_CUDA;
+  double* dst[7] = {out->x, out->y, out->z, out->t, out->dx, out->dy, out->dz};
+  int launches = 0;
+  for (int64_t c = 0; c < chunks; ++c) {
+    const int k = (int)(c % nslots);
+    cudaStream_t st = s->dev->host_streams[k];
+    const Slot& sl = slots[k];
+    const int64_t off = c * cap, m = n - off < cap ? n - off : cap;
+    for (int a = 0; a < 8; ++a)
+      if (src[a] && cudaMemcpyAsync(sl.in[a], src[a] + off, m * 8, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return RBG_ERR_CUDA;
+    KernelRays kr{sl.in[0], sl.in[1], sl.in[2], in->t ? sl.in[3] : nullptr, sl.in[4], sl.in[5], sl.in[6], sl.in[7]};
+    KernelOut ko{out->status ? sl.status : nullptr, out->npoints ? sl.npoints : nullptr,
+                 out->last_node ? sl.last_node : nullptr, dst[0] ? sl.out[0] : nullptr, dst[1] ? sl.out[1] : nullptr,
+                 dst[2] ? sl.out[2] : nullptr, dst[3] ? sl.out[3] : nullptr, dst[4] ? sl.out[4] : nullptr,
+                 dst[5] ? sl.out[5] : nullptr, dst[6] ? sl.out[6] : nullptr, hcap, sl.hist, sl.hist_node};
+    rbg_trace_opts o = *opts;
+    o.ray_id_offset = opts->ray_id_offset + (uint64_t)off;
+    int nl = 0;
+    if ((rc = launch_trace(s, kr, ko, m, o, st, sl.err, sl.counter, &nl))) return rc;
+    launches += nl;
+    if (out->status && cudaMemcpyAsync(out->status + off, sl.status, m, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return RBG_ERR_CUDA;
+    if (out->npoints &&
+        cudaMemcpyAsync(out->npoints + off, sl.npoints, m * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return RBG_ERR_CUDA;
+    if (out->last_node &&
+        cudaMemcpyAsync(out->last_node + off, sl.last_node, m * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return RBG_ERR_CUDA;
+    for (int a = 0; a < 7; ++a)
+      if (dst[a] && cudaMemcpyAsync(dst[a] + off, sl.out[a], m * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return RBG_ERR_CUDA;
+    if (hcap) {
+      if (cudaMemcpyAsync(out->hist_xyzt + off * hcap * 4, sl.hist, (size_t)m * hcap * 32, cudaMemcpyDeviceToHost,
+                          st) != cudaSuccess ||
+          cudaMemcpyAsync(out->hist_node + off * hcap, sl.hist_node, (size_t)m * hcap * 4, cudaMemcpyDeviceToHost,
+                          st) != cudaSuccess)
+        return RBG_ERR_CUDA;
+    }
   }
-  rbg_rays dr{n, din[0], din[1], din[2], in->t ? din[3] : nullptr, din[4], din[5], din[6], din[7]};
-  rbg_result dres{};
-  dres.status = out->status ? dst : nullptr;
-  dres.npoints = out->npoints ? dnp : nullptr;
-  dres.last_node = out->last_node ? dln : nullptr;
-  double* hout[7] = {out->x, out->y, out->z, out->t, out->dx, out->dy, out->dz};
-  double** dslots[7] = {&dres.x, &dres.y, &dres.z, &dres.t, &dres.dx, &dres.dy, &dres.dz};
-  for (int k = 0; k < 7; ++k) *dslots[k] = hout[k] ? dout[k] : nullptr;
-  dres.hist_cap = hist ? out->hist_cap : 0;
-  dres.hist_xyzt = dhist;
-  dres.hist_node = dhnode;
-  int trc = rbg_trace(s, &dr, &dres, opts, st);
-  if (trc != RBG_OK && trc != RBG_ERR_NAN && trc != RBG_ERR_CAP) return trc;
-  if (out->status && cudaMemcpyAsync(out->status, dst, n, cudaMemcpyDeviceToHost, st) != cudaSuccess)
-    return RBG_ERR_CUDA;
-  if (out->npoints && cudaMemcpyAsync(out->npoints, dnp, n * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
-    return RBG_ERR_CUDA;
-  if (out->last_node && cudaMemcpyAsync(out->last_node, dln, n * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
-    return RBG_ERR_CUDA;
-  for (int k = 0; k < 7; ++k)
-    if (hout[k] && cudaMemcpyAsync(hout[k], dout[k], d8, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+  unsigned bits = 0;
+  for (int k = 0; k < nslots; ++k) {
+    unsigned b = 0;
+    cudaStream_t st = s->dev->host_streams[k];
+    if (cudaMemcpyAsync(&b, slots[k].err, sizeof(b), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
       return RBG_ERR_CUDA;
-  if (hist) {
-    if (cudaMemcpyAsync(out->hist_xyzt, dhist, hist * 4 * sizeof(double), cudaMemcpyDeviceToHost, st) !=
-        cudaSuccess)
-      return RBG_ERR_CUDA;
-    if (cudaMemcpyAsync(out->hist_node, dhnode, hist * sizeof(int32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess)
-      return RBG_ERR_CUDA;
+    bits |= b;
   }
-  if (cudaStreamSynchronize(st) != cudaSuccess) return RBG_ERR_CUDA;
-  return trc;
+  s->last_launches = launches;
+  if (bits & ERR_BIT_NAN) return RBG_ERR_NAN;
+  if (bits & ERR_BIT_CAP) return RBG_ERR_CAP;
+  return RBG_OK;
 }
 
 // ---------------------------------------------------------------------

@@ -9,6 +9,7 @@ struct rbg_device_scene {
   std::vector<void*> allocations;
   unsigned* err_flags;          // device word of error bits
   unsigned long long* counter;  // ray queue head of the persistent kernel
+  cudaStream_t host_streams[2] = {nullptr, nullptr};  // rbg_trace_host pipeline
 };
 
 namespace rbg {

@@ -571,101 +571,6 @@ RBG_D double asph_dist_wall(const Asph& a, bool outer, d3 point, d3 dir) {
   return kBig;
 }
 
-// Mixed precision DistToAsphere: the same iteration (spherical start, Newton
-// along the ray with the reference's update formula) run in FP32 in
-// coordinates relative to the surface vertex, then polished in FP64 with
-// the FP32 slope: each polish step evaluates only the sag residual
-// x(H2) - z in FP64 (Horner in H2), so it converges by ~7 digits per step.
-// The stopping rule and the final checks are the reference's (|e| < 1e-10,
-// forward, rmin <= r <= rmax).  Any FP32 breakdown falls back to the FP64
-// routine.
-RBG_D double asph_dist_surface_mixed(const Asph& a, int n, d3 point, d3 dir) {
-  const double d = a.z(n);
-  const float curve = (float)a.c(n), kappa = (float)a.kap(n);
-  const int npol = a.npol(n);
-  const double* K = a.K(n);
-  const float px = (float)point.x, py = (float)point.y, pz = (float)(point.z - d);
-  const float dx = (float)dir.x, dy = (float)dir.y, dz = (float)dir.z;
-  float H2 = px * px + py * py;
-  float p = -(pz * dz + px * dx + py * dy);
-  float M = p * dz + pz;
-  float M2 = pz * pz + H2 - p * p;
-  float check = 1.f - (M2 * curve - 2.f * M) * curve / dz / dz;
-  if (check < 0) return asph_dist_surface(a, n, point, dir);
-  float q = p + (M2 * curve - 2.f * M) / (dz * (1.f + sqrtf(check)));
-  float nx = px + q * dx, ny = py + q * dy, nz = pz + q * dz;
-  float Kf[RBG_ASPH_MAXPOL];
-  for (int j = 0; j < npol; ++j) Kf[j] = (float)K[j];
-  float l = 1.f, scale = 1.f;
-  bool ok = false;
-  for (int i = 0; i < 40; i++) {
-    H2 = nx * nx + ny * ny;
-    check = 1.f - kappa * H2 * curve * curve;
-    if (check < 0) break;
-    l = sqrtf(check);
-    float x = 0.f, v = 0.f;
-    for (int j = npol - 1; j >= 0; --j) {
-      x = (x + Kf[j]) * H2;
-      v = v * H2 + 2.f * (j + 1) * Kf[j];
-    }
-    if (curve != 0.f) x += (1.f - l) / curve / kappa;
-    v = curve * kappa + l * v;
-    float m = -nx * v, nn = -ny * v;
-    float norm = sqrtf(l * l + m * m + nn * nn);
-    l /= norm;
-    m /= norm;
-    nn /= norm;
-    check = dz * l + dx * m + dy * nn;
-    if (check == 0.f) break;
-    scale = l / check;  // dt per unit sag residual
-    float e = scale * (x - nz);
-    nx += e * dx;
-    ny += e * dy;
-    nz += e * dz;
-    if (fabsf(e) < 4e-6f * (1.f + fabsf(nz) + sqrtf(H2))) {
-      ok = true;
-      break;
-    }
-  }
-  if (!ok) return asph_dist_surface(a, n, point, dir);
-  // FP64 polish on t, the distance along the ray from `point`; the FP32
-  // estimate of t uses the largest direction cosine
-  double t;
-  {
-    double ax = fabs(dir.x), ay = fabs(dir.y), az = fabs(dir.z);
-    if (az >= ax && az >= ay) t = ((double)nz - (point.z - d)) / dir.z;
-    else if (ax >= ay) t = ((double)nx - point.x) / dir.x;
-    else t = ((double)ny - point.y) / dir.y;
-  }
-  const double kap64 = a.kap(n), c64 = a.c(n);
-  const double sc = (double)scale;
-  d3 np;
-  bool conv = false;
-  for (int it = 0; it < 8; ++it) {
-    np = mk(point.x + t * dir.x, point.y + t * dir.y, point.z - d + t * dir.z);
-    double h2 = np.x * np.x + np.y * np.y;
-    double chk = 1 - kap64 * h2 * c64 * c64;
-    if (chk < 0) return asph_dist_surface(a, n, point, dir);
-    double x = 0;
-    for (int j = npol - 1; j >= 0; --j) x = (x + K[j]) * h2;
-    if (c64 != 0) x += (1 - sqrt(chk)) / c64 / kap64;
-    double e = sc * (x - np.z);
-    t += e;
-    if (fabs(e) < 1e-10) {
-      conv = true;
-      np = mk(point.x + t * dir.x, point.y + t * dir.y, point.z - d + t * dir.z);
-      break;
-    }
-  }
-  if (!conv) return asph_dist_surface(a, n, point, dir);
-  np.z += d;
-  d3 dv = np - point;
-  if (dot(dir, dv) < 0) return kBig;
-  double rz = sqrt(np.x * np.x + np.y * np.y);
-  if (rz < a.rmin() || rz > a.rmax()) return kBig;
-  return sqrt(dot(dv, dv));
-}
-
 // Sag F(H2) and dF/dH2 of face s in FP64 without the conic square roots
 // when the curvature is zero (the SC and light-guide surfaces); the values
 // equal CalcF1/CalcF2 to rounding.
@@ -734,55 +639,10 @@ RBG_D d3 asph_normal_fast(const Asph& a, d3 point, d3 dir) {
   return n;
 }
 
-// FP32 screen of DistToInner/DistToOuter: could the wall be hit at a
-// distance <= limit?  Conservative (enlarged z window and radius).
-RBG_D bool asph_wall_maybe(const Asph& a, bool outer, d3 point, d3 dir, double limit) {
-  if (!outer && !a.rseg()) return false;
-  const float R = (float)(outer ? a.rmax() : a.rmin());
-  const float px = (float)point.x, py = (float)point.y, pz = (float)point.z;
-  const float dx = (float)dir.x, dy = (float)dir.y, dz = (float)dir.z;
-  float nsq = dx * dx + dy * dy;
-  if (nsq < 1e-20f) return false;
-  float rsq = px * px + py * py, rdotn = px * dx + py * dy;
-  float b = rdotn / nsq, delta = b * b - (rsq - R * R) / nsq;
-  const float pad = 1e-3f + 1e-5f * (R + fabsf(px) + fabsf(py) + fabsf(pz));
-  if (delta < -pad) return false;
-  float sq = sqrtf(fmaxf(delta, 0.f));
-  float t1 = -b + sq, t2 = -b - sq;
-  if (t1 < -pad && t2 < -pad) return false;
-  double zlo = a.P[outer ? RBG_ASPH_F1RMAX : RBG_ASPH_F1RMIN], zhi = a.P[outer ? RBG_ASPH_F2RMAX : RBG_ASPH_F2RMIN];
-  if (isnan(zlo) || isnan(zhi)) return false;
-  float lim = (float)limit + pad;
-  for (int k = 0; k < 2; ++k) {
-    float t = k == 0 ? t1 : t2;
-    if (t < -pad || t > lim) continue;
-    float z = pz + t * dz;
-    if (z >= (float)zlo - pad && z <= (float)zhi + pad) return true;
-  }
-  return false;
-}
-
-template <bool MIXED, unsigned F = kFeatAll>
-RBG_D double asph_surface(const Asph& a, int n, d3 p, d3 d) {
-  return MIXED ? asph_dist_surface_mixed(a, n, p, d) : asph_dist_surface(a, n, p, d);
-}
-
-template <bool MIXED = false, unsigned F = kFeatAll>
+// DistFromInside (:363-380): nearest of the two faces and the two walls
 RBG_D double asph_dist4(const Asph& a, d3 p, d3 d) {
-  double best = asph_surface<MIXED>(a, 1, p, d);
-  double v = asph_surface<MIXED>(a, 2, p, d);
-  if (MIXED) {
-    if (v < best) best = v;
-    if (asph_wall_maybe(a, false, p, d, best)) {
-      v = asph_dist_wall(a, false, p, d);
-      if (v < best) best = v;
-    }
-    if (asph_wall_maybe(a, true, p, d, best)) {
-      v = asph_dist_wall(a, true, p, d);
-      if (v < best) best = v;
-    }
-    return best;
-  }
+  double best = asph_dist_surface(a, 1, p, d);
+  double v = asph_dist_surface(a, 2, p, d);
   if (v < best) best = v;
   v = asph_dist_wall(a, false, p, d);
   if (v < best) best = v;
@@ -817,41 +677,11 @@ RBG_D bool tube_reached(d3 o, d3 d, double rmin, double rmax, double dz) {
   return false;
 }
 
-// FP32 screen of the bounding tube, enlarged so that it never rejects a ray
-// the exact test accepts: slab in z, then the outer cylinder
-RBG_D bool tube_reached_f32(d3 o, d3 d, double rmin, double rmax, double dz) {
-  const float pad = 1e-4f + 1e-5f * (float)(rmax + dz);
-  const float R = (float)rmax + pad, Z = (float)dz + pad;
-  const float ox = (float)o.x, oy = (float)o.y, oz = (float)o.z;
-  const float dx = (float)d.x, dy = (float)d.y, dzz = (float)d.z;
-  float t0 = 0.f, t1 = 3.0e38f;
-  if (dzz != 0.f) {
-    float ta = (-Z - oz) / dzz, tb = (Z - oz) / dzz;
-    t0 = fmaxf(t0, fminf(ta, tb));
-    t1 = fminf(t1, fmaxf(ta, tb));
-  } else if (fabsf(oz) > Z) {
-    return false;
-  }
-  if (t0 > t1) return false;
-  float A = dx * dx + dy * dy, B = ox * dx + oy * dy, C = ox * ox + oy * oy - R * R;
-  if (A == 0.f) return C <= 0.f;
-  float disc = B * B - A * C;
-  if (disc < 0.f) return false;
-  float sq = sqrtf(disc);
-  float c0 = (-B - sq) / A, c1 = (-B + sq) / A;
-  return fmaxf(t0, c0) <= fminf(t1, c1) + pad;
-  (void)rmin;
-}
-
-template <bool MIXED = false, unsigned F = kFeatAll>
+// DistFromOutside (:383-412): the bounding-tube test, then the faces
 RBG_D double asph_dist_out(const Asph& a, d3 p, d3 d) {
   d3 pp = mk(p.x, p.y, p.z - a.P[RBG_ASPH_ORIGIN_Z]);
-  if (MIXED) {
-    if (!tube_reached_f32(pp, d, a.rmin(), a.rmax(), a.P[RBG_ASPH_DZ])) return kBig;
-  } else {
-    if (!tube_reached(pp, d, a.rmin(), a.rmax(), a.P[RBG_ASPH_DZ])) return kBig;
-  }
-  return asph_dist4<MIXED>(a, p, d);
+  if (!tube_reached(pp, d, a.rmin(), a.rmax(), a.P[RBG_ASPH_DZ])) return kBig;
+  return asph_dist4(a, p, d);
 }
 
 // ComputeNormal (:246-327)
@@ -1091,29 +921,28 @@ RBG_D double box_dist_fast(const double* P, d3 p, d3 d, bool exit, d3& nrm) {
   return tnear;
 }
 
-template <bool MIXED = false, unsigned F = kFeatAll>
+// shape queries of the FP64 path (the mixed path has its own, below)
+template <unsigned F = kFeatAll>
 RBG_D bool shape_contains(const DevScene& S, int shape, d3 p) {
   const int type = S.shapes[shape].type;
-  if (type == RBG_SHAPE_ASPHERIC_DISK)
-    return MIXED ? asph_contains_fast(Asph{SP(S, shape)}, p) : asph_contains(Asph{SP(S, shape)}, p);
+  if (type == RBG_SHAPE_ASPHERIC_DISK) return asph_contains(Asph{SP(S, shape)}, p);
   if (type == RBG_SHAPE_WINSTON_POLY) return (F & kFeatWinston) ? win_contains(win_load(SP(S, shape)), p) : false;
   if (!(F & kFeatCSG) && type == RBG_SHAPE_BOX) return prim_contains(RBG_SHAPE_BOX, SP(S, shape), p);
   return (F & kFeatCSG) ? csg_contains(S, shape, p) : false;
 }
 
-template <bool MIXED = false, unsigned F = kFeatAll>
+template <unsigned F = kFeatAll>
 RBG_D double shape_dist(const DevScene& S, int shape, d3 p, d3 d, bool exit, d3& nrm, unsigned& err) {
   const int type = S.shapes[shape].type;
   if (type == RBG_SHAPE_ASPHERIC_DISK) {
     Asph a{SP(S, shape)};
-    return exit ? asph_dist4<MIXED>(a, p, d) : asph_dist_out<MIXED>(a, p, d);
+    return exit ? asph_dist4(a, p, d) : asph_dist_out(a, p, d);
   }
   if (type == RBG_SHAPE_WINSTON_POLY) {
     if (!(F & kFeatWinston)) return kBig;
     Win w = win_load(SP(S, shape));
     return exit ? win_dist_in(w, p, d) : win_dist_out(w, p, d);
   }
-  if (MIXED && type == RBG_SHAPE_BOX) return box_dist_fast(SP(S, shape), p, d, exit, nrm);
   return (F & kFeatCSG) ? csg_dist(S, shape, p, d, exit, nrm, err) : kBig;
 }
 

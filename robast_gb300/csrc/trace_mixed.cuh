@@ -1,0 +1,108 @@
+// trace_mixed.cuh -- the mixed-precision tracer ("chosen form").
+//
+// A persistent kernel: one launch fills every SM with resident warps; each
+// warp keeps 32 rays in flight and advances them one boundary step at a
+// time.  Lanes whose ray has terminated are refilled from a global ray
+// counter: one __ballot_sync finds the free lanes, one atomicAdd per warp
+// reserves that many consecutive rays and each free lane takes its slot
+// (warp-ballot compaction of live rays), so lanes do not idle while the
+// warp's longest path finishes.  The per-step arithmetic uses the MIXED
+// instantiation of the tracer: FP32 screening and Newton iterations with an
+// FP64 polish of each accepted root, FP32 thin-film matrices and Fresnel
+// coefficients; ray positions, times and accepted intersection distances
+// stay FP64.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "scene_internal.h"
+#include "tracer.cuh"
+
+namespace rbg {
+
+constexpr int kMixedBlock = 128;
+
+// Instances: F = kFeatAll runs any scene; F = 0 (boxes and aspheric disks,
+// mirrors, obscurations and focal surfaces only, e.g. two-mirror
+// telescopes) compiles every other code path out, which frees registers.
+template <unsigned F>
+__global__ void __launch_bounds__(kMixedBlock) trace_mixed_kernel(DevScene S, KernelRays in, KernelOut out,
+                                                                  int64_t n, int limit, int disable_fresnel,
+                                                                  uint64_t seed, uint64_t id_offset,
+                                                                  unsigned* err_flags,
+                                                                  unsigned long long* next_ray) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lanes_below = (1u << lane) - 1u;
+  Ray r;
+  Nav nv;
+  int64_t idx = -1;
+  bool active = false;
+  bool drained = false;  // warp-uniform: the global queue is empty
+  unsigned err = 0;
+  r.status = RBG_STOP;
+  for (;;) {
+    unsigned need = __ballot_sync(FULL, !active);
+    if (need && !drained) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(next_ray, (unsigned long long)__popc(need));
+      base = __shfl_sync(FULL, base, leader);
+      if (base >= (unsigned long long)n) drained = true;
+      if (!active) {
+        unsigned long long mine = base + __popc(need & lanes_below);
+        if (mine < (unsigned long long)n) {
+          idx = (int64_t)mine;
+          if (load_ray(in, out, idx, seed, id_offset, r)) {
+            trace_begin<true, F>(S, r, nv);
+            active = true;
+          } else {
+            err |= r.err;
+            store_ray(out, idx, r);
+          }
+        }
+      }
+    }
+    if (!__any_sync(FULL, active)) {
+      if (drained) break;
+      continue;
+    }
+    if (active) {
+      trace_step<true, F>(S, r, nv, limit, disable_fresnel != 0);
+      if (r.status != RBG_RUN) {
+        err |= r.err;
+        store_ray(out, idx, r);
+        active = false;
+      }
+    }
+  }
+  if (err) atomicOr(err_flags, err);
+}
+
+// Launch over n rays on stream st: one block per resident slot of every SM
+// (occupancy queried once per instantiation), never more blocks than rays
+// need; the queue head is reset on the stream first.
+template <unsigned F>
+int launch_mixed_impl(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n,
+                      const rbg_trace_opts& o, cudaStream_t st, unsigned* err_flags, unsigned long long* counter) {
+  static int bps = 0;
+  static int sms = 0;
+  if (bps == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return RBG_ERR_CUDA;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return RBG_ERR_CUDA;
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_mixed_kernel<F>, kMixedBlock, 0) != cudaSuccess)
+      return RBG_ERR_CUDA;
+    bps = b < 1 ? 1 : b;
+  }
+  int64_t want = (n + kMixedBlock - 1) / kMixedBlock;
+  int64_t grid = (int64_t)sms * bps;
+  if (want < grid) grid = want;
+  if (cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st) != cudaSuccess) return RBG_ERR_CUDA;
+  trace_mixed_kernel<F><<<(int)grid, kMixedBlock, 0, st>>>(S, in, out, n, o.limit, o.disable_fresnel, o.seed,
+                                                          o.ray_id_offset, err_flags, counter);
+  if (cudaGetLastError() != cudaSuccess) return RBG_ERR_CUDA;
+  return RBG_OK;
+}
+
+}  // namespace rbg

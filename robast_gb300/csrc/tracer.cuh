@@ -23,11 +23,11 @@ RBG_D bool in_fbox(const float* lo, const float* hi, d3 p) {
   return !(p.x < lo[0] || p.x > hi[0] || p.y < lo[1] || p.y > hi[1] || p.z < lo[2] || p.z > hi[2]);
 }
 
-template <bool MIXED = false, unsigned F = kFeatAll>
+template <unsigned F = kFeatAll>
 RBG_D bool node_contains(const DevScene& S, int k, d3 p) {
   const rbg_node& N = S.nodes[k];
   if (!in_box(N.lo, N.hi, p)) return false;
-  return shape_contains<MIXED, F>(S, N.shape, to_local(N.m, p));
+  return shape_contains<F>(S, N.shape, to_local(N.m, p));
 }
 
 // FP32 segment/box test for the mixed path, enlarged so that it never
@@ -81,13 +81,13 @@ RBG_D bool seg_box(d3 o, d3 inv, d3 d, double smax, const T* lo, const T* hi) {
 }
 
 // first child (in placement order) of node k containing p, or -1
-template <bool MIXED = false, unsigned F = kFeatAll>
+template <unsigned F = kFeatAll>
 RBG_D int first_child_containing(const DevScene& S, int k, d3 p) {
   const rbg_node& N = S.nodes[k];
   if (!(F & kFeatBVH) || N.bvh_root < 0) {
     for (int i = 0; i < N.child_count; ++i) {
       int c = S.children[N.child_begin + i];
-      if (node_contains<MIXED, F>(S, c, p)) return c;
+      if (node_contains<F>(S, c, p)) return c;
     }
     return -1;
   }
@@ -101,7 +101,7 @@ RBG_D int first_child_containing(const DevScene& S, int k, d3 p) {
     if (b.left < 0) {
       for (int i = 0; i < b.right; ++i) {
         int c = S.bvh_items[b.item_begin + i];
-        if ((best < 0 || c < best) && node_contains<MIXED, F>(S, c, p)) best = c;
+        if ((best < 0 || c < best) && node_contains<F>(S, c, p)) best = c;
       }
     } else if (sp + 2 <= 32) {
       stack[sp++] = b.left;
@@ -111,19 +111,19 @@ RBG_D int first_child_containing(const DevScene& S, int k, d3 p) {
   return best;
 }
 
-template <bool MIXED = false, unsigned F = kFeatAll>
+template <unsigned F = kFeatAll>
 RBG_D int locate_down(const DevScene& S, int k, d3 p) {
   for (int depth = 0; depth < 64; ++depth) {
-    int c = first_child_containing<MIXED, F>(S, k, p);
+    int c = first_child_containing<F>(S, k, p);
     if (c < 0) return k;
     k = c;
   }
   return k;
 }
-template <bool MIXED = false, unsigned F = kFeatAll>
+template <unsigned F = kFeatAll>
 RBG_D int locate_from_top(const DevScene& S, d3 p) {
-  if (!node_contains<MIXED, F>(S, 0, p)) return -1;
-  return locate_down<MIXED, F>(S, 0, p);
+  if (!node_contains<F>(S, 0, p)) return -1;
+  return locate_down<F>(S, 0, p);
 }
 
 // ---- mixed-precision navigation: the same tree walks with FP32 screens
@@ -218,12 +218,12 @@ RBG_D double shape_dist_f(const DevScene& S, int shape, const LRay& L, bool exit
 }
 
 // candidate daughter test shared by the scan and the BVH walk
-template <bool MIXED, unsigned F = kFeatAll>
+template <unsigned F = kFeatAll>
 RBG_D void try_child(const DevScene& S, int k, d3 p, d3 d, double& best, int& xnode, bool& enter, d3& nbest,
                      unsigned& err) {
   const rbg_node& K = S.nodes[k];
   d3 nrm = mk(0, 0, 1);
-  double s = shape_dist<MIXED, F>(S, K.shape, to_local(K.m, p), dir_to_local(K.m, d), false, nrm, err);
+  double s = shape_dist<F>(S, K.shape, to_local(K.m, p), dir_to_local(K.m, d), false, nrm, err);
   // ties: leaving the mother first, then the lowest node id (placement order)
   if (s < best || (s == best && enter && k < xnode)) {
     best = s;
@@ -234,7 +234,7 @@ RBG_D void try_child(const DevScene& S, int k, d3 p, d3 d, double& best, int& xn
 }
 
 // TGeoNavigator::FindNextBoundaryAndStep
-template <bool MIXED, unsigned F = kFeatAll>
+template <unsigned F = kFeatAll>
 RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, unsigned& err) {
   const int c = nv.node;
   double best;
@@ -243,7 +243,7 @@ RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, 
   bool enter;
   if (c < 0) {
     const rbg_node& T = S.nodes[0];
-    best = shape_dist<MIXED, F>(S, T.shape, to_local(T.m, nv.p), dir_to_local(T.m, nv.d), false, nbest, err);
+    best = shape_dist<F>(S, T.shape, to_local(T.m, nv.p), dir_to_local(T.m, nv.d), false, nbest, err);
     if (best >= kBig) {
       step = 0;
       nv.xnode = -1;
@@ -253,33 +253,16 @@ RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, 
     enter = true;
   } else {
     const rbg_node& N = S.nodes[c];
-    best = shape_dist<MIXED, F>(S, N.shape, to_local(N.m, nv.p), dir_to_local(N.m, nv.d), true, nbest, err);
+    best = shape_dist<F>(S, N.shape, to_local(N.m, nv.p), dir_to_local(N.m, nv.d), true, nbest, err);
     xnode = c;
     enter = false;
-    d3 inv = mk(0, 0, 0);
-    float fo[3], fi[3];
-    bool fz[3];
-    if (MIXED) {
-      const double dd[3] = {nv.d.x, nv.d.y, nv.d.z}, pp[3] = {nv.p.x, nv.p.y, nv.p.z};
-      for (int a = 0; a < 3; ++a) {
-        fo[a] = (float)pp[a];
-        fz[a] = dd[a] == 0;
-        fi[a] = fz[a] ? 0.f : 1.0f / (float)dd[a];
-      }
-    } else {
-      inv = mk(1.0 / nv.d.x, 1.0 / nv.d.y, 1.0 / nv.d.z);
-    }
-    auto culled = [&](auto lo, auto hi) {
-      if (MIXED) return !seg_box_f32(fo[0], fo[1], fo[2], fi[0], fi[1], fi[2], fz[0], fz[1], fz[2],
-                                     best >= kBig ? 3e38f : (float)best, lo, hi);
-      return !seg_box(nv.p, inv, nv.d, best, lo, hi);
-    };
+    const d3 inv = mk(1.0 / nv.d.x, 1.0 / nv.d.y, 1.0 / nv.d.z);
     if (!(F & kFeatBVH) || N.bvh_root < 0) {
       for (int i = 0; i < N.child_count; ++i) {
         int k = S.children[N.child_begin + i];
         const rbg_node& K = S.nodes[k];
-        if (culled(K.lo, K.hi)) continue;
-        try_child<MIXED, F>(S, k, nv.p, nv.d, best, xnode, enter, nbest, err);
+        if (!seg_box(nv.p, inv, nv.d, best, K.lo, K.hi)) continue;
+        try_child<F>(S, k, nv.p, nv.d, best, xnode, enter, nbest, err);
       }
     } else {
       int stack[32];
@@ -287,13 +270,13 @@ RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, 
       stack[sp++] = N.bvh_root;
       while (sp > 0) {
         const rbg_bvh_node& b = S.bvh[stack[--sp]];
-        if (culled(b.lo, b.hi)) continue;
+        if (!seg_box(nv.p, inv, nv.d, best, b.lo, b.hi)) continue;
         if (b.left < 0) {
           for (int i = 0; i < b.right; ++i) {
             int k = S.bvh_items[b.item_begin + i];
             const rbg_node& K = S.nodes[k];
-            if (culled(K.lo, K.hi)) continue;
-            try_child<MIXED, F>(S, k, nv.p, nv.d, best, xnode, enter, nbest, err);
+            if (!seg_box(nv.p, inv, nv.d, best, K.lo, K.hi)) continue;
+            try_child<F>(S, k, nv.p, nv.d, best, xnode, enter, nbest, err);
           }
         } else if (sp + 2 <= 32) {
           stack[sp++] = b.right;
@@ -309,11 +292,11 @@ RBG_D int find_next_boundary_and_step(const DevScene& S, Nav& nv, double& step, 
   nv.xn = nbest;
   int next;
   if (enter) {
-    next = locate_down<MIXED, F>(S, xnode, nv.p);
+    next = locate_down<F>(S, xnode, nv.p);
   } else {
     int q = S.nodes[c].parent;
-    while (q >= 0 && !node_contains<MIXED, F>(S, q, nv.p)) q = S.nodes[q].parent;
-    next = q < 0 ? -1 : locate_down<MIXED, F>(S, q, nv.p);
+    while (q >= 0 && !node_contains<F>(S, q, nv.p)) q = S.nodes[q].parent;
+    next = q < 0 ? -1 : locate_down<F>(S, q, nv.p);
   }
   nv.node = next;
   step = best;
@@ -788,7 +771,7 @@ RBG_D void do_reflection(const DevScene& S, Nav& nv, Ray& r, double n1, double s
   }
   double t = MIXED ? r.t + step * (n1 * (1.0 / RBG_SPEED_OF_LIGHT_CM)) : r.t + step / (RBG_SPEED_OF_LIGHT_CM / n1);
   nv.p = nv.p - RBG_REFLECT_BACKSTEP * d1;
-  nv.node = MIXED ? locate_from_top_f<F>(S, nv.p) : locate_from_top<MIXED, F>(S, nv.p);
+  nv.node = MIXED ? locate_from_top_f<F>(S, nv.p) : locate_from_top<F>(S, nv.p);
   nv.d = d2;
   add_point(r, nv.p, t);
   add_node(r, next);
@@ -877,7 +860,7 @@ template <bool MIXED = false, unsigned F = kFeatAll>
 RBG_D void trace_begin(const DevScene& S, Ray& r, Nav& nv) {
   nv.p = r.x;
   nv.d = r.d;
-  nv.node = MIXED ? locate_from_top_f<F>(S, nv.p) : locate_from_top<MIXED, F>(S, nv.p);
+  nv.node = MIXED ? locate_from_top_f<F>(S, nv.p) : locate_from_top<F>(S, nv.p);
   nv.xnode = -1;
   nv.xn = mk(0, 0, 1);
   nv.xface = 0;
@@ -892,7 +875,7 @@ RBG_D void trace_step(const DevScene& S, Ray& r, Nav& nv, int limit, bool disabl
   const int cur = nv.node;
   double step;
   const int next = MIXED ? find_next_boundary_and_step_f<F>(S, nv, step, r.err)
-                         : find_next_boundary_and_step<MIXED, F>(S, nv, step, r.err);
+                         : find_next_boundary_and_step<F>(S, nv, step, r.err);
   const int tc = kind_of(S, cur), tn = kind_of(S, next);
 
   if ((F & kFeatLens) && tc == kLens) {

@@ -120,3 +120,39 @@ def test_rays_starting_outside_the_top_volume(prec):
         np.testing.assert_allclose(got[k], ref[k], rtol=1e-6, atol=1e-6)
     assert (got["status"][: n // 4] == N.RBG_EXIT).all()
     assert (got["status"][n // 4: n // 2] == N.RBG_FOCUS).mean() > 0.3
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_host_pipeline_matches_device_trace(prec):
+    """rbg_trace_host runs the batch as chunks of 2^21 rays over two streams
+    with per-chunk ray-id offsets: two chunks (the second partial), with
+    histories, must equal one device-buffer trace bit for bit, and a second
+    call reusing the workspace must equal the first."""
+    import torch
+
+    from robast_gb300 import device
+    from robast_gb300.manager import make_result
+
+    n = (1 << 21) + 3001
+    man, batch = configs.davies_cotton(n_rays=n, n_angles=2)
+    hist = 2
+    rays = device.to_device(batch, "cuda:0")
+    ref_res = device.alloc_result(n, "cuda:0", hist)
+    ref_res, st = device.trace(man, rays, ref_res, precision=prec)
+    torch.cuda.synchronize()
+    assert st == N.RBG_OK
+    ref = {k: v.cpu().numpy() for k, v in ref_res.items()}
+    arr = configs.to_array(batch)
+    dp = C.POINTER(C.c_double)
+    rs = N.Rays(n, *(getattr(arr, f).ctypes.data_as(dp) for f in ("x", "y", "z", "t", "dx", "dy", "dz", "lam")))
+    opts = man.trace_options(prec)
+    for call in range(2):
+        rr, got = make_result(n, hist)
+        st = N.lib().rbg_trace_host(man._ensure_scene().handle, C.byref(rs), C.byref(rr), C.byref(opts))
+        assert st == N.RBG_OK, (call, N.status_string(st))
+        assert N.lib().rbg_last_launch_count(man.scene.handle) == 2
+        for k in FIELDS:
+            np.testing.assert_array_equal(got[k], ref[k], err_msg=f"call {call}: {k}")
+        valid = np.arange(hist)[None, :] < np.minimum(ref["npoints"], hist)[:, None]
+        np.testing.assert_array_equal(got["hist_node"][valid], ref["hist_node"][valid])
+        np.testing.assert_array_equal(got["hist_xyzt"][valid], ref["hist_xyzt"][valid])
