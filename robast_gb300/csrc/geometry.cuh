@@ -1039,20 +1039,31 @@ RBG_NOINLINE double asph_dist_surface_exact(const double* P, int n, d3 point, d3
 RBG_NOINLINE double asph_dist_wall_exact(const double* P, bool outer, d3 point, d3 dir) {
   return asph_dist_wall(Asph{P}, outer, point, dir);
 }
-RBG_NOINLINE bool asph_contains_exact(const double* P, d3 p) { return asph_contains_fast(Asph{P}, p); }
+// Contains in FP64: for faces with c == 0 the sags are z + sum K_j H2^(j+1)
+// by FMA Horner (one sum when both faces share it); conic faces take the
+// full evaluation
+RBG_NOINLINE bool asph_contains_exact(const double* P, d3 p, bool twin) {
+  const double H2 = p.x * p.x + p.y * p.y;
+  const double rmin = P[RBG_ASPH_RMIN], rmax = P[RBG_ASPH_RMAX];
+  if (H2 > rmax * rmax || H2 < rmin * rmin) return false;
+  if (P[RBG_ASPH_C1] != 0 || P[RBG_ASPH_C2] != 0) return asph_contains_fast(Asph{P}, p);
+  const int n1 = (int)P[RBG_ASPH_NPOL1], n2 = (int)P[RBG_ASPH_NPOL2];
+  const double p1 = asph_poly(P + RBG_ASPH_K, n1, H2);
+  if (p.z < P[RBG_ASPH_Z1] + p1) return false;
+  const double p2 = twin ? p1 : asph_poly(P + RBG_ASPH_K + n1, n2, H2);
+  return !(P[RBG_ASPH_Z2] + p2 < p.z);
+}
 RBG_NOINLINE d3 asph_normal_exact(const double* P, d3 point, d3 dir) {
   return asph_normal_fast(Asph{P}, point, dir);
 }
 
-// DistToAsphere (src/AGeoAsphericDisk.cxx:415-526), mixed precision: the
-// reference's iteration (spherical first guess, Newton along the ray) in
-// FP32 from the float parameters, relative to the face vertex, tracking the
-// distance t; then FP64 polish steps t += s (x(h2) - z) with the FP32 slope
-// s until |step| < 1e-10 (the reference's stopping rule).  The distance is
-// t itself (the reference's |np - point| for a unit direction), rejected
-// when t < 0 (its dot(dir, np - point) < 0) or when the hit radius lies
-// outside [rmin, rmax] (compared squared).
-RBG_D double asph_dist_surface_f(const double* P, const float* Pf, int n, const LRay& L) {
+// DistToAsphere (src/AGeoAsphericDisk.cxx:415-526), mixed precision, in
+// three parts.
+//
+// asph_newton_f: the reference's iteration (spherical first guess, Newton
+// along the ray) in FP32 from the float parameters, relative to the face
+// vertex, tracking the distance t.  Returns false when it breaks down.
+RBG_D bool asph_newton_f(const float* Pf, int n, const LRay& L, float& t_out, float& scale_out) {
   const int npol1 = (int)Pf[RBG_ASPH_NPOL1];
   const int npol = n == 1 ? npol1 : (int)Pf[RBG_ASPH_NPOL2];
   const float* Kf = Pf + RBG_ASPH_K + (n == 1 ? 0 : npol1);
@@ -1064,15 +1075,13 @@ RBG_D double asph_dist_surface_f(const double* P, const float* Pf, int n, const 
   float M = p * dz + pz;
   float M2 = pz * pz + H2 - p * p;
   float check = 1.f - (M2 * curve - 2.f * M) * curve / dz / dz;
-  if (!(check >= 0.f)) return asph_dist_surface_exact(P, n, L.p, L.d);
+  if (!(check >= 0.f)) return false;
   float tf = p + (M2 * curve - 2.f * M) / (dz * (1.f + sqrtf(check)));
   float nx = px + tf * dx, ny = py + tf * dy, nz = pz + tf * dz;
-  float scale = 1.f;
-  bool ok = false;
   for (int i = 0; i < 40; i++) {
     H2 = nx * nx + ny * ny;
     check = 1.f - kappa * H2 * curve * curve;
-    if (check < 0) break;
+    if (check < 0) return false;
     float l = sqrtf(check);
     float x = 0.f, v = 0.f;
     for (int j = npol - 1; j >= 0; --j) {
@@ -1087,50 +1096,89 @@ RBG_D double asph_dist_surface_f(const double* P, const float* Pf, int n, const 
     m /= norm;
     nn /= norm;
     check = dz * l + dx * m + dy * nn;
-    if (check == 0.f) break;
-    scale = l / check;  // dt per unit sag residual
+    if (check == 0.f) return false;
+    const float scale = l / check;  // dt per unit sag residual
     float e = scale * (x - nz);
     tf += e;
     nx += e * dx;
     ny += e * dy;
     nz += e * dz;
     if (fabsf(e) < 4e-6f * (1.f + fabsf(nz) + sqrtf(H2))) {
-      ok = true;
-      break;
+      if (!isfinite(tf)) return false;
+      t_out = tf;
+      scale_out = scale;
+      return true;
     }
   }
-  if (!ok || !isfinite(tf)) return asph_dist_surface_exact(P, n, L.p, L.d);
+  return false;
+}
+
+// asph_polish: FP64 steps t += s (x(h2) - z) with the FP32 slope s from t
+// until |step| < 1e-10 (the reference's stopping rule).  Returns false when
+// it does not converge in 8 steps or leaves the conic's domain.
+RBG_D bool asph_polish(const double* P, int n, const LRay& L, double sc, double& t) {
   const int s1 = n == 1;
+  const int npol1 = (int)P[RBG_ASPH_NPOL1];
+  const int npol = s1 ? npol1 : (int)P[RBG_ASPH_NPOL2];
   const double* K = P + RBG_ASPH_K + (s1 ? 0 : npol1);
   const double c64 = P[s1 ? RBG_ASPH_C1 : RBG_ASPH_C2];
   const double kap64 = P[s1 ? RBG_ASPH_KAPPA1 : RBG_ASPH_KAPPA2];
   const double pz0 = L.p.z - P[s1 ? RBG_ASPH_Z1 : RBG_ASPH_Z2];
-  const double sc = (double)scale;
-  double t = (double)tf;
-  bool conv = false;
   for (int it = 0; it < 8; ++it) {
     double qx = fma(t, L.d.x, L.p.x), qy = fma(t, L.d.y, L.p.y), qz = fma(t, L.d.z, pz0);
     double h2 = fma(qx, qx, qy * qy);
     double x = asph_poly(K, npol, h2);
     if (c64 != 0) {
       double chk = 1 - kap64 * h2 * c64 * c64;
-      if (chk < 0) return asph_dist_surface_exact(P, n, L.p, L.d);
+      if (chk < 0) return false;
       x += (1 - sqrt(chk)) / c64 / kap64;
     }
     double e = sc * (x - qz);
     t += e;
-    if (fabs(e) < 1e-10) {
-      conv = true;
-      break;
-    }
+    if (fabs(e) < 1e-10) return true;
   }
-  if (!conv) return asph_dist_surface_exact(P, n, L.p, L.d);
+  return false;
+}
+
+// asph_accept: the distance to a converged root is t itself (the
+// reference's |np - point| for a unit direction), rejected when t < 0 (its
+// dot(dir, np - point) < 0) or when the hit radius lies outside
+// [rmin, rmax] (compared squared)
+RBG_D double asph_accept(const double* P, const LRay& L, double t) {
   if (t < 0) return kBig;
   double qx = fma(t, L.d.x, L.p.x), qy = fma(t, L.d.y, L.p.y);
   double h2 = fma(qx, qx, qy * qy);
   const double rmin = P[RBG_ASPH_RMIN], rmax = P[RBG_ASPH_RMAX];
   if (h2 < rmin * rmin || h2 > rmax * rmax) return kBig;
   return t;
+}
+
+// Both faces.  With twin faces (same polynomial, c and kappa; vertex z
+// apart by dz) the residual of face 2 at face 1's root is exactly dz, so
+// face 2's polish starts from t1 + s dz without a second FP32 iteration.
+RBG_D void asph_faces_f(const double* P, const float* Pf, const LRay& L, bool twin, double& d1, double& d2) {
+  float tf, sf;
+  double t1 = 0, sc = 1;
+  bool ok1 = asph_newton_f(Pf, 1, L, tf, sf);
+  if (ok1) {
+    t1 = (double)tf;
+    sc = (double)sf;
+    ok1 = asph_polish(P, 1, L, sc, t1);
+  }
+  d1 = ok1 ? asph_accept(P, L, t1) : asph_dist_surface_exact(P, 1, L.p, L.d);
+  double t2;
+  bool ok2;
+  if (twin && ok1) {
+    t2 = t1 + sc * (P[RBG_ASPH_Z2] - P[RBG_ASPH_Z1]);
+    ok2 = asph_polish(P, 2, L, sc, t2);
+  } else {
+    ok2 = asph_newton_f(Pf, 2, L, tf, sf);
+    if (ok2) {
+      t2 = (double)tf;
+      ok2 = asph_polish(P, 2, L, (double)sf, t2);
+    }
+  }
+  d2 = ok2 ? asph_accept(P, L, t2) : asph_dist_surface_exact(P, 2, L.p, L.d);
 }
 
 // FP32 screen of DistToInner/DistToOuter from the float parameters (the
@@ -1164,10 +1212,10 @@ RBG_D bool asph_wall_maybe_f(const float* Pf, bool outer, const LRay& L, float l
 
 // DistFromInside (:363-380): nearest of the two faces and the two walls;
 // `face` = 1, 2 (faces), 3 (inner wall), 4 (outer wall) of the minimum
-RBG_D double asph_dist4_f(const double* P, const float* Pf, const LRay& L, int& face) {
-  double best = asph_dist_surface_f(P, Pf, 1, L);
+RBG_D double asph_dist4_f(const double* P, const float* Pf, const LRay& L, bool twin, int& face) {
+  double best, v;
+  asph_faces_f(P, Pf, L, twin, best, v);
   face = 1;
-  double v = asph_dist_surface_f(P, Pf, 2, L);
   if (v < best) {
     best = v;
     face = 2;
@@ -1192,7 +1240,7 @@ RBG_D double asph_dist4_f(const double* P, const float* Pf, const LRay& L, int& 
 
 // DistFromOutside (:383-412): the bounding-tube screen in FP32 (enlarged,
 // never rejecting a ray the exact TGeoTube test accepts), then the faces
-RBG_D double asph_dist_out_f(const double* P, const float* Pf, const LRay& L, int& face) {
+RBG_D double asph_dist_out_f(const double* P, const float* Pf, const LRay& L, bool twin, int& face) {
   // pad: 1e-4 cm, plus 1e-5 of the tube size and 1e-6 of the coordinates
   // (the float position and origin carry ~6e-8 relative error each)
   const float pad = 1e-4f + 1e-5f * (Pf[RBG_ASPH_RMAX] + Pf[RBG_ASPH_DZ]) +
@@ -1220,13 +1268,13 @@ RBG_D double asph_dist_out_f(const double* P, const float* Pf, const LRay& L, in
     const float lo = fmaxf(t0, c0), hi = fminf(t1, c1);
     if (lo > hi + pad + 1e-5f * (fabsf(lo) + fabsf(hi))) return kBig;
   }
-  return asph_dist4_f(P, Pf, L, face);
+  return asph_dist4_f(P, Pf, L, twin, face);
 }
 
 // Contains (:330-347) behind FP32 screens of the radius and of both sags
 // (faces with c == 0; the screen margin is 2e-5 of the sum of the sag's term
 // magnitudes plus the coordinates, >10x the FP32 rounding of the sums)
-RBG_D bool asph_contains_f(const double* P, const float* Pf, const LRay& L) {
+RBG_D bool asph_contains_f(const double* P, const float* Pf, const LRay& L, bool twin) {
   const float h = L.pf.x * L.pf.x + L.pf.y * L.pf.y;
   const float rmax = Pf[RBG_ASPH_RMAX], rmin = Pf[RBG_ASPH_RMIN];
   const float hr = 4e-6f * h + 1e-12f;
@@ -1244,7 +1292,7 @@ RBG_D bool asph_contains_f(const double* P, const float* Pf, const LRay& L) {
     if (z < f1 - e1 || z > f2 + e2) return false;
     if (radial_in && z > f1 + e1 && z < f2 - e2) return true;
   }
-  return asph_contains_exact(P, L.p);
+  return asph_contains_exact(P, L.p, twin);
 }
 
 // TGeoBBox::Contains behind an FP32 screen
@@ -1257,6 +1305,36 @@ RBG_D bool box_contains_f(const double* P, const float* Pf, const LRay& L) {
   if (ax > Pf[RBG_BOX_DX] + ex || ay > Pf[RBG_BOX_DY] + ey || az > Pf[RBG_BOX_DZ] + ez) return false;
   if (ax < Pf[RBG_BOX_DX] - ex && ay < Pf[RBG_BOX_DY] - ey && az < Pf[RBG_BOX_DZ] - ez) return true;
   return prim_contains(RBG_SHAPE_BOX, P, L.p);
+}
+
+// Lower and upper bounds of TGeoBBox::DistFromInside (the slab exit
+// distance box_dist_fast computes in FP64) from the float ray.  Each
+// axis's bound allows 1e-6 of the terms it is made of (the float inputs
+// carry ~6e-8 relative error, three float operations follow).  Returns
+// false when an axis's direction underflows to zero in float while it is
+// not zero in FP64 (then only the FP64 distance is valid).
+RBG_D bool box_exit_bounds_f(const float* Pf, const LRay& L, float& lo, float& hi) {
+  const float pf[3] = {L.pf.x, L.pf.y, L.pf.z}, df[3] = {L.df.x, L.df.y, L.df.z};
+  const double dd[3] = {L.d.x, L.d.y, L.d.z};
+  lo = 3e38f;
+  hi = 3e38f;
+  bool any = false;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (df[k] == 0.f) {
+      if (dd[k] != 0.0) return false;
+      continue;
+    }
+    const float o = pf[k] - Pf[RBG_BOX_OX + k];
+    const float half = Pf[RBG_BOX_DX + k];
+    const float inv = 1.0f / df[k];
+    const float t = ((df[k] > 0.f ? half : -half) - o) * inv;
+    const float e = 1e-6f * ((fabsf(pf[k]) + fabsf(Pf[RBG_BOX_OX + k]) + half) * fabsf(inv) + fabsf(t)) + 1e-30f;
+    lo = fminf(lo, t - e);
+    hi = fminf(hi, t + e);
+    any = true;
+  }
+  return any;
 }
 
 // Node-local normal of an aspheric disk at a point just past face `face`

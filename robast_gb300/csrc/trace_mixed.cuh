@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kMixedBlock) trace_mixed_kernel(DevScene S, Ke
         unsigned long long mine = base + __popc(need & lanes_below);
         if (mine < (unsigned long long)n) {
           idx = (int64_t)mine;
-          if (load_ray(in, out, idx, seed, id_offset, r)) {
+          if (load_ray_f(in, out, idx, seed, id_offset, r)) {
             trace_begin<true, F>(S, r, nv);
             active = true;
           } else {

@@ -133,11 +133,11 @@ RBG_D bool in_fbox3(const float* lo, const float* hi, f3 p) {
 }
 
 template <unsigned F>
-RBG_D bool shape_contains_f(const DevScene& S, int shape, const LRay& L) {
+RBG_D bool shape_contains_f(const DevScene& S, int shape, const LRay& L, bool twin) {
   const rbg_shape_desc& sh = S.shapes[shape];
   const double* P = S.params + sh.param_offset;
   const float* Pf = S.fparams + sh.param_offset;
-  if (sh.type == RBG_SHAPE_ASPHERIC_DISK) return asph_contains_f(P, Pf, L);
+  if (sh.type == RBG_SHAPE_ASPHERIC_DISK) return asph_contains_f(P, Pf, L, twin);
   if (sh.type == RBG_SHAPE_BOX) return box_contains_f(P, Pf, L);
   if (sh.type == RBG_SHAPE_WINSTON_POLY) return (F & kFeatWinston) ? win_contains(win_load(P), L.p) : false;
   return (F & kFeatCSG) ? csg_contains(S, shape, L.p) : false;
@@ -149,16 +149,31 @@ template <unsigned F>
 RBG_D bool node_contains_f(const DevScene& S, int k, d3 p, f3 pf) {
   const rbg_node_aux& A = S.aux[k];
   if (!in_fbox3(A.lo, A.hi, pf)) return false;
-  return shape_contains_f<F>(S, S.nodes[k].shape, local_point(S, k, p, pf));
+  return shape_contains_f<F>(S, S.nodes[k].shape, local_point(S, k, p, pf), A.flags & RBG_AUX_ASPH_TWIN_FACES);
 }
 
 template <unsigned F>
 RBG_D int first_child_containing_f(const DevScene& S, int k, d3 p, f3 pf) {
   const rbg_node& N = S.nodes[k];
   if (!(F & kFeatBVH) || N.bvh_root < 0) {
-    for (int i = 0; i < N.child_count; ++i) {
-      int c = S.children[N.child_begin + i];
-      if (node_contains_f<F>(S, c, p, pf)) return c;
+    // box tests of every daughter first, then the shape tests of the
+    // survivors in placement order: the lanes of a warp run the same shape
+    // code on different daughters instead of taking turns
+    for (int base = 0; base < N.child_count; base += 32) {
+      const int m = N.child_count - base < 32 ? N.child_count - base : 32;
+      unsigned mask = 0;
+      for (int i = 0; i < m; ++i) {
+        const rbg_node_aux& A = S.aux[S.children[N.child_begin + base + i]];
+        if (in_fbox3(A.lo, A.hi, pf)) mask |= 1u << i;
+      }
+      while (mask) {
+        const int i = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int c = S.children[N.child_begin + base + i];
+        if (shape_contains_f<F>(S, S.nodes[c].shape, local_point(S, c, p, pf),
+                                S.aux[c].flags & RBG_AUX_ASPH_TWIN_FACES))
+          return c;
+      }
     }
     return -1;
   }
@@ -198,15 +213,17 @@ RBG_D int locate_from_top_f(const DevScene& S, d3 p) {
   return locate_down_f<F>(S, 0, p, pf);
 }
 
-// shape distance in the mixed path; `face` receives the aspheric face
+// shape distance of node k in the mixed path; `face` receives the aspheric face
 template <unsigned F>
-RBG_D double shape_dist_f(const DevScene& S, int shape, const LRay& L, bool exit, d3& nrm, int& face, unsigned& err) {
+RBG_D double shape_dist_f(const DevScene& S, int k, const LRay& L, bool exit, d3& nrm, int& face, unsigned& err) {
+  const int shape = S.nodes[k].shape;
   const rbg_shape_desc& sh = S.shapes[shape];
   const double* P = S.params + sh.param_offset;
   face = 0;
   if (sh.type == RBG_SHAPE_ASPHERIC_DISK) {
     const float* Pf = S.fparams + sh.param_offset;
-    return exit ? asph_dist4_f(P, Pf, L, face) : asph_dist_out_f(P, Pf, L, face);
+    const bool twin = S.aux[k].flags & RBG_AUX_ASPH_TWIN_FACES;
+    return exit ? asph_dist4_f(P, Pf, L, twin, face) : asph_dist_out_f(P, Pf, L, twin, face);
   }
   if (sh.type == RBG_SHAPE_WINSTON_POLY) {
     if (!(F & kFeatWinston)) return kBig;
@@ -317,7 +334,7 @@ RBG_D int find_next_boundary_and_step_f(const DevScene& S, Nav& nv, double& step
   int xnode, face = 0, xface = 0;
   bool enter;
   if (c < 0) {
-    best = shape_dist_f<F>(S, S.nodes[0].shape, local_ray(S, 0, nv.p, nv.d, pf, df), false, nbest, xface, err);
+    best = shape_dist_f<F>(S, 0, local_ray(S, 0, nv.p, nv.d, pf, df), false, nbest, xface, err);
     if (best >= kBig) {
       step = 0;
       nv.xnode = -1;
@@ -327,17 +344,29 @@ RBG_D int find_next_boundary_and_step_f(const DevScene& S, Nav& nv, double& step
     enter = true;
   } else {
     const rbg_node& N = S.nodes[c];
-    best = shape_dist_f<F>(S, N.shape, local_ray(S, c, nv.p, nv.d, pf, df), true, nbest, xface, err);
+    const LRay Lc = local_ray(S, c, nv.p, nv.d, pf, df);
+    // A box mother's exit distance is needed only if no daughter is hit
+    // before it: start from an FP32 upper bound (it only widens the
+    // culling) and take the FP64 distance afterwards unless a daughter
+    // lies below the FP32 lower bound.  The result equals taking the FP64
+    // exit first: a daughter replaces the mother only when strictly nearer.
+    float exit_lo = 0.f, exit_hi = 0.f;
+    const bool lazy = S.shapes[N.shape].type == RBG_SHAPE_BOX &&
+                      box_exit_bounds_f(S.fparams + S.shapes[N.shape].param_offset, Lc, exit_lo, exit_hi) &&
+                      exit_lo > 0.f;
+    best = lazy ? (double)exit_hi : shape_dist_f<F>(S, c, Lc, true, nbest, xface, err);
     xnode = c;
     enter = false;
     const bool zx = df.x == 0.f, zy = df.y == 0.f, zz = df.z == 0.f;
     const float ix = zx ? 0.f : 1.0f / df.x, iy = zy ? 0.f : 1.0f / df.y, iz = zz ? 0.f : 1.0f / df.z;
+    auto reach = [&](const float* lo, const float* hi) {
+      return seg_box_f32(pf.x, pf.y, pf.z, ix, iy, iz, zx, zy, zz, best >= kBig ? 3e38f : (float)best, lo, hi);
+    };
     auto visit = [&](int k) {
       const rbg_node_aux& A = S.aux[k];
-      if (!seg_box_f32(pf.x, pf.y, pf.z, ix, iy, iz, zx, zy, zz, best >= kBig ? 3e38f : (float)best, A.lo, A.hi))
-        return;
+      if (!reach(A.lo, A.hi)) return;
       d3 nrm = mk(0, 0, 1);
-      double s = shape_dist_f<F>(S, S.nodes[k].shape, local_ray(S, k, nv.p, nv.d, pf, df), false, nrm, face, err);
+      double s = shape_dist_f<F>(S, k, local_ray(S, k, nv.p, nv.d, pf, df), false, nrm, face, err);
       // ties: leaving the mother first, then the lowest node id (placement order)
       if (s < best || (s == best && enter && k < xnode)) {
         best = s;
@@ -348,15 +377,29 @@ RBG_D int find_next_boundary_and_step_f(const DevScene& S, Nav& nv, double& step
       }
     };
     if (!(F & kFeatBVH) || N.bvh_root < 0) {
-      for (int i = 0; i < N.child_count; ++i) visit(S.children[N.child_begin + i]);
+      // cull every daughter first, then test the survivors in placement
+      // order (visit re-checks the box against the shrinking distance, so
+      // the tested set is the one a single pass would test)
+      for (int base = 0; base < N.child_count; base += 32) {
+        const int m = N.child_count - base < 32 ? N.child_count - base : 32;
+        unsigned mask = 0;
+        for (int i = 0; i < m; ++i) {
+          const rbg_node_aux& A = S.aux[S.children[N.child_begin + base + i]];
+          if (reach(A.lo, A.hi)) mask |= 1u << i;
+        }
+        while (mask) {
+          const int i = __ffs(mask) - 1;
+          mask &= mask - 1;
+          visit(S.children[N.child_begin + base + i]);
+        }
+      }
     } else {
       int stack[32];
       int sp = 0;
       stack[sp++] = N.bvh_root;
       while (sp > 0) {
         const rbg_bvh_node& b = S.bvh[stack[--sp]];
-        if (!seg_box_f32(pf.x, pf.y, pf.z, ix, iy, iz, zx, zy, zz, best >= kBig ? 3e38f : (float)best, b.lo, b.hi))
-          continue;
+        if (!reach(b.lo, b.hi)) continue;
         if (b.left < 0) {
           for (int i = 0; i < b.right; ++i) visit(S.bvh_items[b.item_begin + i]);
         } else if (sp + 2 <= 32) {
@@ -365,6 +408,17 @@ RBG_D int find_next_boundary_and_step_f(const DevScene& S, Nav& nv, double& step
         } else {
           err |= ERR_BIT_CAP;
         }
+      }
+    }
+    if (lazy && !(enter && best < (double)exit_lo)) {
+      d3 en = mk(0, 0, 1);
+      const double e = box_dist_fast(S.params + S.shapes[N.shape].param_offset, Lc.p, Lc.d, true, en);
+      if (!enter || e <= best) {
+        best = e;
+        xnode = c;
+        enter = false;
+        nbest = en;
+        xface = 0;
       }
     }
   }
@@ -985,6 +1039,45 @@ RBG_D bool load_ray(const KernelRays& in, const KernelOut& out, int64_t i, uint6
     return false;
   }
   set_direction(r, dd);
+  return true;
+}
+
+// load_ray for the mixed path: the same checks, with the finiteness tests
+// on the exponent bits and the direction scaled by a refined reciprocal
+// square root instead of three FP64 divisions (the unit vector differs from
+// ARay::SetDirection's by at most a few ulp)
+RBG_D bool finite_bits(double v) {
+  return (__double_as_longlong(v) & 0x7ff0000000000000LL) != 0x7ff0000000000000LL;
+}
+RBG_D bool load_ray_f(const KernelRays& in, const KernelOut& out, int64_t i, uint64_t seed, uint64_t id_offset,
+                      Ray& r) {
+  r.x = mk(in.x[i], in.y[i], in.z[i]);
+  r.t = in.t ? in.t[i] : 0.0;
+  r.lambda = in.lambda[i];
+  d3 dd = mk(in.dx[i], in.dy[i], in.dz[i]);
+  r.status = RBG_RUN;
+  r.npoints = 0;
+  r.last_node = -2;
+  r.err = 0;
+  r.hist_cap = out.hist_cap;
+  r.hist_xyzt = out.hist_cap ? out.hist_xyzt + (size_t)i * out.hist_cap * 4 : nullptr;
+  r.hist_node = out.hist_cap ? out.hist_node + (size_t)i * out.hist_cap : nullptr;
+  r.rng.init(seed, id_offset + (uint64_t)i, 0);
+  add_point(r, r.x, r.t);
+  const double m2 = dot(dd, dd);
+  const bool bad = !finite_bits(r.x.x) || !finite_bits(r.x.y) || !finite_bits(r.x.z) || !finite_bits(dd.x) ||
+                   !finite_bits(dd.y) || !finite_bits(dd.z) || !(m2 > 0) || !finite_bits(m2);
+  if (bad) {
+    r.d = dd;
+    r.err |= ERR_BIT_NAN;
+    return false;
+  }
+  if (m2 > 1e-30 && m2 < 1e30) {
+    const double inv = rsqrt_refined(m2);
+    r.d = mk(dd.x * inv, dd.y * inv, dd.z * inv);
+  } else {
+    set_direction(r, dd);
+  }
   return true;
 }
 
