@@ -76,7 +76,9 @@ int ensure_device(rbg_scene* s) {
       (rc = upload(d->allocations, s->borders, &v.borders)) ||
       (rc = upload(d->allocations, s->params, &v.params)) ||
       (rc = upload(d->allocations, s->node_aux, &v.aux)) ||
-      (rc = upload(d->allocations, s->fparams, &v.fparams))) {
+      (rc = upload(d->allocations, s->fparams, &v.fparams)) ||
+      (rc = upload(d->allocations, s->trig, &v.trig)) ||
+      (rc = upload(d->allocations, s->trig_off, &v.trig_off))) {
     for (void* p : d->allocations) cudaFree(p);
     delete d;
     return rc;

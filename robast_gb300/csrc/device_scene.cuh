@@ -30,6 +30,9 @@ struct DevScene {
   // float copy of params (same offsets)
   const rbg_node_aux* aux;
   const float* fparams;
+  // per-shape trigonometric constants (node_aux.h), both tracers
+  const double* trig;
+  const int32_t* trig_off;
   int32_t n_nodes, n_borders, n_multilayers, n_tables;
   uint32_t features;  // kFeat* bits present in the scene
 };

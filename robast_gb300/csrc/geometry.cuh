@@ -14,6 +14,9 @@
 #pragma once
 #include "device_scene.cuh"
 
+// out-of-line device helpers (one copy per translation unit)
+#define RBG_NOINLINE static __device__ __noinline__
+
 namespace rbg {
 
 constexpr double kBig = RBG_BIG;
@@ -21,37 +24,50 @@ constexpr double kPi = 3.14159265358979323846;
 constexpr double kD2R = kPi / 180.0;
 
 RBG_D const double* SP(const DevScene& S, int shape) { return S.params + S.shapes[shape].param_offset; }
+// the shape's trigonometric constants (node_aux.h), or null
+RBG_D const double* ST(const DevScene& S, int shape) {
+  const int o = S.trig_off[shape];
+  return o < 0 ? nullptr : S.trig + o;
+}
 
 // --------------------------------------------------------------------
 // containment
 // --------------------------------------------------------------------
-RBG_D bool phi_in(double x, double y, double phi1, double dphi) {
+// phi in [phi1, phi1 + dphi] from the two phi-plane normals T[0..3]
+// (n1 = (-sin a1, cos a1), n2 = (-sin a2, cos a2)): the point is on the
+// inner side of both planes for dphi <= 180, of either plane above
+RBG_D bool phi_in(double x, double y, const double* T, double dphi) {
   if (dphi >= 360.0) return true;
-  double rel = atan2(y, x) / kD2R - phi1;
-  while (rel < 0) rel += 360.0;
-  while (rel >= 360.0) rel -= 360.0;
-  return rel <= dphi;
+  const double s1 = x * T[0] + y * T[1], s2 = x * T[2] + y * T[3];
+  return dphi <= 180.0 ? (s1 >= 0 && s2 <= 0) : (s1 >= 0 || s2 <= 0);
 }
 
-RBG_D bool pxcon_contains(const double* P, bool pg, d3 p) {
+RBG_D bool pxcon_contains(const double* P, const double* T, bool pg, d3 p) {
   const int head = pg ? 4 : 3;
   const int nz = (int)P[pg ? 3 : 2];
   const double* Z = P + head;
   const double* RMIN = Z + nz;
   const double* RMAX = RMIN + nz;
   if (p.z < Z[0] || p.z > Z[nz - 1]) return false;
-  if (!phi_in(p.x, p.y, P[0], P[1])) return false;
+  if (!phi_in(p.x, p.y, T + RBG_TRIG_PHI, P[1])) return false;
   double rho;
   if (pg) {
-    int ned = (int)P[2];
-    double sector = P[1] / ned;
-    double rel = atan2(p.y, p.x) / kD2R - P[0];
-    while (rel < 0) rel += 360.0;
-    while (rel >= 360.0) rel -= 360.0;
-    int e = (int)floor(rel / sector);
-    if (e >= ned) e = ned - 1;
-    double pe = (P[0] + (e + 0.5) * sector) * kD2R;
-    rho = p.x * cos(pe) + p.y * sin(pe);
+    const int ned = (int)P[2];
+    const double* E = T + RBG_TRIG_PGON_EDGE;
+    if (P[1] >= 360.0) {
+      // the edge whose angular sector holds the point has the largest
+      // projection p . n_e (regular polygon)
+      rho = p.x * E[0] + p.y * E[1];
+      for (int e = 1; e < ned; ++e) rho = fmax(rho, p.x * E[2 * e] + p.y * E[2 * e + 1]);
+    } else {
+      double sector = P[1] / ned;
+      double rel = atan2(p.y, p.x) / kD2R - P[0];
+      while (rel < 0) rel += 360.0;
+      while (rel >= 360.0) rel -= 360.0;
+      int e = (int)floor(rel / sector);
+      if (e >= ned) e = ned - 1;
+      rho = p.x * E[2 * e] + p.y * E[2 * e + 1];
+    }
   } else {
     rho = sqrt(p.x * p.x + p.y * p.y);
   }
@@ -72,7 +88,22 @@ RBG_D bool pxcon_contains(const double* P, bool pg, d3 p) {
   return false;
 }
 
-RBG_D bool prim_contains(int type, const double* P, d3 p) {
+// theta in [th1, th2] (degrees, polar angle from +z) from the cosines
+// c1 = cos th1, c2 = cos th2: th < th1 <=> z > c1 r and th > th2 <=> z < c2 r,
+// compared squared with the signs taken apart
+RBG_D bool theta_in(double z, double r2, double th1, double th2, double c1, double c2) {
+  if (th1 > 0) {
+    const bool below = c1 >= 0 ? (z > 0 && z * z > c1 * c1 * r2) : (z >= 0 || z * z < c1 * c1 * r2);
+    if (below) return false;
+  }
+  if (th2 < 180) {
+    const bool above = c2 <= 0 ? (z < 0 && z * z > c2 * c2 * r2) : (z < 0 || z * z < c2 * c2 * r2);
+    if (above) return false;
+  }
+  return true;
+}
+
+RBG_D bool prim_contains(int type, const double* P, const double* T, d3 p) {
   switch (type) {
     case RBG_SHAPE_BOX:
       return fabs(p.x - P[RBG_BOX_OX]) <= P[RBG_BOX_DX] && fabs(p.y - P[RBG_BOX_OY]) <= P[RBG_BOX_DY] &&
@@ -81,14 +112,14 @@ RBG_D bool prim_contains(int type, const double* P, d3 p) {
       if (fabs(p.z) > P[RBG_TUBE_DZ]) return false;
       double r2 = p.x * p.x + p.y * p.y;
       if (r2 > P[RBG_TUBE_RMAX] * P[RBG_TUBE_RMAX] || r2 < P[RBG_TUBE_RMIN] * P[RBG_TUBE_RMIN]) return false;
-      return phi_in(p.x, p.y, P[RBG_TUBE_PHI1], P[RBG_TUBE_DPHI]);
+      return phi_in(p.x, p.y, T + RBG_TRIG_PHI, P[RBG_TUBE_DPHI]);
     }
     case RBG_SHAPE_SPHERE: {
       double r2 = dot(p, p);
       if (r2 > P[RBG_SPH_RMAX] * P[RBG_SPH_RMAX] || r2 < P[RBG_SPH_RMIN] * P[RBG_SPH_RMIN]) return false;
-      double th = atan2(sqrt(p.x * p.x + p.y * p.y), p.z) / kD2R;
-      if (th < P[RBG_SPH_TH1] || th > P[RBG_SPH_TH2]) return false;
-      return phi_in(p.x, p.y, P[RBG_SPH_PHI1], P[RBG_SPH_DPHI]);
+      if (!theta_in(p.z, r2, P[RBG_SPH_TH1], P[RBG_SPH_TH2], T[RBG_TRIG_SPH_COS], T[RBG_TRIG_SPH_COS + 1]))
+        return false;
+      return phi_in(p.x, p.y, T + RBG_TRIG_PHI, P[RBG_SPH_DPHI]);
     }
     case RBG_SHAPE_PARABOLOID: {
       if (fabs(p.z) > P[RBG_PARA_DZ]) return false;
@@ -96,27 +127,41 @@ RBG_D bool prim_contains(int type, const double* P, d3 p) {
       return P[RBG_PARA_A] > 0 ? f <= p.z : f >= p.z;
     }
     case RBG_SHAPE_PGON:
-      return pxcon_contains(P, true, p);
+      return pxcon_contains(P, T, true, p);
     case RBG_SHAPE_PCON:
-      return pxcon_contains(P, false, p);
+      return pxcon_contains(P, T, false, p);
   }
   return false;
 }
 
-// iterative CSG containment (composite trees are shallow; explicit stack)
-RBG_D bool csg_contains(const DevScene& S, int shape, d3 p) {
+// CSG containment.  A primitive, or a composite of two primitives (the
+// common case: every composite of the telescope scenes), is resolved
+// without recursion from the composite's own operand matrices; deeper trees
+// recurse.  Both are compiled once, out of line.
+RBG_NOINLINE bool csg_contains_deep(const DevScene& S, int shape, d3 p) {
   const rbg_shape_desc sh = S.shapes[shape];
-  if (sh.type != RBG_SHAPE_COMPOSITE) return prim_contains(sh.type, SP(S, shape), p);
-  // depth-2 composites (the common case) are resolved without recursion;
-  // deeper trees recurse through this same function
+  if (sh.type != RBG_SHAPE_COMPOSITE) return prim_contains(sh.type, SP(S, shape), ST(S, shape), p);
   const double* P = SP(S, shape);
-  d3 pl = to_local(P + RBG_COMP_ML, p);
-  bool a = csg_contains(S, sh.left, pl);
+  bool a = csg_contains_deep(S, sh.left, to_local(P + RBG_COMP_ML, p));
   if (sh.op == RBG_OP_INTERSECTION && !a) return false;
   if (sh.op == RBG_OP_SUBTRACTION && !a) return false;
   if (sh.op == RBG_OP_UNION && a) return true;
-  d3 pr = to_local(P + RBG_COMP_MR, p);
-  bool b = csg_contains(S, sh.right, pr);
+  bool b = csg_contains_deep(S, sh.right, to_local(P + RBG_COMP_MR, p));
+  if (sh.op == RBG_OP_SUBTRACTION) return !b;
+  return b;
+}
+
+RBG_NOINLINE bool csg_contains(const DevScene& S, int shape, d3 p) {
+  const rbg_shape_desc& sh = S.shapes[shape];
+  if (sh.type != RBG_SHAPE_COMPOSITE) return prim_contains(sh.type, SP(S, shape), ST(S, shape), p);
+  const int lt = S.shapes[sh.left].type, rt = S.shapes[sh.right].type;
+  if (lt == RBG_SHAPE_COMPOSITE || rt == RBG_SHAPE_COMPOSITE) return csg_contains_deep(S, shape, p);
+  const double* P = SP(S, shape);
+  bool a = prim_contains(lt, SP(S, sh.left), ST(S, sh.left), to_local(P + RBG_COMP_ML, p));
+  if (sh.op == RBG_OP_INTERSECTION && !a) return false;
+  if (sh.op == RBG_OP_SUBTRACTION && !a) return false;
+  if (sh.op == RBG_OP_UNION && a) return true;
+  bool b = prim_contains(rt, SP(S, sh.right), ST(S, sh.right), to_local(P + RBG_COMP_MR, p));
   if (sh.op == RBG_OP_SUBTRACTION) return !b;
   return b;
 }
@@ -155,14 +200,14 @@ RBG_D void add_plane(XList& L, d3 o, d3 d, d3 n, double rhs, uint32_t code) {
 //  PCON k<nz z-plane k; nz + k*2+w cone face; 0x3ffe/0x3fff phi
 constexpr uint32_t kPhi1 = 0x3ffe, kPhi2 = 0x3fff;
 
-RBG_D void add_phi(XList& L, d3 o, d3 d, double phi1, double dphi, uint32_t leaf) {
+// the two phi planes from their normals T[0..3]
+RBG_D void add_phi(XList& L, d3 o, d3 d, const double* T, double dphi, uint32_t leaf) {
   if (dphi >= 360.0) return;
-  double a1 = phi1 * kD2R, a2 = (phi1 + dphi) * kD2R;
-  add_plane(L, o, d, mk(-sin(a1), cos(a1), 0), 0.0, leaf | kPhi1);
-  add_plane(L, o, d, mk(-sin(a2), cos(a2), 0), 0.0, leaf | kPhi2);
+  add_plane(L, o, d, mk(T[0], T[1], 0), 0.0, leaf | kPhi1);
+  add_plane(L, o, d, mk(T[2], T[3], 0), 0.0, leaf | kPhi2);
 }
 
-RBG_D void prim_collect(int type, const double* P, d3 o, d3 d, uint32_t leaf, XList& L) {
+RBG_D void prim_collect(int type, const double* P, const double* T, d3 o, d3 d, uint32_t leaf, XList& L) {
   double r[2];
   switch (type) {
     case RBG_SHAPE_BOX: {
@@ -187,7 +232,7 @@ RBG_D void prim_collect(int type, const double* P, d3 o, d3 d, uint32_t leaf, XL
         k = quad_roots(A, B, C0 - P[RBG_TUBE_RMIN] * P[RBG_TUBE_RMIN], r);
         for (int i = 0; i < k; ++i) xl_add(L, r[i], leaf | 3u);
       }
-      add_phi(L, o, d, P[RBG_TUBE_PHI1], P[RBG_TUBE_DPHI], leaf);
+      add_phi(L, o, d, T + RBG_TRIG_PHI, P[RBG_TUBE_DPHI], leaf);
       break;
     }
     case RBG_SHAPE_SPHERE: {
@@ -201,8 +246,7 @@ RBG_D void prim_collect(int type, const double* P, d3 o, d3 d, uint32_t leaf, XL
       for (int w = 0; w < 2; ++w) {
         double th = w == 0 ? P[RBG_SPH_TH1] : P[RBG_SPH_TH2];
         if ((w == 0 && th <= 0) || (w == 1 && th >= 180)) continue;
-        double c2 = cos(th * kD2R);
-        c2 *= c2;
+        const double c2 = T[RBG_TRIG_SPH_COS2 + w];
         double s2 = 1 - c2;
         double Ac = d.z * d.z * s2 - c2 * (d.x * d.x + d.y * d.y);
         double Bc = 2 * (o.z * d.z * s2 - c2 * (o.x * d.x + o.y * d.y));
@@ -210,7 +254,7 @@ RBG_D void prim_collect(int type, const double* P, d3 o, d3 d, uint32_t leaf, XL
         k = quad_roots(Ac, Bc, Cc, r);
         for (int i = 0; i < k; ++i) xl_add(L, r[i], leaf | (uint32_t)(2 + w));
       }
-      add_phi(L, o, d, P[RBG_SPH_PHI1], P[RBG_SPH_DPHI], leaf);
+      add_phi(L, o, d, T + RBG_TRIG_PHI, P[RBG_SPH_DPHI], leaf);
       break;
     }
     case RBG_SHAPE_PARABOLOID: {
@@ -233,7 +277,7 @@ RBG_D void prim_collect(int type, const double* P, d3 o, d3 d, uint32_t leaf, XL
       const double* RMAX = RMIN + nz;
       if (d.z != 0)
         for (int k = 0; k < nz; ++k) xl_add(L, (Z[k] - o.z) / d.z, leaf | (uint32_t)k);
-      const double sector = P[1] / ned;
+      const double* E = T + RBG_TRIG_PGON_EDGE;
       for (int k = 0; k < nz - 1; ++k) {
         double h = Z[k + 1] - Z[k];
         if (h <= 0) continue;
@@ -241,14 +285,12 @@ RBG_D void prim_collect(int type, const double* P, d3 o, d3 d, uint32_t leaf, XL
           const double* R = w ? RMIN : RMAX;
           if (w && R[k] == 0 && R[k + 1] == 0) continue;
           double s = (R[k + 1] - R[k]) / h;
-          for (int e = 0; e < ned; ++e) {
-            double pe = (P[0] + (e + 0.5) * sector) * kD2R;
-            add_plane(L, o, d, mk(cos(pe), sin(pe), -s), R[k] - s * Z[k],
+          for (int e = 0; e < ned; ++e)
+            add_plane(L, o, d, mk(E[2 * e], E[2 * e + 1], -s), R[k] - s * Z[k],
                       leaf | (uint32_t)(nz + (k * 2 + w) * ned + e));
-          }
         }
       }
-      add_phi(L, o, d, P[0], P[1], leaf);
+      add_phi(L, o, d, T + RBG_TRIG_PHI, P[1], leaf);
       break;
     }
     case RBG_SHAPE_PCON: {
@@ -273,19 +315,17 @@ RBG_D void prim_collect(int type, const double* P, d3 o, d3 d, uint32_t leaf, XL
           for (int i = 0; i < m; ++i) xl_add(L, r[i], leaf | (uint32_t)(nz + k * 2 + w));
         }
       }
-      add_phi(L, o, d, P[0], P[1], leaf);
+      add_phi(L, o, d, T + RBG_TRIG_PHI, P[1], leaf);
       break;
     }
   }
 }
 
 // local normal of a primitive surface at point p (leaf frame)
-RBG_D d3 prim_normal(int type, const double* P, uint32_t surf, d3 p) {
+RBG_D d3 prim_normal(int type, const double* P, const double* T, uint32_t surf, d3 p) {
   if (surf == kPhi1 || surf == kPhi2) {
-    double phi1 = type == RBG_SHAPE_TUBE ? P[RBG_TUBE_PHI1] : type == RBG_SHAPE_SPHERE ? P[RBG_SPH_PHI1] : P[0];
-    double dphi = type == RBG_SHAPE_TUBE ? P[RBG_TUBE_DPHI] : type == RBG_SHAPE_SPHERE ? P[RBG_SPH_DPHI] : P[1];
-    double a = (surf == kPhi1 ? phi1 : phi1 + dphi) * kD2R;
-    return mk(-sin(a), cos(a), 0);
+    const double* n = T + RBG_TRIG_PHI + (surf == kPhi1 ? 0 : 2);
+    return mk(n[0], n[1], 0);
   }
   switch (type) {
     case RBG_SHAPE_BOX: {
@@ -298,9 +338,7 @@ RBG_D d3 prim_normal(int type, const double* P, uint32_t surf, d3 p) {
     case RBG_SHAPE_SPHERE:
       if (surf < 2) return p;
       {
-        double th = surf == 2 ? P[RBG_SPH_TH1] : P[RBG_SPH_TH2];
-        double c2 = cos(th * kD2R);
-        c2 *= c2;
+        const double c2 = T[RBG_TRIG_SPH_COS2 + (surf == 2 ? 0 : 1)];
         return mk(-c2 * p.x, -c2 * p.y, (1 - c2) * p.z);
       }
     case RBG_SHAPE_PARABOLOID:
@@ -314,8 +352,8 @@ RBG_D d3 prim_normal(int type, const double* P, uint32_t surf, d3 p) {
       const double* Z = P + 4;
       const double* R = (w ? Z + nz : Z + 2 * nz);
       double s = (R[k + 1] - R[k]) / (Z[k + 1] - Z[k]);
-      double pe = (P[0] + (e + 0.5) * (P[1] / ned)) * kD2R;
-      return mk(cos(pe), sin(pe), -s);
+      const double* E = T + RBG_TRIG_PGON_EDGE;
+      return mk(E[2 * e], E[2 * e + 1], -s);
     }
     case RBG_SHAPE_PCON: {
       const int nz = (int)P[2];
@@ -332,27 +370,28 @@ RBG_D d3 prim_normal(int type, const double* P, uint32_t surf, d3 p) {
   return mk(0, 0, 1);
 }
 
-// Collect crossings of a (possibly composite) shape.  Leaves are numbered
-// in depth-first order; M maps the shape's frame to the query frame.
-// Recursion depth is bounded by the composite depth checked at build.
-RBG_D void csg_collect(const DevScene& S, int shape, const double* M, d3 o, d3 d, uint32_t& leaf, XList& L) {
+// Collect crossings of a composite tree deeper than two primitives.  Leaves
+// are numbered in depth-first order; M maps the shape's frame to the query
+// frame.  Recursion depth is bounded by the composite depth checked at build.
+RBG_NOINLINE void csg_collect_deep(const DevScene& S, int shape, const double* M, d3 o, d3 d, uint32_t& leaf,
+                                   XList& L) {
   const rbg_shape_desc sh = S.shapes[shape];
   if (sh.type != RBG_SHAPE_COMPOSITE) {
     d3 ol = to_local(M, o), dl = dir_to_local(M, d);
-    prim_collect(sh.type, SP(S, shape), ol, dl, leaf << 16, L);
+    prim_collect(sh.type, SP(S, shape), ST(S, shape), ol, dl, leaf << 16, L);
     ++leaf;
     return;
   }
   const double* P = SP(S, shape);
   M12 ML = mat_mul(M, P + RBG_COMP_ML);
-  csg_collect(S, sh.left, ML.v, o, d, leaf, L);
+  csg_collect_deep(S, sh.left, ML.v, o, d, leaf, L);
   M12 MR = mat_mul(M, P + RBG_COMP_MR);
-  csg_collect(S, sh.right, MR.v, o, d, leaf, L);
+  csg_collect_deep(S, sh.right, MR.v, o, d, leaf, L);
 }
 
 // find leaf #target (depth-first) and its matrix
-RBG_D bool csg_find_leaf(const DevScene& S, int shape, const double* M, uint32_t target, uint32_t& leaf,
-                         int& leaf_shape, M12& leafM) {
+RBG_NOINLINE bool csg_find_leaf(const DevScene& S, int shape, const double* M, uint32_t target, uint32_t& leaf,
+                                int& leaf_shape, M12& leafM) {
   const rbg_shape_desc sh = S.shapes[shape];
   if (sh.type != RBG_SHAPE_COMPOSITE) {
     if (leaf == target) {
@@ -373,14 +412,32 @@ RBG_D bool csg_find_leaf(const DevScene& S, int shape, const double* M, uint32_t
 
 // Distance to enter (exit = false) or leave (exit = true) a TGeo primitive or
 // composite; on success code/normal describe the crossed surface (normal in
-// the shape frame, not oriented).
-RBG_D double csg_dist(const DevScene& S, int shape, d3 o, d3 d, bool exit, d3& nrm, unsigned& err) {
+// the shape frame, not oriented).  Every ray/surface root is collected with
+// its surface code, the roots are sorted, and each segment between two is
+// classified by containment of its midpoint.  Primitives and two-primitive
+// composites take their operand matrices straight from the parameters.
+RBG_NOINLINE double csg_dist(const DevScene& S, int shape, d3 o, d3 d, bool exit, d3& nrm, unsigned& err) {
   XList L;
   L.n = 0;
   L.overflow = false;
-  uint32_t leaf = 0;
-  M12 I = mat_identity();
-  csg_collect(S, shape, I.v, o, d, leaf, L);
+  const rbg_shape_desc& sh = S.shapes[shape];
+  const double* P = SP(S, shape);
+  // 0: primitive, 1: composite of two primitives, 2: deeper composite
+  int form = 0;
+  if (sh.type == RBG_SHAPE_COMPOSITE)
+    form = (S.shapes[sh.left].type == RBG_SHAPE_COMPOSITE || S.shapes[sh.right].type == RBG_SHAPE_COMPOSITE) ? 2 : 1;
+  if (form == 0) {
+    prim_collect(sh.type, P, ST(S, shape), o, d, 0u, L);
+  } else if (form == 1) {
+    prim_collect(S.shapes[sh.left].type, SP(S, sh.left), ST(S, sh.left), to_local(P + RBG_COMP_ML, o),
+                 dir_to_local(P + RBG_COMP_ML, d), 0u << 16, L);
+    prim_collect(S.shapes[sh.right].type, SP(S, sh.right), ST(S, sh.right), to_local(P + RBG_COMP_MR, o),
+                 dir_to_local(P + RBG_COMP_MR, d), 1u << 16, L);
+  } else {
+    uint32_t leaf = 0;
+    M12 I = mat_identity();
+    csg_collect_deep(S, shape, I.v, o, d, leaf, L);
+  }
   if (L.overflow) {
     err |= ERR_BIT_CAP;
     return kBig;
@@ -415,13 +472,21 @@ RBG_D double csg_dist(const DevScene& S, int shape, d3 o, d3 d, bool exit, d3& n
     if ((!exit && !in_prev && in_next) || (exit && in_prev && !in_next)) {
       double t = L.t[j];
       uint32_t target = L.code[j] >> 16, surf = L.code[j] & 0xffffu;
-      uint32_t cnt = 0;
-      int ls = shape;
-      M12 LM = mat_identity();
-      csg_find_leaf(S, shape, I.v, target, cnt, ls, LM);
-      d3 pl = to_local(LM.v, o + t * d);
-      d3 nl = prim_normal(S.shapes[ls].type, SP(S, ls), surf, pl);
-      nrm = dir_to_master(LM.v, normalized(nl));
+      const d3 q = o + t * d;
+      if (form == 0) {
+        nrm = normalized(prim_normal(sh.type, P, ST(S, shape), surf, q));
+      } else if (form == 1) {
+        const double* M = P + (target == 0 ? RBG_COMP_ML : RBG_COMP_MR);
+        const int ls = target == 0 ? sh.left : sh.right;
+        nrm = dir_to_master(M, normalized(prim_normal(S.shapes[ls].type, SP(S, ls), ST(S, ls), surf, to_local(M, q))));
+      } else {
+        uint32_t cnt = 0;
+        int ls = shape;
+        M12 I = mat_identity(), LM = mat_identity();
+        csg_find_leaf(S, shape, I.v, target, cnt, ls, LM);
+        nrm = dir_to_master(LM.v, normalized(prim_normal(S.shapes[ls].type, SP(S, ls), ST(S, ls), surf,
+                                                         to_local(LM.v, q))));
+      }
       return t;
     }
     in_prev = in_next;
@@ -655,11 +720,11 @@ RBG_D double asph_dist4(const Asph& a, d3 p, d3 d) {
 // TGeoTube::DistFromOutsideS test of DistFromOutside, :393-395)
 RBG_D bool tube_reached(d3 o, d3 d, double rmin, double rmax, double dz) {
   double P[RBG_TUBE_NP] = {rmin, rmax, dz, 0, 360};
-  if (prim_contains(RBG_SHAPE_TUBE, P, o)) return true;
+  if (prim_contains(RBG_SHAPE_TUBE, P, nullptr, o)) return true;
   XList L;
   L.n = 0;
   L.overflow = false;
-  prim_collect(RBG_SHAPE_TUBE, P, o, d, 0u, L);
+  prim_collect(RBG_SHAPE_TUBE, P, nullptr, o, d, 0u, L);
   for (int i = 1; i < L.n; ++i) {
     double t = L.t[i];
     int j = i - 1;
@@ -672,7 +737,7 @@ RBG_D bool tube_reached(d3 o, d3 d, double rmin, double rmax, double dz) {
   for (int j = 0; j + 1 < L.n; ++j) {
     if (L.t[j + 1] <= 0) continue;
     double tm = 0.5 * (L.t[j] + L.t[j + 1]);
-    if (prim_contains(RBG_SHAPE_TUBE, P, o + tm * d)) return true;
+    if (prim_contains(RBG_SHAPE_TUBE, P, nullptr, o + tm * d)) return true;
   }
   return false;
 }
@@ -721,11 +786,16 @@ RBG_D d3 asph_normal(const Asph& a, d3 point, d3 dir) {
 // --------------------------------------------------------------------
 // AGeoWinstonConePoly
 // --------------------------------------------------------------------
+// The face angles 2 pi k / n, the cone angle theta and pi / n enter only
+// through constants precomputed per shape (T): face normals (cos, sin),
+// cos theta, sin theta and tan(pi / n).  Angular tests become sign tests.
 struct Win {
   double r1, r2, theta, f, dz;
   int n;
+  double ct, st, tan_half;  // cos theta, sin theta, tan(pi / n)
+  const double* face;       // (cos 2 pi k / n, sin 2 pi k / n) per face k
 };
-RBG_D Win win_load(const double* P) {
+RBG_D Win win_load(const double* P, const double* T) {
   Win w;
   w.r1 = P[RBG_WIN_R1];
   w.r2 = P[RBG_WIN_R2];
@@ -733,12 +803,16 @@ RBG_D Win win_load(const double* P) {
   w.theta = P[RBG_WIN_THETA];
   w.f = P[RBG_WIN_F];
   w.dz = P[RBG_WIN_DZ];
+  w.ct = T[RBG_TRIG_WIN_COS];
+  w.st = T[RBG_TRIG_WIN_SIN];
+  w.tan_half = T[RBG_TRIG_WIN_TANHALF];
+  w.face = T + RBG_TRIG_WIN_FACE;
   return w;
 }
 // CalcR (AGeoWinstonCone2D.cxx:82-98)
 RBG_D bool win_R(const Win& w, double z, double& r) {
   if (fabs(z) > w.dz + 1e-10) return false;
-  double sint = sin(w.theta), cost = cos(w.theta);
+  const double sint = w.st, cost = w.ct;
   double t = z + w.dz;
   double a0 = t * t * sint * sint - 4. * w.f * (t * cost + w.f);
   double a1 = 2. * t * sint * cost + 4. * w.f * sint;
@@ -748,7 +822,7 @@ RBG_D bool win_R(const Win& w, double z, double& r) {
 }
 // CalcdRdZ (:59-79)
 RBG_D double win_dRdZ(const Win& w, double z) {
-  double sint = sin(w.theta), cost = cos(w.theta);
+  const double sint = w.st, cost = w.ct;
   double t = z + w.dz;
   double a0 = t * t * sint * sint - 4. * w.f * (t * cost + w.f);
   double a1 = 2. * t * sint * cost + 4. * w.f * sint;
@@ -757,22 +831,39 @@ RBG_D double win_dRdZ(const Win& w, double z) {
   double da1dt = 2 * sint * cost;
   return (-da1dt + (a1 * da1dt - 2 * da0dt * a2) / sqrt(a1 * a1 - 4 * a0 * a2)) / (2 * a2);
 }
+// Projection of (x, y) on the normal of the face whose sector holds it:
+// the reference reduces atan2(y, x) into [-pi/n, pi/n] and takes
+// sqrt(x^2 + y^2) cos(reduced angle), which is max_k (x, y) . n_k for the n
+// face normals of a regular polygon.  `k` receives the face.
+RBG_D double win_face_proj(const Win& w, double x, double y, int& k) {
+  double best = x * w.face[0] + y * w.face[1];
+  k = 0;
+  for (int i = 1; i < w.n; ++i) {
+    const double v = x * w.face[2 * i] + y * w.face[2 * i + 1];
+    if (v > best) {
+      best = v;
+      k = i;
+    }
+  }
+  return best;
+}
 // InsidePolygon (ConePoly.cxx:293-309)
 RBG_D bool win_inside_polygon(const Win& w, double x, double y, double r) {
-  double th = atan2(y, x);
-  while (th > kPi / w.n) th -= 2 * kPi / w.n;
-  while (th < -kPi / w.n) th += 2 * kPi / w.n;
-  return !(sqrt(x * x + y * y) * cos(th) > r);
+  int k;
+  return !(win_face_proj(w, x, y, k) > r);
 }
-RBG_D bool win_contains(const Win& w, d3 p) {
+RBG_NOINLINE bool win_contains(const Win& w, d3 p) {
   if (fabs(p.z) > w.dz) return false;
   double r;
   if (!win_R(w, p.z, r)) return false;
   return win_inside_polygon(w, p.x, p.y, r);
 }
-// DistToParabola (Cone2D.cxx:325-428)
-RBG_D double win_dist_parabola(const Win& w, d3 point, d3 dir, double phi, double open) {
-  double cp = cos(phi), sp = sin(phi);
+// DistToParabola (Cone2D.cxx:325-428) for face k.  tan(alpha - theta) with
+// alpha = atan2(pz, px) is (pz cos theta - px sin theta) / (px cos theta +
+// pz sin theta); the angular window |atan2(yc, xc)| <= open / 2 is xc >= 0
+// for open = pi and xc > 0, |yc| <= xc tan(pi / n) for open = 2 pi / n.
+RBG_D double win_dist_parabola(const Win& w, d3 point, d3 dir, int k, bool half_space) {
+  const double cp = w.face[2 * k], sp = w.face[2 * k + 1];
   double x = cp * point.x + sp * point.y;
   double y = -sp * point.x + cp * point.y;
   double z = point.z;
@@ -780,11 +871,12 @@ RBG_D double win_dist_parabola(const Win& w, d3 point, d3 dir, double phi, doubl
   double py = -sp * dir.x + cp * dir.y;
   double pz = dir.z;
   if (px == 0 && pz == 0) return kBig;
-  double cost = cos(w.theta), sint = sin(w.theta);
+  const double cost = w.ct, sint = w.st;
   double X = cost * (x + w.r2) + (z + w.dz) * sint;
   double Z = -sint * (x + w.r2) + (z + w.dz) * cost + w.f;
-  double alpha = atan2(pz, px);
-  double tanA = tan(alpha - w.theta);
+  const double den = px * cost + pz * sint;
+  if (den == 0) return kBig;
+  double tanA = (pz * cost - px * sint) / den;
   double tmp = tanA * tanA - (X * tanA - Z) / w.f;
   if (tmp < 0) return kBig;
   double Xp, Xm;
@@ -808,23 +900,27 @@ RBG_D double win_dist_parabola(const Win& w, d3 point, d3 dir, double phi, doubl
     else yc = y + (fabs(px) < 1e-5 ? (zc - z) * py / pz : (xc - x) * py / px);
     double dx = xc - x, dy = yc - y, dz = zc - z;
     double v;
-    if (xc < w.r2 || w.r1 < xc || zc < -w.dz || w.dz < zc || dx * px + dz * pz < 0) v = kBig;
-    else v = fabs(atan2(yc, xc)) <= open / 2. ? sqrt(dx * dx + dy * dy + dz * dz) : kBig;
+    if (xc < w.r2 || w.r1 < xc || zc < -w.dz || w.dz < zc || dx * px + dz * pz < 0) {
+      v = kBig;
+    } else {
+      const bool in_window = half_space ? xc >= 0 : (xc > 0 && fabs(yc) <= xc * w.tan_half);
+      v = in_window ? sqrt(dx * dx + dy * dy + dz * dz) : kBig;
+    }
     if (v < best) best = v;
   }
   return best;
 }
-RBG_D double win_dist_in(const Win& w, d3 p, d3 d) {
+RBG_NOINLINE double win_dist_in(const Win& w, d3 p, d3 d) {
   double best = kBig;
   if (d.z < 0) best = (-p.z - w.dz) / d.z;
   else if (d.z > 0) best = (w.dz - p.z) / d.z;
   for (int i = 0; i < w.n; i++) {
-    double v = win_dist_parabola(w, p, d, i * 2 * kPi / w.n, kPi);
+    double v = win_dist_parabola(w, p, d, i, true);
     if (v < best) best = v;
   }
   return best;
 }
-RBG_D double win_dist_out(const Win& w, d3 p, d3 d) {
+RBG_NOINLINE double win_dist_out(const Win& w, d3 p, d3 d) {
   if (p.z <= -w.dz) {
     if (d.z <= 0) return kBig;
     double s = -(w.dz + p.z) / d.z;
@@ -836,29 +932,22 @@ RBG_D double win_dist_out(const Win& w, d3 p, d3 d) {
   }
   double best = kBig;
   for (int i = 0; i < w.n; i++) {
-    double v = win_dist_parabola(w, p, d, i * 2 * kPi / w.n, 2 * kPi / w.n);
+    double v = win_dist_parabola(w, p, d, i, false);
     if (v < best) best = v;
   }
   return best;
 }
-// ComputeNormal (ConePoly.cxx:67-122)
-RBG_D d3 win_normal(const Win& w, d3 point, d3 dir) {
+// ComputeNormal (ConePoly.cxx:67-122): the face of the point's sector
+RBG_NOINLINE d3 win_normal(const Win& w, d3 point, d3 dir) {
   double x = point.x, y = point.y, z = point.z;
   double saf0 = fabs(fabs(w.dz) - fabs(z)), saf1;
-  double phi = atan2(y, x);
-  while (phi > kPi / w.n) phi -= 2 * kPi / w.n;
-  while (phi < -kPi / w.n) phi += 2 * kPi / w.n;
+  int k;
+  const double proj = win_face_proj(w, x, y, k);
   double R;
-  saf1 = win_R(w, z, R) ? fabs(R - sqrt(x * x + y * y) * cos(phi)) : kBig;
+  saf1 = win_R(w, z, R) ? fabs(R - proj) : kBig;
   d3 n;
-  if (saf0 <= saf1) {
-    n = mk(0, 0, 1);
-  } else {
-    phi = atan2(y, x);
-    if (phi < -kPi / w.n) phi += 2 * kPi;
-    int k = (int)floor((phi + kPi / w.n) / (2 * kPi / w.n));
-    n = mk(cos(k * 2 * kPi / w.n), sin(k * 2 * kPi / w.n), -win_dRdZ(w, z));
-  }
+  if (saf0 <= saf1) n = mk(0, 0, 1);
+  else n = mk(w.face[2 * k], w.face[2 * k + 1], -win_dRdZ(w, z));
   n = normalized(n);
   if (dot(n, dir) < 0) n = neg(n);
   return n;
@@ -921,18 +1010,22 @@ RBG_D double box_dist_fast(const double* P, d3 p, d3 d, bool exit, d3& nrm) {
   return tnear;
 }
 
-// shape queries of the FP64 path (the mixed path has its own, below)
+// shape queries of the FP64 path (the mixed path has its own, below).  In
+// kernels with optional features the dispatch is compiled once, out of line
+// (shape_contains / shape_dist below): every inlined copy of it multiplies
+// the code the instruction cache must hold and the time ptxas takes.
 template <unsigned F = kFeatAll>
-RBG_D bool shape_contains(const DevScene& S, int shape, d3 p) {
+RBG_D bool shape_contains_body(const DevScene& S, int shape, d3 p) {
   const int type = S.shapes[shape].type;
   if (type == RBG_SHAPE_ASPHERIC_DISK) return asph_contains(Asph{SP(S, shape)}, p);
-  if (type == RBG_SHAPE_WINSTON_POLY) return (F & kFeatWinston) ? win_contains(win_load(SP(S, shape)), p) : false;
-  if (!(F & kFeatCSG) && type == RBG_SHAPE_BOX) return prim_contains(RBG_SHAPE_BOX, SP(S, shape), p);
+  if (type == RBG_SHAPE_WINSTON_POLY)
+    return (F & kFeatWinston) ? win_contains(win_load(SP(S, shape), ST(S, shape)), p) : false;
+  if (!(F & kFeatCSG) && type == RBG_SHAPE_BOX) return prim_contains(RBG_SHAPE_BOX, SP(S, shape), nullptr, p);
   return (F & kFeatCSG) ? csg_contains(S, shape, p) : false;
 }
 
 template <unsigned F = kFeatAll>
-RBG_D double shape_dist(const DevScene& S, int shape, d3 p, d3 d, bool exit, d3& nrm, unsigned& err) {
+RBG_D double shape_dist_body(const DevScene& S, int shape, d3 p, d3 d, bool exit, d3& nrm, unsigned& err) {
   const int type = S.shapes[shape].type;
   if (type == RBG_SHAPE_ASPHERIC_DISK) {
     Asph a{SP(S, shape)};
@@ -940,10 +1033,27 @@ RBG_D double shape_dist(const DevScene& S, int shape, d3 p, d3 d, bool exit, d3&
   }
   if (type == RBG_SHAPE_WINSTON_POLY) {
     if (!(F & kFeatWinston)) return kBig;
-    Win w = win_load(SP(S, shape));
+    Win w = win_load(SP(S, shape), ST(S, shape));
     return exit ? win_dist_in(w, p, d) : win_dist_out(w, p, d);
   }
   return (F & kFeatCSG) ? csg_dist(S, shape, p, d, exit, nrm, err) : kBig;
+}
+
+template <unsigned F>
+RBG_NOINLINE bool shape_contains_call(const DevScene& S, int shape, d3 p) {
+  return shape_contains_body<F>(S, shape, p);
+}
+template <unsigned F>
+RBG_NOINLINE double shape_dist_call(const DevScene& S, int shape, d3 p, d3 d, bool exit, d3& nrm, unsigned& err) {
+  return shape_dist_body<F>(S, shape, p, d, exit, nrm, err);
+}
+template <unsigned F = kFeatAll>
+RBG_D bool shape_contains(const DevScene& S, int shape, d3 p) {
+  return F == 0 ? shape_contains_body<F>(S, shape, p) : shape_contains_call<F>(S, shape, p);
+}
+template <unsigned F = kFeatAll>
+RBG_D double shape_dist(const DevScene& S, int shape, d3 p, d3 d, bool exit, d3& nrm, unsigned& err) {
+  return F == 0 ? shape_dist_body<F>(S, shape, p, d, exit, nrm, err) : shape_dist_call<F>(S, shape, p, d, exit, nrm, err);
 }
 
 RBG_D bool is_ageo(int type) { return type == RBG_SHAPE_ASPHERIC_DISK || type == RBG_SHAPE_WINSTON_POLY; }
@@ -959,7 +1069,6 @@ RBG_D bool is_ageo(int type) { return type == RBG_SHAPE_ASPHERIC_DISK || type ==
 // ray's float position and direction are converted once per step and
 // passed along with the FP64 ones.
 // ====================================================================
-#define RBG_NOINLINE static __device__ __noinline__
 
 struct f3 {
   float x, y, z;
@@ -1304,7 +1413,7 @@ RBG_D bool box_contains_f(const double* P, const float* Pf, const LRay& L) {
   const float ez = 1e-6f * (fabsf(L.pf.z) + fabsf(Pf[RBG_BOX_OZ]) + Pf[RBG_BOX_DZ]) + 1e-30f;
   if (ax > Pf[RBG_BOX_DX] + ex || ay > Pf[RBG_BOX_DY] + ey || az > Pf[RBG_BOX_DZ] + ez) return false;
   if (ax < Pf[RBG_BOX_DX] - ex && ay < Pf[RBG_BOX_DY] - ey && az < Pf[RBG_BOX_DZ] - ez) return true;
-  return prim_contains(RBG_SHAPE_BOX, P, L.p);
+  return prim_contains(RBG_SHAPE_BOX, P, nullptr, L.p);
 }
 
 // Lower and upper bounds of TGeoBBox::DistFromInside (the slab exit

@@ -99,7 +99,8 @@ extern "C" int rbg_trace_noalloc(rbg_scene* s, const rbg_rays* in, rbg_result* o
                       table_bytes(s->bvh_items) + table_bytes(s->shapes) + table_bytes(s->volumes) +
                       table_bytes(s->tables) + table_bytes(s->indices) + table_bytes(s->layers) +
                       table_bytes(s->multilayers) + table_bytes(s->borders) + table_bytes(s->params) +
-                      table_bytes(s->node_aux) + table_bytes(s->fparams);
+                      table_bytes(s->node_aux) + table_bytes(s->fparams) + table_bytes(s->trig) +
+                      table_bytes(s->trig_off);
   if (need > RBG_NOALLOC_SCRATCH_BYTES) return RBG_ERR_TOO_LARGE;
   unsigned char* base = nullptr;
   int rc = scratch_address(&base);
@@ -116,7 +117,8 @@ extern "C" int rbg_trace_noalloc(rbg_scene* s, const rbg_rays* in, rbg_result* o
       (rc = place(s->layers, base, &off, st, &v.layers)) ||
       (rc = place(s->multilayers, base, &off, st, &v.multilayers)) ||
       (rc = place(s->borders, base, &off, st, &v.borders)) || (rc = place(s->params, base, &off, st, &v.params)) ||
-      (rc = place(s->node_aux, base, &off, st, &v.aux)) || (rc = place(s->fparams, base, &off, st, &v.fparams)))
+      (rc = place(s->node_aux, base, &off, st, &v.aux)) || (rc = place(s->fparams, base, &off, st, &v.fparams)) ||
+      (rc = place(s->trig, base, &off, st, &v.trig)) || (rc = place(s->trig_off, base, &off, st, &v.trig_off)))
     return rc;
   v.n_nodes = (int32_t)s->nodes.size();
   v.n_borders = (int32_t)s->borders.size();

@@ -26,8 +26,30 @@ struct rbg_node_aux {
 };
 static_assert(sizeof(rbg_node_aux) == 32, "rbg_node_aux layout");
 
+// Per-shape trigonometric constants (rbg_scene::trig at trig_off[shape]),
+// so that no shape query evaluates sin/cos/tan/atan2 of a fixed angle:
+//   TUBE, PCON : [0..3] phi-plane normals (-sin a1, cos a1, -sin a2, cos a2),
+//                a1 = phi1, a2 = phi1 + dphi
+//   SPHERE     : [0..3] phi-plane normals, [4] cos th1, [5] cos th2,
+//                [6] cos^2 th1, [7] cos^2 th2
+//   PGON       : [0..3] phi-plane normals, then per edge e (cos pe, sin pe)
+//                with pe = phi1 + (e + 1/2) dphi / nedges
+//   WINSTON    : [0] cos theta, [1] sin theta, [2] tan(pi / n), then per face
+//                k (cos 2 pi k / n, sin 2 pi k / n)
+enum : int32_t {
+  RBG_TRIG_PHI = 0,
+  RBG_TRIG_SPH_COS = 4,
+  RBG_TRIG_SPH_COS2 = 6,
+  RBG_TRIG_PGON_EDGE = 4,
+  RBG_TRIG_WIN_COS = 0,
+  RBG_TRIG_WIN_SIN = 1,
+  RBG_TRIG_WIN_TANHALF = 2,
+  RBG_TRIG_WIN_FACE = 3
+};
+
 struct rbg_scene;
 namespace rbg {
-// fills s->node_aux and s->fparams from the flattened tables (scene.cpp)
+// fills s->node_aux, s->fparams, s->trig and s->trig_off from the
+// flattened tables (scene.cpp)
 void build_node_aux(rbg_scene* s);
 }  // namespace rbg

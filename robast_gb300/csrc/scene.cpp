@@ -615,6 +615,55 @@ float round_to_float(double v, bool up) {
 }  // namespace
 
 void rbg::build_node_aux(rbg_scene* s) {
+  const double d2r = M_PI / 180.0;
+  s->trig.clear();
+  s->trig_off.assign(s->shapes.size(), -1);
+  for (size_t i = 0; i < s->shapes.size(); ++i) {
+    const rbg_shape_desc& sh = s->shapes[i];
+    const double* P = s->params.data() + sh.param_offset;
+    auto phi_planes = [&](double phi1, double dphi) {
+      const double a1 = phi1 * d2r, a2 = (phi1 + dphi) * d2r;
+      s->trig.insert(s->trig.end(), {-std::sin(a1), std::cos(a1), -std::sin(a2), std::cos(a2)});
+    };
+    const int32_t off = (int32_t)s->trig.size();
+    switch (sh.type) {
+      case RBG_SHAPE_TUBE:
+        phi_planes(P[RBG_TUBE_PHI1], P[RBG_TUBE_DPHI]);
+        break;
+      case RBG_SHAPE_PCON:
+        phi_planes(P[RBG_PCON_PHI1], P[RBG_PCON_DPHI]);
+        break;
+      case RBG_SHAPE_SPHERE: {
+        phi_planes(P[RBG_SPH_PHI1], P[RBG_SPH_DPHI]);
+        const double c1 = std::cos(P[RBG_SPH_TH1] * d2r), c2 = std::cos(P[RBG_SPH_TH2] * d2r);
+        s->trig.insert(s->trig.end(), {c1, c2, c1 * c1, c2 * c2});
+        break;
+      }
+      case RBG_SHAPE_PGON: {
+        phi_planes(P[RBG_PGON_PHI1], P[RBG_PGON_DPHI]);
+        const int ned = (int)P[RBG_PGON_NEDGES];
+        const double sector = P[RBG_PGON_DPHI] / ned;
+        for (int e = 0; e < ned; ++e) {
+          const double pe = (P[RBG_PGON_PHI1] + (e + 0.5) * sector) * d2r;
+          s->trig.insert(s->trig.end(), {std::cos(pe), std::sin(pe)});
+        }
+        break;
+      }
+      case RBG_SHAPE_WINSTON_POLY: {
+        const int n = (int)P[RBG_WIN_N];
+        const double th = P[RBG_WIN_THETA];
+        s->trig.insert(s->trig.end(), {std::cos(th), std::sin(th), std::tan(M_PI / n)});
+        for (int k = 0; k < n; ++k) {
+          const double a = k * 2 * M_PI / n;
+          s->trig.insert(s->trig.end(), {std::cos(a), std::sin(a)});
+        }
+        break;
+      }
+      default:
+        break;
+    }
+    if ((int32_t)s->trig.size() > off) s->trig_off[i] = off;
+  }
   s->fparams.resize(s->params.size());
   for (size_t i = 0; i < s->params.size(); ++i) s->fparams[i] = (float)s->params[i];
   s->node_aux.assign(s->nodes.size(), rbg_node_aux{});

@@ -31,6 +31,9 @@ struct rbg_scene {
   // device-only tables of the mixed-precision tracer (node_aux.h)
   std::vector<rbg_node_aux> node_aux;
   std::vector<float> fparams;
+  // per-shape trigonometric constants (node_aux.h), offsets per shape or -1
+  std::vector<double> trig;
+  std::vector<int32_t> trig_off;
 
   // device mirror, owned by the CUDA side (capi.cu)
   rbg_device_scene* dev = nullptr;

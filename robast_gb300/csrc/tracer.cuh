@@ -133,14 +133,25 @@ RBG_D bool in_fbox3(const float* lo, const float* hi, f3 p) {
 }
 
 template <unsigned F>
-RBG_D bool shape_contains_f(const DevScene& S, int shape, const LRay& L, bool twin) {
+RBG_D bool shape_contains_f_body(const DevScene& S, int shape, const LRay& L, bool twin) {
   const rbg_shape_desc& sh = S.shapes[shape];
   const double* P = S.params + sh.param_offset;
   const float* Pf = S.fparams + sh.param_offset;
   if (sh.type == RBG_SHAPE_ASPHERIC_DISK) return asph_contains_f(P, Pf, L, twin);
   if (sh.type == RBG_SHAPE_BOX) return box_contains_f(P, Pf, L);
-  if (sh.type == RBG_SHAPE_WINSTON_POLY) return (F & kFeatWinston) ? win_contains(win_load(P), L.p) : false;
+  if (sh.type == RBG_SHAPE_WINSTON_POLY)
+    return (F & kFeatWinston) ? win_contains(win_load(P, ST(S, shape)), L.p) : false;
   return (F & kFeatCSG) ? csg_contains(S, shape, L.p) : false;
+}
+
+// out of line except in the lean (F = 0) instance, as shape_contains
+template <unsigned F>
+RBG_NOINLINE bool shape_contains_f_call(const DevScene& S, int shape, LRay L, bool twin) {
+  return shape_contains_f_body<F>(S, shape, L, twin);
+}
+template <unsigned F>
+RBG_D bool shape_contains_f(const DevScene& S, int shape, const LRay& L, bool twin) {
+  return F == 0 ? shape_contains_f_body<F>(S, shape, L, twin) : shape_contains_f_call<F>(S, shape, L, twin);
 }
 
 // node k contains p: float box (rounded outward, so it never rejects a
@@ -215,7 +226,8 @@ RBG_D int locate_from_top_f(const DevScene& S, d3 p) {
 
 // shape distance of node k in the mixed path; `face` receives the aspheric face
 template <unsigned F>
-RBG_D double shape_dist_f(const DevScene& S, int k, const LRay& L, bool exit, d3& nrm, int& face, unsigned& err) {
+RBG_D double shape_dist_f_body(const DevScene& S, int k, const LRay& L, bool exit, d3& nrm, int& face,
+                               unsigned& err) {
   const int shape = S.nodes[k].shape;
   const rbg_shape_desc& sh = S.shapes[shape];
   const double* P = S.params + sh.param_offset;
@@ -227,11 +239,22 @@ RBG_D double shape_dist_f(const DevScene& S, int k, const LRay& L, bool exit, d3
   }
   if (sh.type == RBG_SHAPE_WINSTON_POLY) {
     if (!(F & kFeatWinston)) return kBig;
-    Win w = win_load(P);
+    Win w = win_load(P, ST(S, shape));
     return exit ? win_dist_in(w, L.p, L.d) : win_dist_out(w, L.p, L.d);
   }
   if (sh.type == RBG_SHAPE_BOX) return box_dist_fast(P, L.p, L.d, exit, nrm);
   return (F & kFeatCSG) ? csg_dist(S, shape, L.p, L.d, exit, nrm, err) : kBig;
+}
+
+template <unsigned F>
+RBG_NOINLINE double shape_dist_f_call(const DevScene& S, int k, LRay L, bool exit, d3& nrm, int& face,
+                                      unsigned& err) {
+  return shape_dist_f_body<F>(S, k, L, exit, nrm, face, err);
+}
+template <unsigned F>
+RBG_D double shape_dist_f(const DevScene& S, int k, const LRay& L, bool exit, d3& nrm, int& face, unsigned& err) {
+  return F == 0 ? shape_dist_f_body<F>(S, k, L, exit, nrm, face, err)
+                : shape_dist_f_call<F>(S, k, L, exit, nrm, face, err);
 }
 
 // candidate daughter test shared by the scan and the BVH walk
@@ -461,7 +484,7 @@ RBG_D d3 find_normal(const DevScene& S, const Nav& nv) {
     d3 pl = to_local(N.m, nv.p), dl = dir_to_local(N.m, nv.d);
     nl = asph_normal(a, pl, dl);
   } else if (type == RBG_SHAPE_WINSTON_POLY) {
-    nl = win_normal(win_load(SP(S, N.shape)), to_local(N.m, nv.p), dir_to_local(N.m, nv.d));
+    nl = win_normal(win_load(SP(S, N.shape), ST(S, N.shape)), to_local(N.m, nv.p), dir_to_local(N.m, nv.d));
   } else {
     nl = nv.xn;
   }
