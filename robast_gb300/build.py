@@ -24,7 +24,8 @@ ORACLE = os.path.join(ROOT, "oracle")
 ORACLE_BUILD = os.path.join(ORACLE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["trace_fp64.cu", "trace_mixed_all.cu", "capi.cu", "trace_mixed.cu", "adjoint.cu", "noalloc.cu"]
+CU_SOURCES = ["trace_fp64.cu", "trace_mixed_all.cu", "trace_mixed_facets.cu", "trace_mixed_coated.cu",
+              "trace_mixed_cones.cu", "trace_mixed_csg.cu", "capi.cu", "trace_mixed.cu", "adjoint.cu", "noalloc.cu"]
 CPP_SOURCES = ["scene.cpp", "shoot.cpp"]
 
 
@@ -76,7 +77,7 @@ def build_library(verbose: bool = False, force: bool = False) -> str:
         cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c", os.path.join(CSRC, f), "-o", obj, *common]
         jobs.append((obj, cmd))
     logs = []
-    with cf.ThreadPoolExecutor(max_workers=max(2, min(8, os.cpu_count() or 2))) as ex:
+    with cf.ThreadPoolExecutor(max_workers=max(2, min(16, os.cpu_count() or 2))) as ex:
         for log in ex.map(lambda j: _run(j[1]), jobs):
             logs.append(log)
     tmp = out + ".tmp"

@@ -1,20 +1,50 @@
-// trace_mixed.cu -- launcher of the mixed-precision tracer: scenes made of
+// trace_mixed.cu -- launcher of the mixed-precision tracer.  A scene runs
+// the smallest compiled instance whose feature set covers its own
+// (rbg_scene::features): the lean instance compiled here for scenes of
 // boxes and aspheric disks with mirrors, obscurations and focal surfaces
-// only (two-mirror telescopes) run the lean instance compiled here; any
-// other scene runs the all-features instance (trace_mixed_all.cu).
+// only (two-mirror telescopes), an instance per common scene class, and
+// the all-features instance (trace_mixed_all.cu) for anything else.
 #include "trace_mixed.cuh"
 
 namespace rbg {
 
-int launch_mixed_all(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n,
-                     const rbg_trace_opts& o, cudaStream_t st, unsigned* err_flags, unsigned long long* counter);
+#define RBG_MIXED_LAUNCHER(name)                                                                              \
+  int name(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o, \
+           cudaStream_t st, unsigned* err_flags, unsigned long long* counter);
+RBG_MIXED_LAUNCHER(launch_mixed_csg)
+RBG_MIXED_LAUNCHER(launch_mixed_facets)
+RBG_MIXED_LAUNCHER(launch_mixed_cones)
+RBG_MIXED_LAUNCHER(launch_mixed_coated)
+RBG_MIXED_LAUNCHER(launch_mixed_all)
+#undef RBG_MIXED_LAUNCHER
+
+namespace {
+typedef int (*MixedLauncher)(const DevScene&, const KernelRays&, const KernelOut&, int64_t, const rbg_trace_opts&,
+                             cudaStream_t, unsigned*, unsigned long long*);
+struct Instance {
+  unsigned features;
+  MixedLauncher launch;
+};
+// in order of growing feature sets; the last covers every scene
+const Instance kInstances[] = {
+    {0u, launch_mixed_impl<0u>},
+    {kFeatCSG, launch_mixed_csg},
+    {kFeatCSG | kFeatRough | kFeatBVH, launch_mixed_facets},
+    {kFeatWinston | kFeatLens | kFeatBVH, launch_mixed_cones},
+    {kFeatCSG | kFeatLens | kFeatMultilayer | kFeatBVH, launch_mixed_coated},
+    {kFeatAll, launch_mixed_all},
+};
+}  // namespace
 
 int launch_mixed(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o,
                  cudaStream_t st, unsigned* err_flags, unsigned long long* counter, int* launches) {
-  const int rc = S.features == 0 ? launch_mixed_impl<0u>(S, in, out, n, o, st, err_flags, counter)
-                                 : launch_mixed_all(S, in, out, n, o, st, err_flags, counter);
-  if (rc == RBG_OK) *launches = 1;
-  return rc;
+  for (const Instance& inst : kInstances) {
+    if (S.features & ~inst.features) continue;
+    const int rc = inst.launch(S, in, out, n, o, st, err_flags, counter);
+    if (rc == RBG_OK) *launches = 1;
+    return rc;
+  }
+  return RBG_ERR_UNSUPPORTED;
 }
 
 }  // namespace rbg
