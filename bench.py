@@ -96,7 +96,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -258,7 +258,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
@@ -267,6 +267,7 @@ def main():
     ap.add_argument("--workload", default="schwarzschild_couder", choices=sorted(WORKLOADS))
     ap.add_argument("--rays", type=int, default=0, help="rays per step (default: the workload's size)")
     ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE)
+    ap.add_argument("--compaction", type=int, default=0, help="mixed tracer refill threshold (0: tuned)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -289,6 +290,7 @@ def main():
     man, batch = build_workload(args.workload, n_req)
     n = len(batch["x"])
     man.ray_id_offset = rank * n
+    man.compaction = args.compaction
     rays = device.to_device(batch, f"cuda:{local}")
     res = device.alloc_result(n, f"cuda:{local}")
     stream = torch.cuda.current_stream()
@@ -340,6 +342,11 @@ def main():
             t = float(tt.item())
         return t, nl, ck.summary()
 
+    # autotune the mixed tracer's compaction threshold on this batch (outside
+    # the timed region, like the warm-up) unless one was given
+    tuned = None
+    if prec == N.PREC_MIXED and args.compaction == 0:
+        tuned = device.autotune(man, rays, res)
     ms, launches, clocks = timed(prec, res)
     seg = int((res["npoints"].to(torch.int64) - 1).sum().item())
     value = n * ws / (ms / 1e3)
@@ -414,6 +421,7 @@ def main():
             "vs_baseline": None, "dtype": "f64" if prec == N.PREC_FP64 else "f32+f64", "data": "synthetic",
             "config": workload_config(args.workload, n, args.precision), "gpu_launches": launches * args.steps,
             "segments_per_step": seg,
+            "compaction": args.compaction or tuned,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": None, "peak_source": how,
                          "note": "algorithmic ray-state bytes; the kernel is FP64-pipe bound, see profiles/"},

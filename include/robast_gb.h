@@ -281,6 +281,13 @@ typedef struct {
   uint64_t ray_id_offset; /* ray id of element 0 (for sharded/batched calls) */
   int32_t precision;      /* RBG_PREC_* */
   int32_t block_size;     /* 0: library default */
+  /* mixed tracer: a warp refills its idle lanes with consecutive rays once
+   * at least this many (1..32) are idle; 1 keeps every lane busy, 32 keeps
+   * a warp's rays together (coherent paths).  0: the scene's tuned value
+   * (rbg_scene_autotune), else the library default.  Results do not depend
+   * on it. */
+  int32_t compaction;
+  int32_t reserved;       /* 0 */
 } rbg_trace_opts;
 
 /* ---- entry points ------------------------------------------------------ */
@@ -303,6 +310,15 @@ int rbg_scene_upload(rbg_scene* scene);
  * default).  The per-ray fates, points and directions land in `out`. */
 int rbg_trace(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
               const rbg_trace_opts* opts, void* stream);
+
+/* Autotuner of the mixed tracer (no counterpart in the reference, whose
+ * thread split is fixed by the caller, src/AOpticsManager.cxx:529-567):
+ * traces the DEVICE rays `in` with each candidate compaction threshold,
+ * keeps the fastest in the scene for later calls that leave
+ * opts->compaction at 0, and returns it in *chosen.  `out` receives the
+ * trace results (identical for every threshold).  Synchronises `stream`. */
+int rbg_scene_autotune(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
+                       const rbg_trace_opts* opts, void* stream, int32_t* chosen);
 
 /* Same, with HOST buffers: copies the rays in, traces, copies the results
  * out and synchronises (the call a ROOT-side AOpticsManager binding makes,

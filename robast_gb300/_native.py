@@ -137,7 +137,7 @@ class Result(C.Structure):
 class TraceOpts(C.Structure):
     _fields_ = [("limit", C.c_int32), ("disable_fresnel", C.c_int32), ("seed", C.c_uint64),
                 ("ray_id_offset", C.c_uint64), ("precision", C.c_int32),
-                ("block_size", C.c_int32)]
+                ("block_size", C.c_int32), ("compaction", C.c_int32), ("reserved", C.c_int32)]
 
 
 class NativeError(RuntimeError):
@@ -178,6 +178,8 @@ def _declare(L):
     L.rbg_scene_upload.argtypes = [vp]
     L.rbg_trace.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts), vp]
     L.rbg_trace_host.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts)]
+    L.rbg_scene_autotune.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts), vp,
+                                     C.POINTER(C.c_int32)]
     L.rbg_last_launch_count.argtypes = [vp]
     L.rbg_focal_moments.argtypes = [C.c_int64, vp, vp, vp, vp, vp, C.c_int32, vp, vp]
     L.rbg_focal_histogram.argtypes = [C.c_int64, vp, vp, vp, C.c_int32, C.c_double, C.c_double,

@@ -168,7 +168,9 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
                out->dx, out->dy, out->dz, out->hist_cap, out->hist_xyzt, out->hist_node};
   if (opts->precision == RBG_PREC_MIXED) {
     int launches = 0;
-    rc = launch_mixed(s->dev->view, kr, ko, in->n, *opts, st, s->dev->err_flags, s->dev->counter, &launches);
+    rbg_trace_opts o = *opts;
+    if (o.compaction == 0) o.compaction = s->tuned_compaction;
+    rc = launch_mixed(s->dev->view, kr, ko, in->n, o, st, s->dev->err_flags, s->dev->counter, &launches);
     if (rc) return rc;
     s->last_launches = launches;
   } else {
@@ -182,6 +184,57 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
   if (bits & ERR_BIT_NAN) return RBG_ERR_NAN;
   if (bits & ERR_BIT_CAP) return RBG_ERR_CAP;
   return RBG_OK;
+}
+
+// The autotuner of the mixed tracer's compaction threshold: trace the
+// caller's rays once to warm up, then once per candidate threshold, timed
+// with events on the stream, and keep the fastest in the scene (used by
+// every later call whose options leave the threshold at 0).  The results
+// in `out` are those of any single trace: they do not depend on the
+// threshold.
+extern "C" int rbg_scene_autotune(rbg_scene* s, const rbg_rays* in, rbg_result* out, const rbg_trace_opts* opts,
+                                  void* stream, int32_t* chosen) {
+  if (!s || !in || !out || !opts) return RBG_ERR_ARG;
+  static const int32_t kCandidates[] = {1, 8, 16, 32};
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  rbg_trace_opts o = *opts;
+  o.precision = RBG_PREC_MIXED;
+  o.compaction = 32;
+  int rc = rbg_trace(s, in, out, &o, stream);
+  if (rc != RBG_OK && rc != RBG_ERR_NAN && rc != RBG_ERR_CAP) return rc;
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return RBG_ERR_CUDA;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return RBG_ERR_CUDA;
+  }
+  float best_ms = 0.f;
+  int32_t best = 32;
+  for (int32_t c : kCandidates) {
+    o.compaction = c;
+    float ms = 0.f;
+    if (cudaEventRecord(e0, st) != cudaSuccess) {
+      rc = RBG_ERR_CUDA;
+      break;
+    }
+    rc = rbg_trace(s, in, out, &o, stream);
+    if (rc != RBG_OK && rc != RBG_ERR_NAN && rc != RBG_ERR_CAP) break;
+    if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      rc = RBG_ERR_CUDA;
+      break;
+    }
+    if (c == kCandidates[0] || ms < best_ms) {
+      best_ms = ms;
+      best = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != RBG_OK && rc != RBG_ERR_NAN && rc != RBG_ERR_CAP) return rc;
+  s->tuned_compaction = best;
+  if (chosen) *chosen = best;
+  return rc;
 }
 
 namespace rbg {
@@ -304,6 +357,7 @@ extern "C" int rbg_trace_host(rbg_scene* s, const rbg_rays* in, rbg_result* out,
                  dst[5] ? sl.out[5] : nullptr, dst[6] ? sl.out[6] : nullptr, hcap, sl.hist, sl.hist_node};
     rbg_trace_opts o = *opts;
     o.ray_id_offset = opts->ray_id_offset + (uint64_t)off;
+    if (o.compaction == 0) o.compaction = s->tuned_compaction;
     int nl = 0;
     if ((rc = launch_trace(s, kr, ko, m, o, st, sl.err, sl.counter, &nl))) return rc;
     launches += nl;

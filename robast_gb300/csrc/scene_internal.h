@@ -39,6 +39,7 @@ struct rbg_scene {
   rbg_device_scene* dev = nullptr;
   int dev_id = -1;
   int last_launches = 0;
+  int tuned_compaction = 0;  // rbg_scene_autotune's choice, 0: none yet
   void* workspace = nullptr;
   size_t workspace_bytes = 0;
 };

@@ -20,6 +20,9 @@
 namespace rbg {
 
 constexpr int kMixedBlock = 128;
+// compaction threshold when neither the options nor the scene's tuning
+// give one
+constexpr int kDefaultCompaction = 32;
 
 // Instances: F = kFeatAll runs any scene; F = 0 (boxes and aspheric disks,
 // mirrors, obscurations and focal surfaces only, e.g. two-mirror
@@ -28,7 +31,7 @@ template <unsigned F>
 __global__ void __launch_bounds__(kMixedBlock) trace_mixed_kernel(DevScene S, KernelRays in, KernelOut out,
                                                                   int64_t n, int limit, int disable_fresnel,
                                                                   uint64_t seed, uint64_t id_offset,
-                                                                  unsigned* err_flags,
+                                                                  int refill_min, unsigned* err_flags,
                                                                   unsigned long long* next_ray) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -42,7 +45,9 @@ __global__ void __launch_bounds__(kMixedBlock) trace_mixed_kernel(DevScene S, Ke
   r.status = RBG_STOP;
   for (;;) {
     unsigned need = __ballot_sync(FULL, !active);
-    if (need && !drained) {
+    // refill once enough lanes are idle (compaction threshold): fewer,
+    // larger refills keep a warp's rays consecutive and their paths alike
+    if (need && !drained && (need == FULL || __popc(need) >= refill_min)) {
       const int leader = __ffs(need) - 1;
       unsigned long long base = 0;
       if (lane == leader) base = atomicAdd(next_ray, (unsigned long long)__popc(need));
@@ -99,8 +104,9 @@ int launch_mixed_impl(const DevScene& S, const KernelRays& in, const KernelOut& 
   int64_t grid = (int64_t)sms * bps;
   if (want < grid) grid = want;
   if (cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st) != cudaSuccess) return RBG_ERR_CUDA;
+  const int refill = o.compaction < 1 ? kDefaultCompaction : (o.compaction > 32 ? 32 : o.compaction);
   trace_mixed_kernel<F><<<(int)grid, kMixedBlock, 0, st>>>(S, in, out, n, o.limit, o.disable_fresnel, o.seed,
-                                                          o.ray_id_offset, err_flags, counter);
+                                                          o.ray_id_offset, refill, err_flags, counter);
   if (cudaGetLastError() != cudaSuccess) return RBG_ERR_CUDA;
   return RBG_OK;
 }

@@ -98,6 +98,24 @@ def trace(manager, rays, res=None, precision: Optional[int] = None, stream=None,
     return res, status
 
 
+def autotune(manager, rays, res=None, stream=None) -> int:
+    """Pick the mixed tracer's compaction threshold for this scene from a
+    timed trace of `rays` per candidate (rbg_scene_autotune); later traces
+    of the scene use it.  Returns the chosen threshold."""
+    torch = _torch()
+    scene = manager._ensure_scene()
+    if res is None:
+        res = alloc_result(rays["x"].numel(), rays["x"].device)
+    opts = manager.trace_options(N.PREC_MIXED)
+    st_ptr = (stream if stream is not None else torch.cuda.current_stream()).cuda_stream
+    chosen = C.c_int32(0)
+    status = N.lib().rbg_scene_autotune(scene.handle, C.byref(_rays_struct(rays)), C.byref(_result_struct(res)),
+                                        C.byref(opts), C.c_void_p(st_ptr), C.byref(chosen))
+    if status not in (N.RBG_OK, N.RBG_ERR_CAP, N.RBG_ERR_NAN):
+        N.check(status, "rbg_scene_autotune")
+    return int(chosen.value)
+
+
 def focal_moments(res, group=None, n_groups: int = 1, stream=None):
     """(count, sum x, sum y, sum x^2, sum y^2, sum t) of focused rays per group."""
     torch = _torch()

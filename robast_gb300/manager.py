@@ -463,6 +463,7 @@ class AOpticsManager:
         self.seed = 0x5EED5EED
         self.precision = N.PREC_FP64
         self.ray_id_offset = 0
+        self.compaction = 0  # mixed tracer refill threshold, 0: the scene's tuned value
 
     # units (include/AOpticsManager.h:59-71)
     @staticmethod
@@ -566,6 +567,7 @@ class AOpticsManager:
         o.seed = self.seed
         o.ray_id_offset = self.ray_id_offset
         o.precision = self.precision if precision is None else precision
+        o.compaction = int(self.compaction)
         return o
 
     def _ensure_scene(self) -> Scene:

@@ -156,3 +156,40 @@ def test_host_pipeline_matches_device_trace(prec):
         valid = np.arange(hist)[None, :] < np.minimum(ref["npoints"], hist)[:, None]
         np.testing.assert_array_equal(got["hist_node"][valid], ref["hist_node"][valid])
         np.testing.assert_array_equal(got["hist_xyzt"][valid], ref["hist_xyzt"][valid])
+
+
+@pytest.mark.parametrize("name", ["schwarzschild_couder", "davies_cotton", "light_guide"])
+def test_compaction_threshold_does_not_change_results(name):
+    """The mixed tracer's refill threshold only changes which lanes carry
+    which rays; every ray's result depends on (seed, ray id) alone."""
+    kw = {"light_guide": dict(n_rays=6000, n_variants=2)}.get(name, dict(n_rays=6000))
+    man, batch = configs.CONFIGS[name](**kw)
+    results = []
+    for c in (1, 7, 32):
+        man.compaction = c
+        st, got = _trace(man, batch, N.PREC_MIXED)
+        assert st == N.RBG_OK
+        results.append(got)
+    for got in results[1:]:
+        _same(got, results[0])
+
+
+def test_autotune_picks_a_candidate_and_keeps_results():
+    import torch
+
+    from robast_gb300 import device
+
+    man, batch = configs.schwarzschild_couder(n_rays=20000, seed=9)
+    st, ref = _trace(man, batch, N.PREC_MIXED)
+    assert st == N.RBG_OK
+    rays = device.to_device(batch, "cuda:0")
+    res = device.alloc_result(len(batch["x"]), "cuda:0")
+    chosen = device.autotune(man, rays, res)
+    torch.cuda.synchronize()
+    assert chosen in (1, 8, 16, 32)
+    assert man.scene is not None
+    tuned = {k: res[k].cpu().numpy() for k in FIELDS}
+    _same(tuned, ref)
+    st, after = _trace(man, batch, N.PREC_MIXED)
+    assert st == N.RBG_OK
+    _same(after, ref)
