@@ -290,6 +290,20 @@ typedef struct {
   int32_t reserved;       /* 0 */
 } rbg_trace_opts;
 
+/* ---- CORSIKA IACT photon bunches (ACorsikaIACTFile) ------------------- */
+/* One photon bunch per element (struct bunch of CORSIKA's IACT option, as
+ * ACorsikaIACTFile::ReadEvent stores it, src/ACorsikaIACTFile.cxx:443-455):
+ * arrival position relative to the telescope (cm), emission height (cm),
+ * arrival time (ns), direction cosines (cz = -sqrt(1 - cx^2 - cy^2)),
+ * wavelength (nm, 0 = not set by CORSIKA) and photon count (fractional). */
+typedef struct {
+  int64_t n;
+  int32_t *tel, *array;
+  float *x, *y, *zem, *time, *cx, *cy, *cz, *lambda, *photons;
+} rbg_bunches;
+
+typedef struct rbg_corsika rbg_corsika;
+
 /* ---- entry points ------------------------------------------------------ */
 int rbg_abi_version(void);
 const char* rbg_status_string(int status);
@@ -310,6 +324,53 @@ int rbg_scene_upload(rbg_scene* scene);
  * default).  The per-ray fates, points and directions land in `out`. */
 int rbg_trace(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
               const rbg_trace_opts* opts, void* stream);
+
+/* ACorsikaIACTFile::Open (src/ACorsikaIACTFile.cxx:191-257) on an
+ * in-memory, decompressed eventio stream (the caller inflates .gz files):
+ * reads the run header, the input card and the telescope positions.
+ * RBG_ERR_ARG for a stream that is not a CORSIKA IACT file. */
+int rbg_corsika_open(const uint8_t* data, int64_t nbytes, rbg_corsika** out);
+void rbg_corsika_close(rbg_corsika* file);
+/* The 273 words of the run header (ACorsikaIACTRunHeader, word 0 holds
+ * the int32 tag) / of the current event's header (ACorsikaIACTEventHeader). */
+int rbg_corsika_run_header(const rbg_corsika* file, float* out273);
+int rbg_corsika_event_header(const rbg_corsika* file, float* out273);
+/* The input card as newline-separated text (ACorsikaIACTFile::PrintInputCard);
+ * returns the buffer size it needs. */
+int rbg_corsika_input_lines(const rbg_corsika* file, char* buf, int64_t cap, int32_t* n_lines);
+/* Telescope positions and radii, cm (GetTelescopeX/Y/Z/R). */
+int rbg_corsika_telescopes(const rbg_corsika* file, int32_t cap, int32_t* n_tel, double* x, double* y,
+                           double* z, double* r);
+/* ACorsikaIACTFile::ReadEvent (:264-489): read forward to event `num`
+ * (numbers start at 1); *event = num, or -1 when it is not found ahead.
+ * RBG_ERR_ARG for a malformed block. */
+int rbg_corsika_read_event(rbg_corsika* file, int32_t num, int32_t* event);
+/* Array offsets of the current event (SetMultipleUseHeader). */
+int rbg_corsika_offsets(const rbg_corsika* file, int32_t cap, int32_t* n_arrays, double* time_offset,
+                        double* x, double* y);
+/* Bunches of telescope `tel`, array `array` (< 0: any) of the current event
+ * (the reference's TTree "tree"): count, and copy into host arrays of
+ * capacity out->n (out->n becomes the count written). */
+int64_t rbg_corsika_bunch_count(const rbg_corsika* file, int32_t tel, int32_t array);
+int rbg_corsika_get_bunches(const rbg_corsika* file, int32_t tel, int32_t array, rbg_bunches* out);
+
+/* ACorsikaIACTFile::GetRayArray (src/ACorsikaIACTFile.cxx:71-133) on the
+ * GPU: every bunch in DEVICE arrays `b` becomes ceil(photons) rays (the
+ * reference's `for (j = 0; j < photons; j++)`), started at height z (cm)
+ * after back-projection along the bunch direction over
+ * (z - tel_z) / |cz| (x, y and time; light speed c / refractive_index).
+ * A bunch wavelength of 0 is drawn with 1/lambda uniform in
+ * [1/lambda_max, 1/lambda_min] (nm) from Philox keyed by (seed, ray index);
+ * the reference meant this law but passes its bunch-count limit as the
+ * upper wavelength (:125).  Rays go to DEVICE arrays `out` of capacity
+ * `capacity` (out->n is set); *n_rays receives the count.  With out == NULL
+ * or too small a capacity only *n_rays is set (RBG_ERR_TOO_LARGE for the
+ * latter).  `workspace` is a DEVICE buffer of rbg_bunches_workspace_bytes(n)
+ * bytes; nothing is allocated.  Synchronises `stream`. */
+size_t rbg_bunches_workspace_bytes(int64_t n_bunches);
+int rbg_bunches_to_rays(const rbg_bunches* b, double z, double tel_z, double refractive_index,
+                        double lambda_min, double lambda_max, uint64_t seed, void* workspace,
+                        rbg_rays* out, int64_t capacity, int64_t* n_rays, void* stream);
 
 /* Autotuner of the mixed tracer (no counterpart in the reference, whose
  * thread split is fixed by the caller, src/AOpticsManager.cxx:529-567):

@@ -1799,3 +1799,44 @@ void orc_containment_radius(const double* counts, int nx, double xlo, double xhi
   *px = x;
   *py = y;
 }
+
+/* ======================================================================
+ * ACorsikaIACTFile::GetRayArray (src/ACorsikaIACTFile.cxx:71-133) for
+ * bunches in HOST arrays: ceil(photons) rays per bunch, back-projected to
+ * height z over (z - tel_z) / |cz|; a zero wavelength is drawn with
+ * 1/lambda uniform in [1/lambda_max, 1/lambda_min] from Philox counter
+ * (0, 2, ray index) -- the law the reference meant at :122-125, where it
+ * passes its bunch-count limit as the upper wavelength.  Writes at most
+ * `capacity` rays and returns their total count.
+ * ==================================================================== */
+int64_t orc_bunches_to_rays(const rbg_bunches* b, double z, double tel_z, double refractive_index,
+                            double lambda_min, double lambda_max, uint64_t seed, double* x, double* y,
+                            double* zz, double* t, double* dx, double* dy, double* dz, double* lam,
+                            int64_t capacity) {
+  const double speed = 2.99792458e10 / refractive_index;
+  int64_t r = 0;
+  for (int64_t i = 0; i < b->n; ++i) {
+    const double cz = b->cz[i];
+    const double airmass = -1. / cz;
+    const double tel_dist = (z - tel_z) * airmass;
+    for (int64_t j = 0; j < b->photons[i]; ++j, ++r) {
+      double l = b->lambda[i];
+      if (r >= capacity) continue;
+      if (l == 0) {
+        uint32_t c[4] = {0u, 2u, (uint32_t)r, (uint32_t)((uint64_t)r >> 32)};
+        uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)}, v[4];
+        orc_philox(c, k, v);
+        l = 1. / (1. / lambda_min - u53(v[0], v[1]) * (1. / lambda_min - 1. / lambda_max));
+      }
+      x[r] = (double)b->x[i] - tel_dist * b->cx[i];
+      y[r] = (double)b->y[i] - tel_dist * b->cy[i];
+      zz[r] = z;
+      t[r] = (double)b->time[i] * 1e-9 - tel_dist / speed;
+      dx[r] = b->cx[i];
+      dy[r] = b->cy[i];
+      dz[r] = cz;
+      lam[r] = l * 1e-7;
+    }
+  }
+  return r;
+}

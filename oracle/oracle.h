@@ -61,6 +61,13 @@ void orc_containment_radius(const double* counts, int nx, double xlo, double xhi
                             int ny, double ylo, double yhi, double fraction,
                             double* r, double* x, double* y);
 
+/* ACorsikaIACTFile::GetRayArray on host bunch arrays (see oracle.c);
+ * returns the number of rays (at most `capacity` are written). */
+int64_t orc_bunches_to_rays(const rbg_bunches* b, double z, double tel_z, double refractive_index,
+                            double lambda_min, double lambda_max, uint64_t seed, double* x, double* y,
+                            double* zz, double* t, double* dx, double* dy, double* dz, double* lam,
+                            int64_t capacity);
+
 /* Shape queries in a node's local frame (for unit tests of the shapes). */
 double orc_shape_dist_out(const rbg_flat_scene* scene, int shape, const double* p,
                           const double* d);

@@ -134,6 +134,11 @@ class Result(C.Structure):
                 ("hist_xyzt", _dp), ("hist_node", C.POINTER(C.c_int32))]
 
 
+class Bunches(C.Structure):
+    _fields_ = [("n", C.c_int64), ("tel", C.POINTER(C.c_int32)), ("array", C.POINTER(C.c_int32))] + \
+        [(f, C.POINTER(C.c_float)) for f in ("x", "y", "zem", "time", "cx", "cy", "cz", "lambda_", "photons")]
+
+
 class TraceOpts(C.Structure):
     _fields_ = [("limit", C.c_int32), ("disable_fresnel", C.c_int32), ("seed", C.c_uint64),
                 ("ray_id_offset", C.c_uint64), ("precision", C.c_int32),
@@ -188,6 +193,25 @@ def _declare(L):
                                          C.c_double, C.c_double, C.c_double, _dp, _dp, _dp, vp]
     L.rbg_shoot.argtypes = [C.c_int32, _dp, C.c_int64, _dp, _dp, _dp, C.c_uint64, C.c_uint64,
                             C.c_double, C.POINTER(Rays)]
+    fp = C.POINTER(C.c_float)
+    ip = C.POINTER(C.c_int32)
+    L.rbg_corsika_open.argtypes = [C.c_char_p, C.c_int64, C.POINTER(vp)]
+    L.rbg_corsika_close.argtypes = [vp]
+    L.rbg_corsika_close.restype = None
+    L.rbg_corsika_run_header.argtypes = [vp, fp]
+    L.rbg_corsika_event_header.argtypes = [vp, fp]
+    L.rbg_corsika_input_lines.argtypes = [vp, C.c_char_p, C.c_int64, ip]
+    L.rbg_corsika_telescopes.argtypes = [vp, C.c_int32, ip, _dp, _dp, _dp, _dp]
+    L.rbg_corsika_read_event.argtypes = [vp, C.c_int32, ip]
+    L.rbg_corsika_offsets.argtypes = [vp, C.c_int32, ip, _dp, _dp, _dp]
+    L.rbg_corsika_bunch_count.argtypes = [vp, C.c_int32, C.c_int32]
+    L.rbg_corsika_bunch_count.restype = C.c_int64
+    L.rbg_corsika_get_bunches.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(Bunches)]
+    L.rbg_bunches_workspace_bytes.argtypes = [C.c_int64]
+    L.rbg_bunches_workspace_bytes.restype = C.c_size_t
+    L.rbg_bunches_to_rays.argtypes = [C.POINTER(Bunches), C.c_double, C.c_double, C.c_double, C.c_double,
+                                      C.c_double, C.c_uint64, vp, C.POINTER(Rays), C.c_int64,
+                                      C.POINTER(C.c_int64), vp]
 
 
 def check(status: int, what: str):

@@ -45,6 +45,9 @@ def lib():
             getattr(L, f).argtypes = [fs, C.c_int, dp, dp]
             getattr(L, f).restype = C.c_double
         L.orc_shape_contains.argtypes = [fs, C.c_int, dp]
+        L.orc_bunches_to_rays.argtypes = [C.POINTER(N.Bunches), C.c_double, C.c_double, C.c_double, C.c_double,
+                                          C.c_double, C.c_uint64] + [dp] * 8 + [C.c_int64]
+        L.orc_bunches_to_rays.restype = C.c_int64
         _lib = L
     return _lib
 
@@ -88,3 +91,23 @@ def containment_radius(counts: np.ndarray, xlo, xhi, ylo, yhi, fraction):
     lib().orc_containment_radius(counts.ctypes.data_as(C.POINTER(C.c_double)), nx, xlo, xhi, ny, ylo, yhi,
                                  fraction, C.byref(r), C.byref(x), C.byref(y))
     return r.value, x.value, y.value
+
+
+def bunches_to_rays(b, z, tel_z, n_index, lam_min, lam_max, seed):
+    """ACorsikaIACTFile::GetRayArray restated (oracle) on host bunch arrays
+    (dict of float32 arrays as ACorsikaIACTFile.GetBunches returns)."""
+    fields = ("x", "y", "zem", "time", "cx", "cy", "cz", "lambda", "photons")
+    nb = len(b["x"])
+    bs = N.Bunches()
+    bs.n = nb
+    fp = C.POINTER(C.c_float)
+    arrs = {f: np.ascontiguousarray(b[f], dtype=np.float32) for f in fields}
+    for f in fields:
+        setattr(bs, "lambda_" if f == "lambda" else f, arrs[f].ctypes.data_as(fp))
+    cap = int(np.sum(np.ceil(np.maximum(arrs["photons"], 0)))) + 1
+    out = {f: np.zeros(cap) for f in ("x", "y", "z", "t", "dx", "dy", "dz", "lam")}
+    dp = C.POINTER(C.c_double)
+    n = lib().orc_bunches_to_rays(C.byref(bs), z, tel_z, n_index, lam_min, lam_max, seed,
+                                  *(out[f].ctypes.data_as(dp) for f in ("x", "y", "z", "t", "dx", "dy", "dz", "lam")),
+                                  cap)
+    return {k: v[:n] for k, v in out.items()}
