@@ -6,6 +6,10 @@
 set -e
 REF=${1:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+if [ ! -d "$REF/src/bernlohr" ]; then
+  echo "reference tree not present: oracle/_ref not built"
+  exit 0
+fi
 OUT="$HERE/_ref"
 mkdir -p "$OUT"
 gcc -O1 -w -I "$REF/include/bernlohr" -o "$OUT/corsika_dump" "$HERE/corsika_dump.c" \
