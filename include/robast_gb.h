@@ -75,7 +75,8 @@ enum {
   RBG_SHAPE_PCON = 6,           /* TGeoPcon / TGeoCone(Seg)     */
   RBG_SHAPE_ASPHERIC_DISK = 7,  /* AGeoAsphericDisk             */
   RBG_SHAPE_WINSTON_POLY = 8,   /* AGeoWinstonConePoly          */
-  RBG_SHAPE_COMPOSITE = 9       /* TGeoCompositeShape node      */
+  RBG_SHAPE_COMPOSITE = 9,      /* TGeoCompositeShape node      */
+  RBG_SHAPE_WINSTON_2D = 10     /* AGeoWinstonCone2D            */
 };
 enum { RBG_OP_UNION = 0, RBG_OP_INTERSECTION = 1, RBG_OP_SUBTRACTION = 2 };
 
@@ -91,6 +92,7 @@ enum { RBG_OP_UNION = 0, RBG_OP_INTERSECTION = 1, RBG_OP_SUBTRACTION = 2 };
  *   ASPHERIC_DISK  z1 curve1 z2 curve2 rmax rmin conic1 conic2 npol1 npol2
  *                  steps repeat  k1[npol1] k2[npol2]
  *   WINSTON_POLY   r1 r2 n
+ *   WINSTON_2D     r1 r2 y                              (y: half length of the trough)
  *   COMPOSITE      (no params; op/left/right/left_matrix/right_matrix fields)
  * The flattened scene (rbg_flat_scene) holds a canonical layout that adds
  * derived quantities; it is documented in include/robast_gb_layout.h.

@@ -86,7 +86,8 @@
 #define RBG_ASPH_K 17
 #define RBG_ASPH_MAXPOL 16
 
-/* WINSTON_POLY (AGeoWinstonConePoly) */
+/* WINSTON_POLY (AGeoWinstonConePoly) and WINSTON_2D (AGeoWinstonCone2D,
+ * stored with N = 2, DX = r1 and DY = the trough's half length) */
 #define RBG_WIN_R1 0
 #define RBG_WIN_R2 1
 #define RBG_WIN_N 2

@@ -1078,9 +1078,90 @@ static void win_normal(const Win* w, const double* point, const double* dir, dou
 }
 
 /* ======================================================================
+ * AGeoWinstonCone2D (src/AGeoWinstonCone2D.cxx): the trough of two
+ * parabolic walls x = +-R(z), |y| <= dy.  Canonical parameters as the
+ * polygonal cone with n = 2 and the half-length in RBG_WIN_DY.
+ * ==================================================================== */
+/* Contains (:175-190) */
+static int win2d_contains(const Win* w, double dy, const double* p) {
+  double r;
+  if (fabs(p[1]) > dy || fabs(p[2]) > w->dz) return 0;
+  if (!win_R(w, p[2], &r)) return 0;
+  return !(fabs(p[0]) > r);
+}
+/* DistFromInside (:203-238) */
+static double win2d_dist_in(const Win* w, double dy, const double* p, const double* d) {
+  double v[4];
+  int i, k = 0;
+  v[0] = BIG;
+  if (d[2] < 0) v[0] = -(p[2] + w->dz) / d[2];
+  else if (d[2] > 0) v[0] = (w->dz - p[2]) / d[2];
+  v[1] = BIG;
+  if (d[1] < 0) v[1] = -(p[1] + dy) / d[1];
+  else if (d[1] > 0) v[1] = (dy - p[1]) / d[1];
+  v[2] = win_dist_parabola(w, p, d, 0., PI);
+  v[3] = win_dist_parabola(w, p, d, PI, PI);
+  for (i = 1; i < 4; ++i)
+    if (v[i] < v[k]) k = i;
+  return v[k];
+}
+/* DistFromOutside (:241-322) */
+static double win2d_dist_out(const Win* w, double dy, const double* p, const double* d) {
+  double s, r, a, b;
+  if (p[2] <= -w->dz) {
+    if (d[2] <= 0) return BIG;
+    s = -(w->dz + p[2]) / d[2];
+    if (fabs(p[0] + s * d[0]) <= w->r2 && fabs(p[1] + s * d[1]) <= dy) return s;
+  } else if (p[2] >= w->dz) {
+    if (d[2] >= 0) return BIG;
+    s = (w->dz - p[2]) / d[2];
+    if (fabs(p[0] + s * d[0]) <= w->r1 && fabs(p[1] + s * d[1]) <= dy) return s;
+  }
+  if (p[1] <= -dy) {
+    if (d[1] <= 0) return BIG;
+    s = -(dy + p[1]) / d[1];
+    if (fabs(p[2] + s * d[2]) <= w->dz && win_R(w, p[2] + s * d[2], &r) && fabs(p[0] + s * d[0]) <= r) return s;
+  } else if (p[1] >= dy) {
+    if (d[1] >= 0) return BIG;
+    s = (dy - p[1]) / d[1];
+    if (fabs(p[2] + s * d[2]) <= w->dz && win_R(w, p[2] + s * d[2], &r) && fabs(p[0] + s * d[0]) <= r) return s;
+  }
+  s = win_dist_parabola(w, p, d, 0., PI);
+  a = fabs(p[1] + s * d[1]) <= dy ? s : BIG;
+  s = win_dist_parabola(w, p, d, PI, PI);
+  b = fabs(p[1] + s * d[1]) <= dy ? s : BIG;
+  return a < b ? a : b;
+}
+/* ComputeNormal (:120-172) */
+static void win2d_normal(const Win* w, double dy, const double* p, const double* dir, double* n) {
+  double saf[3], r, m;
+  int i = 0, k;
+  saf[0] = fabs(fabs(dy) - fabs(p[1]));
+  saf[1] = fabs(fabs(w->dz) - fabs(p[2]));
+  saf[2] = win_R(w, p[2], &r) ? fabs(r - fabs(p[0])) : BIG;
+  for (k = 1; k < 3; ++k)
+    if (saf[k] < saf[i]) i = k;
+  if (i == 0) {
+    n[0] = 0; n[1] = 1; n[2] = 0;
+  } else if (i == 1) {
+    n[0] = 0; n[1] = 0; n[2] = 1;
+  } else {
+    n[0] = 1; n[1] = 0;
+    n[2] = p[0] > 0 ? -win_dRdZ(w, p[2]) : win_dRdZ(w, p[2]);
+  }
+  m = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  n[0] /= m; n[1] /= m; n[2] /= m;
+  if (n[0] * dir[0] + n[1] * dir[1] + n[2] * dir[2] < 0) {
+    n[0] = -n[0]; n[1] = -n[1]; n[2] = -n[2];
+  }
+}
+
+/* ======================================================================
  * shape dispatch (node-local frame)
  * ==================================================================== */
-static int is_ageo(int type) { return type == RBG_SHAPE_ASPHERIC_DISK || type == RBG_SHAPE_WINSTON_POLY; }
+static int is_ageo(int type) {
+  return type == RBG_SHAPE_ASPHERIC_DISK || type == RBG_SHAPE_WINSTON_POLY || type == RBG_SHAPE_WINSTON_2D;
+}
 
 static int shape_contains(Scene* S, int shape, const double* p) {
   int type = S->shapes[shape].type;
@@ -1093,6 +1174,11 @@ static int shape_contains(Scene* S, int shape, const double* p) {
     Win w;
     win_load(SP(S, shape), &w);
     return win_contains(&w, p);
+  }
+  if (type == RBG_SHAPE_WINSTON_2D) {
+    Win w;
+    win_load(SP(S, shape), &w);
+    return win2d_contains(&w, SP(S, shape)[RBG_WIN_DY], p);
   }
   return csg_contains(S, shape, p);
 }
@@ -1108,6 +1194,12 @@ static double shape_dist(Scene* S, int shape, const double* p, const double* d, 
     Win w;
     win_load(SP(S, shape), &w);
     return exit ? win_dist_in(&w, p, d) : win_dist_out(&w, p, d);
+  }
+  if (type == RBG_SHAPE_WINSTON_2D) {
+    Win w;
+    const double dy = SP(S, shape)[RBG_WIN_DY];
+    win_load(SP(S, shape), &w);
+    return exit ? win2d_dist_in(&w, dy, p, d) : win2d_dist_out(&w, dy, p, d);
   }
   return csg_dist(S, shape, p, d, exit, nrm, cap);
 }
@@ -1255,6 +1347,10 @@ static void nav_find_normal(Scene* S, const Nav* nv, double* n) {
       Asph a;
       asph_load(SP(S, N->shape), &a);
       asph_normal(&a, pl, dl, nl);
+    } else if (type == RBG_SHAPE_WINSTON_2D) {
+      Win w;
+      win_load(SP(S, N->shape), &w);
+      win2d_normal(&w, SP(S, N->shape)[RBG_WIN_DY], pl, dl, nl);
     } else {
       Win w;
       win_load(SP(S, N->shape), &w);

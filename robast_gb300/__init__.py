@@ -3,8 +3,9 @@
 The hot path, AOpticsManager::TraceNonSequential over an ARayArray, runs as
 hand-written sm_103a CUDA kernels behind the C ABI of include/robast_gb.h.
 """
-from .geometry import (AGeoAsphericDisk, AGeoWinstonConePoly, TGeoBBox, TGeoCombiTrans, TGeoCompositeShape,
-                       TGeoCone, TGeoHMatrix, TGeoMatrix, TGeoParaboloid, TGeoPcon, TGeoPgon, TGeoRotation,
+from .geometry import (AGeoAsphericDisk, AGeoBezierPcon, AGeoBezierPgon, AGeoWinstonCone2D, AGeoWinstonConePoly,
+                       TGeoBBox,
+                       TGeoCombiTrans, TGeoCompositeShape, TGeoCone, TGeoHMatrix, TGeoMatrix, TGeoParaboloid, TGeoPcon, TGeoPgon, TGeoRotation,
                        TGeoShape, TGeoSphere, TGeoTranslation, TGeoTube, TGeoTubeSeg)
 from .manager import AOpticsManager, ARay, ARayArray, ARayShooter, Scene
 from .optics import (ABorderSurfaceCondition, ACauchyFormula, AFilmetrixDotCom, AFocalSurface, AGlassCatalog, ALens,

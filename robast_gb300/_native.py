@@ -25,6 +25,7 @@ KIND_LENS, KIND_OBS, KIND_MIRROR, KIND_FOCUS, KIND_OPT, KIND_OTHER = range(6)
 SHAPE_BOX, SHAPE_TUBE, SHAPE_SPHERE, SHAPE_PARABOLOID = 1, 2, 3, 4
 SHAPE_PGON, SHAPE_PCON, SHAPE_ASPHERIC_DISK, SHAPE_WINSTON_POLY = 5, 6, 7, 8
 SHAPE_COMPOSITE = 9
+SHAPE_WINSTON_2D = 10
 OP_UNION, OP_INTERSECTION, OP_SUBTRACTION = 0, 1, 2
 
 TABLE_1D, TABLE_2D = 1, 2

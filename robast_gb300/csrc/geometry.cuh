@@ -954,6 +954,79 @@ RBG_NOINLINE d3 win_normal(const Win& w, d3 point, d3 dir) {
 }
 
 // --------------------------------------------------------------------
+// AGeoWinstonCone2D (src/AGeoWinstonCone2D.cxx): the trough between the
+// parabolic walls x = +-R(z), |y| <= dy -- a two-face Win (faces at phi = 0
+// and pi, each DistToParabola with a half-space window) plus two y slabs
+// --------------------------------------------------------------------
+// Contains (:175-190)
+RBG_NOINLINE bool win2d_contains(const Win& w, double dy, d3 p) {
+  if (fabs(p.y) > dy || fabs(p.z) > w.dz) return false;
+  double r;
+  if (!win_R(w, p.z, r)) return false;
+  return !(fabs(p.x) > r);
+}
+// DistFromInside (:203-238)
+RBG_NOINLINE double win2d_dist_in(const Win& w, double dy, d3 p, d3 d) {
+  double v[4];
+  v[0] = kBig;
+  if (d.z < 0) v[0] = -(p.z + w.dz) / d.z;
+  else if (d.z > 0) v[0] = (w.dz - p.z) / d.z;
+  v[1] = kBig;
+  if (d.y < 0) v[1] = -(p.y + dy) / d.y;
+  else if (d.y > 0) v[1] = (dy - p.y) / d.y;
+  v[2] = win_dist_parabola(w, p, d, 0, true);
+  v[3] = win_dist_parabola(w, p, d, 1, true);
+  int k = 0;
+  for (int i = 1; i < 4; ++i)
+    if (v[i] < v[k]) k = i;
+  return v[k];
+}
+// DistFromOutside (:241-322)
+RBG_NOINLINE double win2d_dist_out(const Win& w, double dy, d3 p, d3 d) {
+  if (p.z <= -w.dz) {
+    if (d.z <= 0) return kBig;
+    const double s = -(w.dz + p.z) / d.z;
+    if (fabs(p.x + s * d.x) <= w.r2 && fabs(p.y + s * d.y) <= dy) return s;
+  } else if (p.z >= w.dz) {
+    if (d.z >= 0) return kBig;
+    const double s = (w.dz - p.z) / d.z;
+    if (fabs(p.x + s * d.x) <= w.r1 && fabs(p.y + s * d.y) <= dy) return s;
+  }
+  double r;
+  if (p.y <= -dy) {
+    if (d.y <= 0) return kBig;
+    const double s = -(dy + p.y) / d.y, zn = p.z + s * d.z;
+    if (fabs(zn) <= w.dz && win_R(w, zn, r) && fabs(p.x + s * d.x) <= r) return s;
+  } else if (p.y >= dy) {
+    if (d.y >= 0) return kBig;
+    const double s = (dy - p.y) / d.y, zn = p.z + s * d.z;
+    if (fabs(zn) <= w.dz && win_R(w, zn, r) && fabs(p.x + s * d.x) <= r) return s;
+  }
+  double s = win_dist_parabola(w, p, d, 0, true);
+  const double a = fabs(p.y + s * d.y) <= dy ? s : kBig;
+  s = win_dist_parabola(w, p, d, 1, true);
+  const double b = fabs(p.y + s * d.y) <= dy ? s : kBig;
+  return a < b ? a : b;
+}
+// ComputeNormal (:120-172)
+RBG_NOINLINE d3 win2d_normal(const Win& w, double dy, d3 p, d3 dir) {
+  double saf[3], r;
+  saf[0] = fabs(fabs(dy) - fabs(p.y));
+  saf[1] = fabs(fabs(w.dz) - fabs(p.z));
+  saf[2] = win_R(w, p.z, r) ? fabs(r - fabs(p.x)) : kBig;
+  int i = 0;
+  for (int k = 1; k < 3; ++k)
+    if (saf[k] < saf[i]) i = k;
+  d3 n;
+  if (i == 0) n = mk(0, 1, 0);
+  else if (i == 1) n = mk(0, 0, 1);
+  else n = mk(1, 0, p.x > 0 ? -win_dRdZ(w, p.z) : win_dRdZ(w, p.z));
+  n = normalized(n);
+  if (dot(n, dir) < 0) n = neg(n);
+  return n;
+}
+
+// --------------------------------------------------------------------
 // dispatch
 // --------------------------------------------------------------------
 // Reciprocal seeded in FP32 and refined by one FP64 Newton step (relative
@@ -1020,6 +1093,9 @@ RBG_D bool shape_contains_body(const DevScene& S, int shape, d3 p) {
   if (type == RBG_SHAPE_ASPHERIC_DISK) return asph_contains(Asph{SP(S, shape)}, p);
   if (type == RBG_SHAPE_WINSTON_POLY)
     return (F & kFeatWinston) ? win_contains(win_load(SP(S, shape), ST(S, shape)), p) : false;
+  if (type == RBG_SHAPE_WINSTON_2D)
+    return (F & kFeatWinston) ? win2d_contains(win_load(SP(S, shape), ST(S, shape)), SP(S, shape)[RBG_WIN_DY], p)
+                              : false;
   if (!(F & kFeatCSG) && type == RBG_SHAPE_BOX) return prim_contains(RBG_SHAPE_BOX, SP(S, shape), nullptr, p);
   return (F & kFeatCSG) ? csg_contains(S, shape, p) : false;
 }
@@ -1031,9 +1107,13 @@ RBG_D double shape_dist_body(const DevScene& S, int shape, d3 p, d3 d, bool exit
     Asph a{SP(S, shape)};
     return exit ? asph_dist4(a, p, d) : asph_dist_out(a, p, d);
   }
-  if (type == RBG_SHAPE_WINSTON_POLY) {
+  if (type == RBG_SHAPE_WINSTON_POLY || type == RBG_SHAPE_WINSTON_2D) {
     if (!(F & kFeatWinston)) return kBig;
     Win w = win_load(SP(S, shape), ST(S, shape));
+    if (type == RBG_SHAPE_WINSTON_2D) {
+      const double dy = SP(S, shape)[RBG_WIN_DY];
+      return exit ? win2d_dist_in(w, dy, p, d) : win2d_dist_out(w, dy, p, d);
+    }
     return exit ? win_dist_in(w, p, d) : win_dist_out(w, p, d);
   }
   return (F & kFeatCSG) ? csg_dist(S, shape, p, d, exit, nrm, err) : kBig;
@@ -1056,7 +1136,9 @@ RBG_D double shape_dist(const DevScene& S, int shape, d3 p, d3 d, bool exit, d3&
   return F == 0 ? shape_dist_body<F>(S, shape, p, d, exit, nrm, err) : shape_dist_call<F>(S, shape, p, d, exit, nrm, err);
 }
 
-RBG_D bool is_ageo(int type) { return type == RBG_SHAPE_ASPHERIC_DISK || type == RBG_SHAPE_WINSTON_POLY; }
+RBG_D bool is_ageo(int type) {
+  return type == RBG_SHAPE_ASPHERIC_DISK || type == RBG_SHAPE_WINSTON_POLY || type == RBG_SHAPE_WINSTON_2D;
+}
 
 // ====================================================================
 // Mixed-precision fast paths.

@@ -339,6 +339,19 @@ struct Builder {
         b = {{-rc, -rc, -dz}, {rc, rc, dz}};
         break;
       }
+      case RBG_SHAPE_WINSTON_2D: {
+        if (u.n_params < 3) return RBG_ERR_SCENE;
+        const double r1 = p[0], r2 = p[1], y = std::fabs(p[2]);
+        if (r1 == r2 || r1 == 0 || r2 == 0) return RBG_ERR_SCENE;
+        // AGeoWinstonCone2D::SetWinstonDimensions (src/AGeoWinstonCone2D.cxx:551-567)
+        const double R1 = std::max(std::fabs(r1), std::fabs(r2)), R2 = std::min(std::fabs(r1), std::fabs(r2));
+        const double theta = std::asin(R2 / R1);
+        const double dz = (R1 + R2) / std::tan(theta) / 2.;
+        const double f = R2 * (1 + std::sin(theta));
+        q = {R1, R2, 2.0, theta, f, dz, R1, y};
+        b = {{-R1, -y, -dz}, {R1, y, dz}};  // ComputeBBox (:109-117)
+        break;
+      }
       case RBG_SHAPE_COMPOSITE: {
         if (u.op < RBG_OP_UNION || u.op > RBG_OP_SUBTRACTION) return RBG_ERR_SCENE;
         if (!matrix_ok(u.left_matrix) || !matrix_ok(u.right_matrix)) return RBG_ERR_SCENE;
@@ -351,7 +364,8 @@ struct Builder {
         composite_depth[id] = depth;
         for (int opnd : {u.left, u.right}) {
           int t = d->shapes[opnd].type;
-          if (t == RBG_SHAPE_ASPHERIC_DISK || t == RBG_SHAPE_WINSTON_POLY) return RBG_ERR_UNSUPPORTED;
+          if (t == RBG_SHAPE_ASPHERIC_DISK || t == RBG_SHAPE_WINSTON_POLY || t == RBG_SHAPE_WINSTON_2D)
+            return RBG_ERR_UNSUPPORTED;
         }
         q.assign(RBG_COMP_NP, 0.0);
         get_matrix(u.left_matrix, q.data() + RBG_COMP_ML);
@@ -589,7 +603,7 @@ struct Builder {
       }
     }
     for (const auto& sh : s->shapes) {
-      if (sh.type == RBG_SHAPE_WINSTON_POLY) s->features |= rbg::kFeatWinston;
+      if (sh.type == RBG_SHAPE_WINSTON_POLY || sh.type == RBG_SHAPE_WINSTON_2D) s->features |= rbg::kFeatWinston;
       else if (sh.type != RBG_SHAPE_BOX && sh.type != RBG_SHAPE_ASPHERIC_DISK) s->features |= rbg::kFeatCSG;
     }
     for (const auto& v : s->volumes)
@@ -649,7 +663,8 @@ void rbg::build_node_aux(rbg_scene* s) {
         }
         break;
       }
-      case RBG_SHAPE_WINSTON_POLY: {
+      case RBG_SHAPE_WINSTON_POLY:
+      case RBG_SHAPE_WINSTON_2D: {
         const int n = (int)P[RBG_WIN_N];
         const double th = P[RBG_WIN_THETA];
         s->trig.insert(s->trig.end(), {std::cos(th), std::sin(th), std::tan(M_PI / n)});

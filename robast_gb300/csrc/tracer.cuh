@@ -141,6 +141,8 @@ RBG_D bool shape_contains_f_body(const DevScene& S, int shape, const LRay& L, bo
   if (sh.type == RBG_SHAPE_BOX) return box_contains_f(P, Pf, L);
   if (sh.type == RBG_SHAPE_WINSTON_POLY)
     return (F & kFeatWinston) ? win_contains(win_load(P, ST(S, shape)), L.p) : false;
+  if (sh.type == RBG_SHAPE_WINSTON_2D)
+    return (F & kFeatWinston) ? win2d_contains(win_load(P, ST(S, shape)), P[RBG_WIN_DY], L.p) : false;
   return (F & kFeatCSG) ? csg_contains(S, shape, L.p) : false;
 }
 
@@ -237,9 +239,11 @@ RBG_D double shape_dist_f_body(const DevScene& S, int k, const LRay& L, bool exi
     const bool twin = S.aux[k].flags & RBG_AUX_ASPH_TWIN_FACES;
     return exit ? asph_dist4_f(P, Pf, L, twin, face) : asph_dist_out_f(P, Pf, L, twin, face);
   }
-  if (sh.type == RBG_SHAPE_WINSTON_POLY) {
+  if (sh.type == RBG_SHAPE_WINSTON_POLY || sh.type == RBG_SHAPE_WINSTON_2D) {
     if (!(F & kFeatWinston)) return kBig;
     Win w = win_load(P, ST(S, shape));
+    if (sh.type == RBG_SHAPE_WINSTON_2D)
+      return exit ? win2d_dist_in(w, P[RBG_WIN_DY], L.p, L.d) : win2d_dist_out(w, P[RBG_WIN_DY], L.p, L.d);
     return exit ? win_dist_in(w, L.p, L.d) : win_dist_out(w, L.p, L.d);
   }
   if (sh.type == RBG_SHAPE_BOX) return box_dist_fast(P, L.p, L.d, exit, nrm);
@@ -485,6 +489,9 @@ RBG_D d3 find_normal(const DevScene& S, const Nav& nv) {
     nl = asph_normal(a, pl, dl);
   } else if (type == RBG_SHAPE_WINSTON_POLY) {
     nl = win_normal(win_load(SP(S, N.shape), ST(S, N.shape)), to_local(N.m, nv.p), dir_to_local(N.m, nv.d));
+  } else if (type == RBG_SHAPE_WINSTON_2D) {
+    nl = win2d_normal(win_load(SP(S, N.shape), ST(S, N.shape)), SP(S, N.shape)[RBG_WIN_DY], to_local(N.m, nv.p),
+                      dir_to_local(N.m, nv.d));
   } else {
     nl = nv.xn;
   }

@@ -297,6 +297,69 @@ class TGeoCone(TGeoPcon):
         self.z, self.rmin, self.rmax = [-dz, dz], [rmin1, rmin2], [rmax1, rmax2]
 
 
+class _BezierSections:
+    """Side surface of AGeoBezierPcon / AGeoBezierPgon
+    (src/AGeoBezierPcon.cxx:35-80, src/AGeoBezierPgon.cxx:45-104): the nz
+    sections sample a Bezier curve B(t), t = i / (nz - 1), from (0, 0) to
+    (1, 1) through 0, 1 or 2 control points, mapped to r = r2 + B.x (r1 - r2)
+    and z = -dz + 2 dz B.y; section i is (z, rmin = 0, rmax = r)."""
+
+    def _bezier_init(self, r1, r2, dz):
+        self.fLength = 2.0 * float(dz)
+        self.fR1, self.fR2 = float(r1), float(r2)
+        self.fNcontrol = 0
+        self.fP1 = (0.0, 0.0)
+        self.fP2 = (0.0, 0.0)
+
+    def Bezier(self, t):
+        t = float(t)
+        if self.fNcontrol == 0:
+            bx, by = t, t
+        elif self.fNcontrol == 1:
+            a, b, c = (1 - t) * (1 - t), 2 * (1 - t) * t, t * t
+            bx, by = b * self.fP1[0] + c, b * self.fP1[1] + c
+        else:
+            a, b, c, d = (1 - t) ** 3, 3 * (1 - t) * (1 - t) * t, 3 * (1 - t) * t * t, t ** 3
+            bx = b * self.fP1[0] + c * self.fP2[0] + d
+            by = b * self.fP1[1] + c * self.fP2[1] + d
+        return self.fR2 + bx * (self.fR1 - self.fR2), -self.fLength / 2.0 + by * self.fLength
+
+    def SetControlPoints(self, r1, z1, r2=None, z2=None):
+        if r2 is None:
+            self.fNcontrol, self.fP1, self.fP2 = 1, (float(r1), float(z1)), (0.0, 0.0)
+        else:
+            self.fNcontrol, self.fP1, self.fP2 = 2, (float(r1), float(z1)), (float(r2), float(z2))
+        self.SetSections()
+
+    def SetSections(self):
+        for i in range(self.nz):
+            r, z = self.Bezier(i / (self.nz - 1))
+            self.DefineSection(i, z, 0.0, r)
+
+
+class AGeoBezierPcon(_BezierSections, TGeoPcon):
+    """AGeoBezierPcon([name,] phi, dphi, nz, r1, r2, dz): a polycone whose
+    side follows a Bezier curve from radius r2 at -dz to r1 at +dz; the
+    sections are set by SetSections / SetControlPoints, as in the reference,
+    and the shape is then a plain TGeoPcon."""
+
+    def __init__(self, *args):
+        name, v = _split_name(args, 6)
+        TGeoPcon.__init__(self, name, v[0], v[1], v[2])
+        self._bezier_init(v[3], v[4], v[5])
+
+
+class AGeoBezierPgon(_BezierSections, TGeoPgon):
+    """AGeoBezierPgon([name,] phi, dphi, nedges, nz, r1, r2, dz): the
+    polygonal counterpart of AGeoBezierPcon, a plain TGeoPgon once its
+    sections are set."""
+
+    def __init__(self, *args):
+        name, v = _split_name(args, 7)
+        TGeoPgon.__init__(self, name, v[0], v[1], v[2], v[3])
+        self._bezier_init(v[4], v[5], v[6])
+
+
 class AGeoAsphericDisk(TGeoShape):
     """AGeoAsphericDisk(z1, curve1, z2, curve2, rmax, rmin)
     (src/AGeoAsphericDisk.cxx:49-87)."""
@@ -371,6 +434,31 @@ class AGeoWinstonConePoly(TGeoShape):
 
     def params(self):
         return [self.r1, self.r2, self.n]
+
+
+class AGeoWinstonCone2D(TGeoShape):
+    """AGeoWinstonCone2D(r1, r2, y) (src/AGeoWinstonCone2D.cxx:37-51): a
+    two-dimensional compound parabolic concentrator, the trough between
+    the walls x = +-R(z) of entrance half-width r1 and exit half-width r2,
+    extruded over |y| <= y."""
+
+    type_id = N.SHAPE_WINSTON_2D
+
+    def __init__(self, *args):
+        name, v = _split_name(args, 3)
+        super().__init__(name)
+        self.r1, self.r2, self.y = float(v[0]), float(v[1]), float(v[2])
+
+    def GetDZ(self):
+        R1, R2 = max(abs(self.r1), abs(self.r2)), min(abs(self.r1), abs(self.r2))
+        theta = math.asin(R2 / R1)
+        return (R1 + R2) / math.tan(theta) / 2.0
+
+    def GetDY(self):
+        return abs(self.y)
+
+    def params(self):
+        return [self.r1, self.r2, self.y]
 
 
 class TGeoCompositeShape(TGeoShape):
