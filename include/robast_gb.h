@@ -137,7 +137,14 @@ typedef struct {
 
 /* AMultilayer: layers[layer_offset .. layer_offset+n_layers), first = top
  * (incident) medium, last = bottom (substrate); their thickness is ignored
- * (semi-infinite).  Coherent TMM only on the per-ray path. */
+ * (semi-infinite) and they count as incoherent.  Per ray the tracer takes
+ * CoherentTMMMixed (src/AMultilayer.cxx:240-481), or, after
+ * PreCalculateCoherentTMM / PreCalculateIncoherentTMM
+ * (include/AMultilayer.h:243-282), TH2::Interpolate of the tabulated
+ * (lambda, theta) reflectance and transmittance: precalc = 1 tabulates the
+ * coherent, 2 the incoherent (IncoherentTMM, :555-731) mixed-polarisation
+ * values at the bin centres of lam_nbins x th_nbins bins over
+ * [lam_min, lam_max) x [th_min, th_max) (lambda in cm, theta in rad). */
 typedef struct {
   int32_t index;      /* refractive index id */
   int32_t coherent;
@@ -146,6 +153,10 @@ typedef struct {
 typedef struct {
   int32_t layer_offset;
   int32_t n_layers;
+  int32_t precalc;    /* 0 none, 1 coherent table, 2 incoherent table */
+  int32_t lam_nbins, th_nbins;
+  int32_t reserved;
+  double lam_min, lam_max, th_min, th_max;
 } rbg_multilayer_desc;
 
 /* ABorderSurfaceCondition(component1, component2)
@@ -373,6 +384,17 @@ size_t rbg_bunches_workspace_bytes(int64_t n_bunches);
 int rbg_bunches_to_rays(const rbg_bunches* b, double z, double tel_z, double refractive_index,
                         double lambda_min, double lambda_max, uint64_t seed, void* workspace,
                         rbg_rays* out, int64_t capacity, int64_t* n_rays, void* stream);
+
+/* AMultilayer::CoherentTMM / IncoherentTMM / CoherentTMMMixed of a
+ * multilayer of the scene for n (angle, wavelength) pairs in DEVICE arrays,
+ * evaluated on the GPU in FP64 (the reference's multi-threaded vector
+ * overloads, include/AMultilayer.h:157-237).  mode: 0 coherent, 1
+ * incoherent, 2 what the tracer uses (the table when precalculated, else
+ * coherent); pol: 0 s, 1 p, 2 mixed (s and p averaged).  The incidence
+ * angle may be complex (th_im may be NULL).  Synchronises `stream`. */
+int rbg_multilayer_rt(rbg_scene* scene, int32_t multilayer, int32_t mode, int32_t pol, int64_t n,
+                      const double* th_re, const double* th_im, const double* lambda, double* R, double* T,
+                      void* stream);
 
 /* Autotuner of the mixed tracer (no counterpart in the reference, whose
  * thread split is fixed by the caller, src/AOpticsManager.cxx:529-567):

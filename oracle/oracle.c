@@ -244,14 +244,14 @@ static int is_forward_angle(double complex n, double complex th) {
   if (fabs(cimag(nc)) > 100 * eps) return cimag(nc) > 0;
   return creal(nc) > 0;
 }
-int orc_coherent_tmm(Scene* S, int ml, int pol, double th0r, double lam, double* R, double* T) {
-  if (ml < 0 || ml >= S->n_multilayers) return RBG_ERR_ARG;
-  const rbg_multilayer_desc* M = &S->multilayers[ml];
-  int N = M->n_layers;
+/* CoherentTMM over the media ids[0..N-1] (indices into S->layers), light
+ * incident from ids[0] at the (possibly complex) angle th0; a reversed
+ * stack (CoherentTMM's `reverse`) is the same call with ids reversed. */
+static void coh_tmm_seq(Scene* S, const int* ids, int N, int pol, double complex th0, double lam, double* R,
+                        double* T) {
   double complex n[64], th[64], ct[64], delta[64], r[64], t[64];
-  double complex th0 = th0r;
   for (int i = 0; i < N; ++i) {
-    const rbg_layer_desc* L = &S->layers[M->layer_offset + i];
+    const rbg_layer_desc* L = &S->layers[ids[i]];
     n[i] = orc_refractive_index(S, L->index, lam) + I * orc_extinction(S, L->index, lam);
   }
   /* ListSnell (src/AMultilayer.cxx:178-209) */
@@ -261,7 +261,7 @@ int orc_coherent_tmm(Scene* S, int ml, int pol, double th0r, double lam, double*
   if (!is_forward_angle(n[N - 1], th[N - 1])) th[N - 1] = PI - th[N - 1];
   for (int i = 0; i < N; ++i) ct[i] = ccos(th[i]);
   for (int i = 1; i < N - 1; ++i) {
-    const rbg_layer_desc* L = &S->layers[M->layer_offset + i];
+    const rbg_layer_desc* L = &S->layers[ids[i]];
     double complex kz = 2 * PI * n[i] * ct[i] / lam;
     delta[i] = kz * L->thickness;
     if (cimag(delta[i]) > 35) delta[i] = creal(delta[i]) + 35 * I; /* opacity clamp */
@@ -298,19 +298,159 @@ int orc_coherent_tmm(Scene* S, int ml, int pol, double th0r, double lam, double*
   }
   double complex rr = c / a, tt = 1. / a;
   *R = cabs(rr) * cabs(rr);
+  /* transmitted power with the incident angle th0 itself (:466-479) */
   if (pol == 0)
     *T = cabs(tt * tt) * (creal(n[N - 1] * ct[N - 1]) / creal(n[0] * ccos(th0)));
   else
     *T = cabs(tt * tt) * (creal(n[N - 1] * conj(ct[N - 1])) / creal(n[0] * conj(ccos(th0))));
+}
+
+static int ml_ids(Scene* S, int ml, int* ids) {
+  const rbg_multilayer_desc* M = &S->multilayers[ml];
+  for (int i = 0; i < M->n_layers; ++i) ids[i] = M->layer_offset + i;
+  return M->n_layers;
+}
+
+int orc_coherent_tmm_c(Scene* S, int ml, int pol, double th_re, double th_im, double lam, double* R, double* T) {
+  int ids[64];
+  if (ml < 0 || ml >= S->n_multilayers) return RBG_ERR_ARG;
+  int N = ml_ids(S, ml, ids);
+  coh_tmm_seq(S, ids, N, pol, th_re + I * th_im, lam, R, T);
   return RBG_OK;
 }
-int orc_coherent_tmm_mixed(Scene* S, int ml, double th0, double lam, double* R, double* T) {
+int orc_coherent_tmm(Scene* S, int ml, int pol, double th0r, double lam, double* R, double* T) {
+  return orc_coherent_tmm_c(S, ml, pol, th0r, 0.0, lam, R, T);
+}
+
+/* interface_RT (src/AMultilayer.cxx:93-104) */
+static void interface_RT(int pol, double complex ni, double complex nf, double complex thi, double complex thf,
+                         double* R, double* T) {
+  double complex ci = ccos(thi), cf = ccos(thf), ii = ni * ci, r, t;
+  if (pol == 0) {
+    double complex ff = nf * cf;
+    r = (ii - ff) / (ii + ff);
+    t = 2. * ii / (ii + ff);
+  } else {
+    double complex fi = nf * ci, iff = ni * cf;
+    r = (fi - iff) / (fi + iff);
+    t = 2. * ii / (fi + iff);
+  }
+  *R = cabs(r) * cabs(r);
+  if (pol == 0) *T = cabs(t * t) * (creal(nf * cf) / creal(ni * ci));
+  else *T = cabs(t * t) * (creal(nf * conj(cf)) / creal(ni * conj(ci)));
+}
+
+/* AMultilayer::IncoherentTMM (src/AMultilayer.cxx:555-731, tmm.inc_tmm):
+ * incoherent media (the first and last always) delimit coherent stacks;
+ * R/T between consecutive incoherent media come from the bare interface
+ * or the stack's forward and reversed CoherentTMM; P_i = exp(-4 pi d
+ * Im(n cos th) / lambda) >= 1e-30 per incoherent medium; the power
+ * matrices L multiply front to back: T = 1 / L00, R = L10 / L00. */
+int orc_incoherent_tmm(Scene* S, int ml, int pol, double th_re, double th_im, double lam, double* R, double* T) {
+  int ids[64], inc[64], ninc = 0;
+  double complex n[64], th[64];
+  double Rl[64][2], Tl[64][2]; /* [i][0]: i -> i+1, [i][1]: i+1 -> i */
+  if (ml < 0 || ml >= S->n_multilayers) return RBG_ERR_ARG;
+  int N = ml_ids(S, ml, ids);
+  for (int i = 0; i < N; ++i) {
+    const rbg_layer_desc* L = &S->layers[ids[i]];
+    n[i] = orc_refractive_index(S, L->index, lam) + I * orc_extinction(S, L->index, lam);
+  }
+  double complex th0 = th_re + I * th_im, n0s = n[0] * csin(th0);
+  for (int i = 0; i < N; ++i) th[i] = casin(n0s / n[i]);
+  if (!is_forward_angle(n[0], th[0])) th[0] = PI - th[0];
+  if (!is_forward_angle(n[N - 1], th[N - 1])) th[N - 1] = PI - th[N - 1];
+  for (int i = 0; i < N; ++i)
+    if (i == 0 || i == N - 1 || !S->layers[ids[i]].coherent) inc[ninc++] = i;
+  for (int k = 0; k + 1 < ninc; ++k) {
+    int p = inc[k], q = inc[k + 1];
+    if (q == p + 1) {
+      interface_RT(pol, n[p], n[q], th[p], th[q], &Rl[k][0], &Tl[k][0]);
+      interface_RT(pol, n[q], n[p], th[q], th[p], &Rl[k][1], &Tl[k][1]);
+    } else {
+      int fwd[64], bwd[64], m = q - p + 1;
+      for (int j = 0; j < m; ++j) {
+        fwd[j] = ids[p + j];
+        bwd[j] = ids[q - j];
+      }
+      coh_tmm_seq(S, fwd, m, pol, th[p], lam, &Rl[k][0], &Tl[k][0]);
+      coh_tmm_seq(S, bwd, m, pol, th[q], lam, &Rl[k][1], &Tl[k][1]);
+    }
+  }
+  /* Ltilde = L(0->1) prod_{k>=1} diag(1/P_k, P_k) L(k->k+1) */
+  double l00 = 1 / Tl[0][0], l01 = -Rl[0][1] / Tl[0][0], l10 = Rl[0][0] / Tl[0][0];
+  double l11 = (Tl[0][1] * Tl[0][0] - Rl[0][1] * Rl[0][0]) / Tl[0][0];
+  for (int k = 1; k + 1 < ninc; ++k) {
+    int i = inc[k];
+    double P = exp(-4 * PI * S->layers[ids[i]].thickness * cimag(n[i] * ccos(th[i])) / lam);
+    if (P < 1e-30) P = 1e-30;
+    double Tf = Tl[k][0], Rf = Rl[k][0], Tb = Tl[k][1], Rb = Rl[k][1];
+    double b00 = 1 / (P * Tf), b01 = -Rb / (P * Tf), b10 = P * Rf / Tf, b11 = P * (Tb * Tf - Rb * Rf) / Tf;
+    double c00 = l00 * b00 + l01 * b10, c01 = l00 * b01 + l01 * b11;
+    double c10 = l10 * b00 + l11 * b10, c11 = l10 * b01 + l11 * b11;
+    l00 = c00; l01 = c01; l10 = c10; l11 = c11;
+  }
+  *T = 1 / l00;
+  *R = l10 / l00;
+  return RBG_OK;
+}
+
+/* mixed-polarisation value of one stack, coherent or incoherent */
+static void stack_mixed(Scene* S, int ml, int incoherent, double th0, double lam, double* R, double* T) {
   double rp, tp, rs, ts;
-  int rc = orc_coherent_tmm(S, ml, 1, th0, lam, &rp, &tp);
-  if (rc) return rc;
-  orc_coherent_tmm(S, ml, 0, th0, lam, &rs, &ts);
+  if (incoherent) {
+    orc_incoherent_tmm(S, ml, 1, th0, 0.0, lam, &rp, &tp);
+    orc_incoherent_tmm(S, ml, 0, th0, 0.0, lam, &rs, &ts);
+  } else {
+    orc_coherent_tmm(S, ml, 1, th0, lam, &rp, &tp);
+    orc_coherent_tmm(S, ml, 0, th0, lam, &rs, &ts);
+  }
   *R = (rp + rs) / 2.;
   *T = (tp + ts) / 2.;
+}
+
+/* TH2::Interpolate of a precalculated table (include/AMultilayer.h:243-282):
+ * bilinear between bin centres, edge bins held in their outer half, 0
+ * outside [min, max); the four bin contents are evaluated on the spot at
+ * their bin centres (the values the table holds) */
+static void table_mixed(Scene* S, int ml, double th0, double lam, double* R, double* T) {
+  const rbg_multilayer_desc* M = &S->multilayers[ml];
+  int nx = M->lam_nbins, ny = M->th_nbins;
+  double xmin = M->lam_min, xmax = M->lam_max, ymin = M->th_min, ymax = M->th_max, x = lam, y = th0;
+  *R = 0;
+  *T = 0;
+  if (!(x >= xmin && x < xmax && y >= ymin && y < ymax)) return;
+  double wx = (xmax - xmin) / nx, wy = (ymax - ymin) / ny;
+  int bx = 1 + (int)floor((x - xmin) / wx), by = 1 + (int)floor((y - ymin) / wy);
+  bx = bx < 1 ? 1 : (bx > nx ? nx : bx);
+  by = by < 1 ? 1 : (by > ny ? ny : by);
+  double cxm = xmin + (bx - 0.5) * wx, cym = ymin + (by - 0.5) * wy, x1, x2, y1, y2;
+  int bx1, bx2, by1, by2;
+  if (x >= cxm) { x1 = cxm; x2 = cxm + wx; bx1 = bx; bx2 = bx + 1; }
+  else { x1 = cxm - wx; x2 = cxm; bx1 = bx - 1; bx2 = bx; }
+  if (y >= cym) { y1 = cym; y2 = cym + wy; by1 = by; by2 = by + 1; }
+  else { y1 = cym - wy; y2 = cym; by1 = by - 1; by2 = by; }
+  if (bx1 < 1) bx1 = 1;
+  if (bx2 > nx) bx2 = nx;
+  if (by1 < 1) by1 = 1;
+  if (by2 > ny) by2 = ny;
+  int bxs[2] = {bx1, bx2}, bys[2] = {by1, by2};
+  double qr[2][2], qt[2][2];
+  for (int u = 0; u < 2; ++u)
+    for (int v = 0; v < 2; ++v)
+      stack_mixed(S, ml, M->precalc == 2, ymin + (bys[v] - 0.5) * wy, xmin + (bxs[u] - 0.5) * wx, &qr[u][v],
+                  &qt[u][v]);
+  double dd = (x2 - x1) * (y2 - y1);
+  double w11 = (x2 - x) * (y2 - y), w21 = (x - x1) * (y2 - y), w12 = (x2 - x) * (y - y1), w22 = (x - x1) * (y - y1);
+  *R = (qr[0][0] * w11 + qr[1][0] * w21 + qr[0][1] * w12 + qr[1][1] * w22) / dd;
+  *T = (qt[0][0] * w11 + qt[1][0] * w21 + qt[0][1] * w12 + qt[1][1] * w22) / dd;
+}
+
+/* AMultilayer::CoherentTMMMixed (include/AMultilayer.h:114-132) */
+int orc_coherent_tmm_mixed(Scene* S, int ml, double th0, double lam, double* R, double* T) {
+  if (ml < 0 || ml >= S->n_multilayers) return RBG_ERR_ARG;
+  if (S->multilayers[ml].precalc != 0) table_mixed(S, ml, th0, lam, R, T);
+  else stack_mixed(S, ml, 0, th0, lam, R, T);
   return RBG_OK;
 }
 

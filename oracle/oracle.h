@@ -44,6 +44,12 @@ int orc_coherent_tmm(const rbg_flat_scene* scene, int multilayer, int pol,
                      double th0, double lambda, double* R, double* T);
 int orc_coherent_tmm_mixed(const rbg_flat_scene* scene, int multilayer,
                            double th0, double lambda, double* R, double* T);
+/* The same for a complex incidence angle th_re + i th_im, and
+ * AMultilayer::IncoherentTMM (coherent flags of the layers honoured). */
+int orc_coherent_tmm_c(const rbg_flat_scene* scene, int multilayer, int pol,
+                       double th_re, double th_im, double lambda, double* R, double* T);
+int orc_incoherent_tmm(const rbg_flat_scene* scene, int multilayer, int pol,
+                       double th_re, double th_im, double lambda, double* R, double* T);
 /* Refractive index / extinction of an index entry at lambda (cm). */
 double orc_refractive_index(const rbg_flat_scene* scene, int index, double lambda);
 double orc_extinction(const rbg_flat_scene* scene, int index, double lambda);

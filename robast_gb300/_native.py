@@ -55,7 +55,9 @@ class LayerDesc(C.Structure):
 
 
 class MultilayerDesc(C.Structure):
-    _fields_ = [("layer_offset", C.c_int32), ("n_layers", C.c_int32)]
+    _fields_ = [("layer_offset", C.c_int32), ("n_layers", C.c_int32), ("precalc", C.c_int32),
+                ("lam_nbins", C.c_int32), ("th_nbins", C.c_int32), ("reserved", C.c_int32),
+                ("lam_min", C.c_double), ("lam_max", C.c_double), ("th_min", C.c_double), ("th_max", C.c_double)]
 
 
 class BorderDesc(C.Structure):
@@ -187,6 +189,7 @@ def _declare(L):
     L.rbg_scene_autotune.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts), vp,
                                      C.POINTER(C.c_int32)]
     L.rbg_last_launch_count.argtypes = [vp]
+    L.rbg_multilayer_rt.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int64, vp, vp, vp, vp, vp, vp]
     L.rbg_focal_moments.argtypes = [C.c_int64, vp, vp, vp, vp, vp, C.c_int32, vp, vp]
     L.rbg_focal_histogram.argtypes = [C.c_int64, vp, vp, vp, C.c_int32, C.c_double, C.c_double,
                                       C.c_int32, C.c_double, C.c_double, vp, vp]

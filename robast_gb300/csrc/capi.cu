@@ -78,7 +78,9 @@ int ensure_device(rbg_scene* s) {
       (rc = upload(d->allocations, s->node_aux, &v.aux)) ||
       (rc = upload(d->allocations, s->fparams, &v.fparams)) ||
       (rc = upload(d->allocations, s->trig, &v.trig)) ||
-      (rc = upload(d->allocations, s->trig_off, &v.trig_off))) {
+      (rc = upload(d->allocations, s->trig_off, &v.trig_off)) ||
+      (rc = upload(d->allocations, s->tmm_tables, &v.tmm_tables)) ||
+      (rc = upload(d->allocations, s->tmm_off, &v.tmm_off))) {
     for (void* p : d->allocations) cudaFree(p);
     delete d;
     return rc;
@@ -97,6 +99,18 @@ int ensure_device(rbg_scene* s) {
   v.n_multilayers = (int32_t)s->multilayers.size();
   v.n_tables = (int32_t)s->tables.size();
   v.features = s->features;
+  if (!s->tmm_ready) {
+    // precalculated thin-film tables: fill on the device, keep a host copy
+    double* tab = const_cast<double*>(v.tmm_tables);
+    if ((rc = fill_tmm_tables(s, v, tab, 0)) ||
+        cudaMemcpy(s->tmm_tables.data(), tab, s->tmm_tables.size() * sizeof(double), cudaMemcpyDeviceToHost) !=
+            cudaSuccess) {
+      for (void* p : d->allocations) cudaFree(p);
+      delete d;
+      return rc ? rc : RBG_ERR_CUDA;
+    }
+    s->tmm_ready = true;
+  }
   s->dev = d;
   s->dev_id = dev;
   return RBG_OK;

@@ -33,6 +33,10 @@ struct DevScene {
   // per-shape trigonometric constants (node_aux.h), both tracers
   const double* trig;
   const int32_t* trig_off;
+  // precalculated thin-film tables (R then T per multilayer), offsets per
+  // multilayer or -1
+  const double* tmm_tables;
+  const int64_t* tmm_off;
   int32_t n_nodes, n_borders, n_multilayers, n_tables;
   uint32_t features;  // kFeat* bits present in the scene
 };

@@ -15,4 +15,6 @@ struct rbg_device_scene {
 namespace rbg {
 int ensure_device(rbg_scene* s);  // upload on first use (capi.cu)
 int sm_count();
+// precalculated thin-film tables of s into `tables` (device), tmm.cu
+int fill_tmm_tables(const rbg_scene* s, const DevScene& S, double* tables, cudaStream_t st);
 }  // namespace rbg

@@ -32,6 +32,10 @@
 #include "scene_internal.h"
 #include "tracer.cuh"
 
+namespace rbg {
+int fill_tmm_tables(const rbg_scene* s, const DevScene& S, double* tables, cudaStream_t st);
+}
+
 #define RBG_NOALLOC_SCRATCH_BYTES (4u << 20)
 
 static __device__ __align__(256) unsigned char g_trace_scratch[RBG_NOALLOC_SCRATCH_BYTES];
@@ -100,7 +104,7 @@ extern "C" int rbg_trace_noalloc(rbg_scene* s, const rbg_rays* in, rbg_result* o
                       table_bytes(s->tables) + table_bytes(s->indices) + table_bytes(s->layers) +
                       table_bytes(s->multilayers) + table_bytes(s->borders) + table_bytes(s->params) +
                       table_bytes(s->node_aux) + table_bytes(s->fparams) + table_bytes(s->trig) +
-                      table_bytes(s->trig_off);
+                      table_bytes(s->trig_off) + table_bytes(s->tmm_tables) + table_bytes(s->tmm_off);
   if (need > RBG_NOALLOC_SCRATCH_BYTES) return RBG_ERR_TOO_LARGE;
   unsigned char* base = nullptr;
   int rc = scratch_address(&base);
@@ -118,13 +122,26 @@ extern "C" int rbg_trace_noalloc(rbg_scene* s, const rbg_rays* in, rbg_result* o
       (rc = place(s->multilayers, base, &off, st, &v.multilayers)) ||
       (rc = place(s->borders, base, &off, st, &v.borders)) || (rc = place(s->params, base, &off, st, &v.params)) ||
       (rc = place(s->node_aux, base, &off, st, &v.aux)) || (rc = place(s->fparams, base, &off, st, &v.fparams)) ||
-      (rc = place(s->trig, base, &off, st, &v.trig)) || (rc = place(s->trig_off, base, &off, st, &v.trig_off)))
+      (rc = place(s->trig, base, &off, st, &v.trig)) || (rc = place(s->trig_off, base, &off, st, &v.trig_off)) ||
+      (rc = place(s->tmm_tables, base, &off, st, &v.tmm_tables)) ||
+      (rc = place(s->tmm_off, base, &off, st, &v.tmm_off)))
     return rc;
   v.n_nodes = (int32_t)s->nodes.size();
   v.n_borders = (int32_t)s->borders.size();
   v.n_multilayers = (int32_t)s->multilayers.size();
   v.n_tables = (int32_t)s->tables.size();
   v.features = s->features;
+  if (!s->tmm_ready) {
+    // precalculated thin-film tables not computed yet (no rbg_trace on this
+    // scene so far): fill them in place in the array, keep a host copy
+    double* tab = const_cast<double*>(v.tmm_tables);
+    if ((rc = fill_tmm_tables(s, v, tab, st))) return rc;
+    if (cudaMemcpyAsync(s->tmm_tables.data(), tab, s->tmm_tables.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                        st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return RBG_ERR_CUDA;
+    s->tmm_ready = true;
+  }
   unsigned* err_flags = reinterpret_cast<unsigned*>(base);
   unsigned long long* counter = reinterpret_cast<unsigned long long*>(base + 8);
   // the error word and the queue head must start at zero on every call

@@ -574,9 +574,23 @@ struct Builder {
     for (auto& l : s->layers)
       if (l.index < 0 || l.index >= d->n_indices) return RBG_ERR_SCENE;
     s->multilayers.assign(d->multilayers, d->multilayers + d->n_multilayers);
-    for (auto& m : s->multilayers)
+    s->tmm_off.assign(s->multilayers.size(), -1);
+    int64_t tmm_cells = 0;
+    for (size_t i = 0; i < s->multilayers.size(); ++i) {
+      const auto& m = s->multilayers[i];
       if (m.n_layers < 2 || m.n_layers > 64 || m.layer_offset < 0 || m.layer_offset + m.n_layers > d->n_layers)
         return RBG_ERR_SCENE;
+      if (m.precalc < 0 || m.precalc > 2) return RBG_ERR_SCENE;
+      if (m.precalc != 0) {
+        if (m.lam_nbins < 1 || m.th_nbins < 1 || (int64_t)m.lam_nbins * m.th_nbins > (int64_t)1 << 24 ||
+            !(m.lam_max > m.lam_min) || !(m.th_max > m.th_min))
+          return RBG_ERR_SCENE;
+        s->tmm_off[i] = tmm_cells;
+        tmm_cells += 2 * (int64_t)m.lam_nbins * m.th_nbins;
+      }
+    }
+    s->tmm_tables.assign((size_t)tmm_cells, 0.0);
+    s->tmm_ready = tmm_cells == 0;
     s->borders.assign(d->borders, d->borders + d->n_borders);
     for (auto& b : s->borders)
       if (b.component1 < 0 || b.component1 >= d->n_volumes || b.component2 < -1 ||

@@ -34,6 +34,11 @@ struct rbg_scene {
   // per-shape trigonometric constants (node_aux.h), offsets per shape or -1
   std::vector<double> trig;
   std::vector<int32_t> trig_off;
+  // precalculated thin-film tables: R then T per multilayer at tmm_off (or
+  // -1); filled on the GPU at the first upload (tmm.cu), then kept here
+  std::vector<double> tmm_tables;
+  std::vector<int64_t> tmm_off;
+  bool tmm_ready = true;
 
   // device mirror, owned by the CUDA side (capi.cu)
   rbg_device_scene* dev = nullptr;

@@ -579,32 +579,34 @@ RBG_D bool is_forward_angle(cplxT<T> n, cplxT<T> th) {
 }
 
 // AMultilayer::CoherentTMM (src/AMultilayer.cxx:240-481), pol 0 = s, 1 = p,
-// evaluated in precision T; the stack is walked front to back, building the
-// transfer-matrix product on the fly
+// in precision T, for the m media S.layers[base + a + k dir], k = 0..m-1
+// (dir = +1 front to back, -1 reversed as CoherentTMM's `reverse`), light
+// incident from medium k = 0 at the (possibly complex) angle th0.  The
+// transfer-matrix product is built on the fly, front to back.
 template <typename T>
-RBG_D void coherent_tmm(const DevScene& S, int ml, int pol, double th0r, double lam, double& R, double& Tr) {
+RBG_D void tmm_coherent(const DevScene& S, int base, int a, int m, int dir, int pol, cplxT<T> th0, double lam,
+                        double& R, double& Tr) {
   typedef cplxT<T> C;
-  const rbg_multilayer_desc M = S.multilayers[ml];
-  const int N = M.n_layers;
-  auto nidx = [&](int i) {
-    const rbg_layer_desc& L = S.layers[M.layer_offset + i];
+  auto layer = [&](int k) -> const rbg_layer_desc& { return S.layers[base + a + k * dir]; };
+  auto nidx = [&](int k) {
+    const rbg_layer_desc& L = layer(k);
     return cx<T>((T)index_n(S, L.index, lam), (T)index_k(S, L.index, lam));
   };
   const T pi = T(kPi);
-  C th0 = cx<T>((T)th0r);
   C n0 = nidx(0);
   C n0s = n0 * csin_(th0);
+  // ListSnell (:178-209): the first and the last angle are the forward ones
   C th_first = casin_(cdiv(n0s, n0));
   if (!is_forward_angle(n0, th_first)) th_first = cx<T>(pi) - th_first;
-  C a = cx<T>(1), b = cx<T>(0), c = cx<T>(0), d = cx<T>(1);
+  C a00 = cx<T>(1), a01 = cx<T>(0), a10 = cx<T>(0), a11 = cx<T>(1);
   C n_prev = n0, ct_prev = ccos_(th_first);
   C r0 = cx<T>(0), t0 = cx<T>(1);
-  for (int i = 1; i < N; ++i) {
+  for (int i = 1; i < m; ++i) {
     C ni = nidx(i);
     C thi = casin_(cdiv(n0s, ni));
-    if (i == N - 1 && !is_forward_angle(ni, thi)) thi = cx<T>(pi) - thi;
+    if (i == m - 1 && !is_forward_angle(ni, thi)) thi = cx<T>(pi) - thi;
     C cti = ccos_(thi);
-    // interface (i-1) -> i
+    // interface (i-1) -> i, interface_rt (:26-56)
     C ii = n_prev * ct_prev, r, t;
     if (pol == 0) {
       C ff = ni * cti;
@@ -620,30 +622,30 @@ RBG_D void coherent_tmm(const DevScene& S, int ml, int pol, double th0r, double 
       t0 = t;
     } else {
       // layer i-1: (1/t) diag(e^{-i delta}, e^{i delta}) [[1, r],[r, 1]]
-      const rbg_layer_desc& L = S.layers[M.layer_offset + i - 1];
       C kz = (T(2) * pi / (T)lam) * (n_prev * ct_prev);
-      C delta = (T)L.thickness * kz;
+      C delta = (T)layer(i - 1).thickness * kz;
       if (delta.im > 35) delta.im = 35;
       C em = cexp_(C{delta.im, -delta.re});
       C ep = cexp_(C{-delta.im, delta.re});
       C it = cdiv(cx<T>(1), t);
       C m00 = em * it, m01 = em * r * it, m10 = ep * r * it, m11 = ep * it;
-      C na = a * m00 + b * m10, nb = a * m01 + b * m11;
-      C nc = c * m00 + d * m10, nd = c * m01 + d * m11;
-      a = na;
-      b = nb;
-      c = nc;
-      d = nd;
+      C na = a00 * m00 + a01 * m10, nb = a00 * m01 + a01 * m11;
+      C nc = a10 * m00 + a11 * m10, nd = a10 * m01 + a11 * m11;
+      a00 = na;
+      a01 = nb;
+      a10 = nc;
+      a11 = nd;
     }
     n_prev = ni;
     ct_prev = cti;
   }
   // prepend the first interface: (1/t0) [[1, r0],[r0, 1]] * Mtilde
   C it0 = cdiv(cx<T>(1), t0);
-  C A = (a + r0 * c) * it0, Cc = (r0 * a + c) * it0;
+  C A = (a00 + r0 * a10) * it0, Cc = (r0 * a00 + a10) * it0;
   C rr = cdiv(Cc, A), tt = cdiv(cx<T>(1), A);
   T ar = cabs_(rr);
   R = (double)(ar * ar);
+  // transmitted power with the incident angle th0 itself (:466-479)
   C ct0 = ccos_(th0);
   C nf = n_prev, ctf = ct_prev;
   T tt2 = cabs_(tt * tt);
@@ -651,8 +653,147 @@ RBG_D void coherent_tmm(const DevScene& S, int ml, int pol, double th0r, double 
   else Tr = (double)(tt2 * ((nf * C{ctf.re, -ctf.im}).re / (n0 * C{ct0.re, -ct0.im}).re));
 }
 
+template <typename T>
+RBG_D void coherent_tmm(const DevScene& S, int ml, int pol, double th0r, double lam, double& R, double& Tr) {
+  const rbg_multilayer_desc& M = S.multilayers[ml];
+  tmm_coherent<T>(S, M.layer_offset, 0, M.n_layers, 1, pol, cx<T>((T)th0r), lam, R, Tr);
+}
+
+// interface_RT (:93-104): power reflection and transmission of one interface
+RBG_D void tmm_interface_RT(int pol, cplxT<double> ni, cplxT<double> nf, cplxT<double> thi, cplxT<double> thf,
+                            double& R, double& T) {
+  typedef cplxT<double> C;
+  const C ci = ccos_(thi), cf = ccos_(thf);
+  const C ii = ni * ci;
+  C r, t;
+  if (pol == 0) {
+    const C ff = nf * cf;
+    r = cdiv(ii - ff, ii + ff);
+    t = cdiv(2.0 * ii, ii + ff);
+  } else {
+    const C fi = nf * ci, iff = ni * cf;
+    r = cdiv(fi - iff, fi + iff);
+    t = cdiv(2.0 * ii, fi + iff);
+  }
+  const double ar = cabs_(r);
+  R = ar * ar;
+  const double t2 = cabs_(t * t);
+  if (pol == 0) T = t2 * ((nf * cf).re / (ni * ci).re);
+  else T = t2 * ((nf * C{cf.re, -cf.im}).re / (ni * C{ci.re, -ci.im}).re);
+}
+
+// AMultilayer::IncoherentTMM (:555-731), the incoherent / partly coherent
+// transfer-matrix method of tmm.inc_tmm: the media flagged incoherent (the
+// first and the last always) split the stack into coherent sub-stacks; each
+// sub-stack (or bare interface) between two incoherent media contributes its
+// forward and backward power R and T; an incoherent medium of thickness d
+// passes P = exp(-4 pi d Im(n cos th) / lambda) of the power (at least
+// 1e-30); the 2x2 power matrices multiply front to back, T = 1 / L00,
+// R = L10 / L00.  FP64, evaluated where the tables are filled.
+RBG_D void tmm_incoherent(const DevScene& S, int ml, int pol, cplxT<double> th0, double lam, double& R, double& T) {
+  typedef cplxT<double> C;
+  const rbg_multilayer_desc& M = S.multilayers[ml];
+  const int N = M.n_layers, base = M.layer_offset;
+  auto n_of = [&](int k) {
+    const rbg_layer_desc& L = S.layers[base + k];
+    return cx<double>(index_n(S, L.index, lam), index_k(S, L.index, lam));
+  };
+  const C n0s = n_of(0) * csin_(th0);
+  // ListSnell over all media, forward angles at both ends
+  auto th_of = [&](int k) {
+    const C nk = n_of(k);
+    C th = casin_(cdiv(n0s, nk));
+    if ((k == 0 || k == N - 1) && !is_forward_angle(nk, th)) th = cx<double>(kPi) - th;
+    return th;
+  };
+  auto incoherent = [&](int k) { return k == 0 || k == N - 1 || !S.layers[base + k].coherent; };
+  // power R/T from incoherent medium p to the next incoherent medium q, both ways
+  auto pair = [&](int p, int q, double& Rf, double& Tf, double& Rb, double& Tb) {
+    if (q == p + 1) {
+      const C np = n_of(p), nq = n_of(q), thp = th_of(p), thq = th_of(q);
+      tmm_interface_RT(pol, np, nq, thp, thq, Rf, Tf);
+      tmm_interface_RT(pol, nq, np, thq, thp, Rb, Tb);
+    } else {
+      tmm_coherent<double>(S, base, p, q - p + 1, 1, pol, th_of(p), lam, Rf, Tf);
+      tmm_coherent<double>(S, base, q, q - p + 1, -1, pol, th_of(q), lam, Rb, Tb);
+    }
+  };
+  // Ltilde = L(0->1) [ prod_i diag(1/P_i, P_i) L(i->i+1) ]
+  int p = 0, q = 1;
+  while (!incoherent(q)) ++q;
+  double Rf, Tf, Rb, Tb;
+  pair(p, q, Rf, Tf, Rb, Tb);
+  double l00 = 1 / Tf, l01 = -Rb / Tf, l10 = Rf / Tf, l11 = (Tb * Tf - Rb * Rf) / Tf;
+  while (q < N - 1) {
+    p = q;
+    q = p + 1;
+    while (!incoherent(q)) ++q;
+    const C np = n_of(p);
+    const C thp = th_of(p);
+    const C nc = np * ccos_(thp);
+    double P = exp(-4 * kPi * S.layers[base + p].thickness * nc.im / lam);
+    if (P < 1e-30) P = 1e-30;
+    pair(p, q, Rf, Tf, Rb, Tb);
+    // L = diag(1/P, P) [[1, -Rb],[Rf, Tb Tf - Rb Rf]] / Tf
+    const double b00 = 1 / (P * Tf), b01 = -Rb / (P * Tf), b10 = P * Rf / Tf, b11 = P * (Tb * Tf - Rb * Rf) / Tf;
+    const double c00 = l00 * b00 + l01 * b10, c01 = l00 * b01 + l01 * b11;
+    const double c10 = l10 * b00 + l11 * b10, c11 = l10 * b01 + l11 * b11;
+    l00 = c00;
+    l01 = c01;
+    l10 = c10;
+    l11 = c11;
+  }
+  T = 1 / l00;
+  R = l10 / l00;
+}
+
+// TH2::Interpolate on a lam_nbins x th_nbins table (x = lambda, y = theta)
+// stored [ix * ny + iy]: bilinear between bin centres, the edge bins held
+// constant in their outer half, 0 outside [min, max) of either axis
+RBG_D double th2_interpolate(const double* tab, int nx, double xmin, double xmax, int ny, double ymin, double ymax,
+                             double x, double y) {
+  if (!(x >= xmin && x < xmax && y >= ymin && y < ymax)) return 0.0;
+  const double wx = (xmax - xmin) / nx, wy = (ymax - ymin) / ny;
+  int bx = 1 + (int)floor((x - xmin) / wx), by = 1 + (int)floor((y - ymin) / wy);
+  bx = bx < 1 ? 1 : (bx > nx ? nx : bx);
+  by = by < 1 ? 1 : (by > ny ? ny : by);
+  const double cxm = xmin + (bx - 0.5) * wx, cym = ymin + (by - 0.5) * wy;
+  double x1, x2, y1, y2;
+  int bx1, bx2, by1, by2;
+  if (x >= cxm) {
+    x1 = cxm; x2 = cxm + wx; bx1 = bx; bx2 = bx + 1;
+  } else {
+    x1 = cxm - wx; x2 = cxm; bx1 = bx - 1; bx2 = bx;
+  }
+  if (y >= cym) {
+    y1 = cym; y2 = cym + wy; by1 = by; by2 = by + 1;
+  } else {
+    y1 = cym - wy; y2 = cym; by1 = by - 1; by2 = by;
+  }
+  bx1 = bx1 < 1 ? 1 : bx1;
+  bx2 = bx2 > nx ? nx : bx2;
+  by1 = by1 < 1 ? 1 : by1;
+  by2 = by2 > ny ? ny : by2;
+  const double q11 = tab[(bx1 - 1) * ny + by1 - 1], q21 = tab[(bx2 - 1) * ny + by1 - 1];
+  const double q12 = tab[(bx1 - 1) * ny + by2 - 1], q22 = tab[(bx2 - 1) * ny + by2 - 1];
+  const double d = (x2 - x1) * (y2 - y1);
+  return (q11 * (x2 - x) * (y2 - y) + q21 * (x - x1) * (y2 - y) + q12 * (x2 - x) * (y - y1) +
+          q22 * (x - x1) * (y - y1)) / d;
+}
+
+// CoherentTMMMixed (include/AMultilayer.h:114-132): the precalculated table
+// when there is one, else the mean of the p and s evaluations (FP32 in the
+// mixed tracer)
 template <bool MIXED, unsigned F = kFeatAll>
 RBG_D void coherent_tmm_mixed(const DevScene& S, int ml, double th0, double lam, double& R, double& T) {
+  const rbg_multilayer_desc& M = S.multilayers[ml];
+  if (M.precalc != 0 && S.tmm_off[ml] >= 0) {
+    const double* tab = S.tmm_tables + S.tmm_off[ml];
+    const int64_t cells = (int64_t)M.lam_nbins * M.th_nbins;
+    R = th2_interpolate(tab, M.lam_nbins, M.lam_min, M.lam_max, M.th_nbins, M.th_min, M.th_max, lam, th0);
+    T = th2_interpolate(tab + cells, M.lam_nbins, M.lam_min, M.lam_max, M.th_nbins, M.th_min, M.th_max, lam, th0);
+    return;
+  }
   double rp, tp, rs, ts;
   if (MIXED) {
     coherent_tmm<float>(S, ml, 1, th0, lam, rp, tp);

@@ -354,7 +354,12 @@ class SceneBuilder:
         off = len(self.layers)
         for (idx, th, coh), iid in zip(m.layers, ids):
             self.layers.append(N.LayerDesc(iid, int(bool(coh)), th if math.isfinite(th) else 0.0))
-        self.multilayers.append(N.MultilayerDesc(off, len(m.layers)))
+        md = N.MultilayerDesc(off, len(m.layers))
+        if m.precalc is not None:
+            kind, nl, lmin, lmax, nt, tmin, tmax = m.precalc
+            md.precalc, md.lam_nbins, md.th_nbins = kind, nl, nt
+            md.lam_min, md.lam_max, md.th_min, md.th_max = lmin, lmax, tmin, tmax
+        self.multilayers.append(md)
         self.multilayer_ids[key] = len(self.multilayers) - 1
         return self.multilayer_ids[key]
 

@@ -329,6 +329,21 @@ class AMultilayer:
 
     def __init__(self, top: ARefractiveIndex, bottom: ARefractiveIndex):
         self.layers = [(top, math.inf, False), (bottom, math.inf, False)]
+        self.precalc = None
+
+    def PreCalculateCoherentTMM(self, lam_nbins, lam_min, lam_max, th_nbins, th_min, th_max):
+        """Tabulate CoherentTMMMixed at the centres of a lam_nbins x th_nbins
+        grid; traces then interpolate the table (TH2::Interpolate) instead
+        of evaluating the stack per ray (include/AMultilayer.h:243-262).
+        The table is computed on the GPU when the scene is uploaded."""
+        self.precalc = (1, int(lam_nbins), float(lam_min), float(lam_max), int(th_nbins), float(th_min),
+                        float(th_max))
+
+    def PreCalculateIncoherentTMM(self, lam_nbins, lam_min, lam_max, th_nbins, th_min, th_max):
+        """As PreCalculateCoherentTMM with IncoherentTMMMixed values
+        (include/AMultilayer.h:263-282)."""
+        self.precalc = (2, int(lam_nbins), float(lam_min), float(lam_max), int(th_nbins), float(th_min),
+                        float(th_max))
 
     def AddLayer(self, idx, thickness, coherent=True):
         self.layers.insert(1, (idx, float(thickness), coherent))

@@ -30,6 +30,8 @@ def lib():
         L.orc_trace.argtypes = [fs, C.POINTER(N.Rays), C.POINTER(N.Result), C.POINTER(N.TraceOpts), C.c_int]
         L.orc_coherent_tmm.argtypes = [fs, C.c_int, C.c_int, C.c_double, C.c_double, dp, dp]
         L.orc_coherent_tmm_mixed.argtypes = [fs, C.c_int, C.c_double, C.c_double, dp, dp]
+        for f in ("orc_coherent_tmm_c", "orc_incoherent_tmm"):
+            getattr(L, f).argtypes = [fs, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, dp, dp]
         L.orc_refractive_index.argtypes = [fs, C.c_int, C.c_double]
         L.orc_refractive_index.restype = C.c_double
         L.orc_extinction.argtypes = [fs, C.c_int, C.c_double]
@@ -111,3 +113,13 @@ def bunches_to_rays(b, z, tel_z, n_index, lam_min, lam_max, seed):
                                   *(out[f].ctypes.data_as(dp) for f in ("x", "y", "z", "t", "dx", "dy", "dz", "lam")),
                                   cap)
     return {k: v[:n] for k, v in out.items()}
+
+
+def tmm_c(manager_or_scene, ml: int, pol: int, th: complex, lam: float, incoherent=False):
+    """Oracle CoherentTMM / IncoherentTMM for a complex incidence angle."""
+    scene = manager_or_scene._ensure_scene() if hasattr(manager_or_scene, "_ensure_scene") else manager_or_scene
+    R, T = C.c_double(), C.c_double()
+    f = lib().orc_incoherent_tmm if incoherent else lib().orc_coherent_tmm_c
+    st = f(C.byref(scene.flat), ml, pol, complex(th).real, complex(th).imag, lam, C.byref(R), C.byref(T))
+    assert st == 0
+    return R.value, T.value
