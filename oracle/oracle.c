@@ -647,6 +647,9 @@ static void add_pgon_faces(XList* L, const double* P, const double* o, const dou
       const double* R = which ? RMIN : RMAX;
       if (which && R[k] == 0 && R[k + 1] == 0) continue;
       double s = (R[k + 1] - R[k]) / h;
+      /* crossings of a face plane outside its section's z range are no
+       * boundary points of the solid; they are skipped */
+      double tol = 1e-6 * (h + fabs(Z[k]) + fabs(Z[k + 1])) + 1e-9;
       for (int e = 0; e < ned; ++e) {
         double pe = (P[0] + (e + 0.5) * sector) * D2R;
         double n[3] = {cos(pe), sin(pe), -s};
@@ -654,7 +657,9 @@ static void add_pgon_faces(XList* L, const double* P, const double* o, const dou
         double rhs = R[k] - s * Z[k];
         double den = dot3(n, d);
         if (den == 0) continue;
-        xl_add(L, (rhs - dot3(n, o)) / den, n, M);
+        double t = (rhs - dot3(n, o)) / den, zt = o[2] + t * d[2];
+        if (zt < Z[k] - tol || zt > Z[k + 1] + tol) continue;
+        xl_add(L, t, n, M);
       }
     }
   }
@@ -677,8 +682,10 @@ static void add_pcon_faces(XList* L, const double* P, const double* o, const dou
       double C = o[0] * o[0] + o[1] * o[1] - (c0 + s * o[2]) * (c0 + s * o[2]);
       double r[2];
       int m = quad_roots(A, B, C, r);
+      double tol = 1e-6 * (h + fabs(Z[k]) + fabs(Z[k + 1])) + 1e-9;
       for (int i = 0; i < m; ++i) {
         double p[3] = {o[0] + r[i] * d[0], o[1] + r[i] * d[1], o[2] + r[i] * d[2]};
+        if (p[2] < Z[k] - tol || p[2] > Z[k + 1] + tol) continue; /* not on this section's cone */
         double rz = c0 + s * p[2];
         double n[3] = {p[0], p[1], -s * rz};
         xl_add(L, r[i], n, M);

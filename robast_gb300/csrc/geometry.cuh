@@ -281,13 +281,22 @@ RBG_D void prim_collect(int type, const double* P, const double* T, d3 o, d3 d, 
       for (int k = 0; k < nz - 1; ++k) {
         double h = Z[k + 1] - Z[k];
         if (h <= 0) continue;
+        // a face plane crossed outside its own section's z range is no
+        // boundary point of the solid: dropping it changes no midpoint
+        // classification and keeps the list short
+        const double tol = 1e-6 * (h + fabs(Z[k]) + fabs(Z[k + 1])) + 1e-9;
         for (int w = 0; w < 2; ++w) {
           const double* R = w ? RMIN : RMAX;
           if (w && R[k] == 0 && R[k + 1] == 0) continue;
           double s = (R[k + 1] - R[k]) / h;
-          for (int e = 0; e < ned; ++e)
-            add_plane(L, o, d, mk(E[2 * e], E[2 * e + 1], -s), R[k] - s * Z[k],
-                      leaf | (uint32_t)(nz + (k * 2 + w) * ned + e));
+          for (int e = 0; e < ned; ++e) {
+            const d3 n = mk(E[2 * e], E[2 * e + 1], -s);
+            const double den = dot(n, d);
+            if (den == 0) continue;
+            const double t = (R[k] - s * Z[k] - dot(n, o)) / den, zt = o.z + t * d.z;
+            if (zt < Z[k] - tol || zt > Z[k + 1] + tol) continue;
+            xl_add(L, t, leaf | (uint32_t)(nz + (k * 2 + w) * ned + e));
+          }
         }
       }
       add_phi(L, o, d, T + RBG_TRIG_PHI, P[1], leaf);
@@ -312,7 +321,12 @@ RBG_D void prim_collect(int type, const double* P, const double* T, d3 o, d3 d, 
           double B = 2 * (o.x * d.x + o.y * d.y - s * d.z * (c0 + s * o.z));
           double C = o.x * o.x + o.y * o.y - (c0 + s * o.z) * (c0 + s * o.z);
           int m = quad_roots(A, B, C, r);
-          for (int i = 0; i < m; ++i) xl_add(L, r[i], leaf | (uint32_t)(nz + k * 2 + w));
+          const double tol = 1e-6 * (h + fabs(Z[k]) + fabs(Z[k + 1])) + 1e-9;
+          for (int i = 0; i < m; ++i) {
+            const double zt = o.z + r[i] * d.z;
+            if (zt < Z[k] - tol || zt > Z[k + 1] + tol) continue;  // not on this section's cone
+            xl_add(L, r[i], leaf | (uint32_t)(nz + k * 2 + w));
+          }
         }
       }
       add_phi(L, o, d, T + RBG_TRIG_PHI, P[1], leaf);
