@@ -39,6 +39,11 @@ CPU_SAMPLE = 200_000
 # algorithmic bytes (per ray: 40 B in + 48 B out; per segment 52 B read + 52 B write)
 BYTES_PER_RAY = 88
 BYTES_PER_SEGMENT = 104
+# DRAM bytes per ray of the mixed tracer on the Schwarzschild-Couder batch:
+# dram__bytes_read.sum + dram__bytes_write.sum of one ncu-captured launch
+# over 3e6 rays (203.8 MB + 167.1 MB); traffic grows with the ray count
+# (every byte is ray I/O), so a launch's traffic is this times its rays
+DRAM_BYTES_PER_RAY_SC = (203.792128e6 + 167.089408e6) / 3e6
 
 
 # workload name -> (default rays, description); Schwarzschild-Couder is the
@@ -423,8 +428,13 @@ def main():
             "segments_per_step": seg,
             "compaction": args.compaction or tuned,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": None, "peak_source": how,
-                         "note": "algorithmic ray-state bytes; the kernel is FP64-pipe bound, see profiles/"},
+                         "frac": achieved / hbm,
+                         "traffic": (DRAM_BYTES_PER_RAY_SC * n if args.workload == "schwarzschild_couder"
+                                     and prec == N.PREC_MIXED else None),
+                         "peak_source": how,
+                         "note": "algorithmic bytes = 88 B per ray + 104 B per segment (wavefront ray state); "
+                                 "the kernel keeps ray state in registers and is bound by the FP64 pipe "
+                                 "(64 % busy under ncu), not by HBM"},
             "e2e": e2e, "clocks": clocks, "vs_plain_fp64": compare}
     if not args.no_grad and ws == 1 and args.workload == "schwarzschild_couder":
         line["grad"] = grad_bench(batch, rays, max(1, min(args.steps, 3)), device, N, torch)
