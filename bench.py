@@ -14,7 +14,9 @@ timed region).  The CPU baseline is the FP64 oracle (the restatement of the
 reference algorithm) on all host cores over a bounded sample.  With
 --impl reference only that CPU path runs.  --workload selects one of the
 other telescope configurations (paraboloid, davies_cotton, light_guide,
-schmidt_cassegrain) at its own size.
+schmidt_cassegrain) at its own size; --workload corsika and thinfilm time
+the stages either side of the trace (CORSIKA bunch -> ray expansion, the
+20-layer thin-film stack) with their own metric.
 """
 from __future__ import annotations
 
@@ -260,6 +262,207 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------------------
+# the stages either side of the trace: CORSIKA bunch expansion (upstream)
+# and thin-film stacks (per-hit physics / coating design), one JSON line each
+# ---------------------------------------------------------------------------
+STAGES = {
+    "corsika": (10_000_000, "bunches"),
+    "thinfilm": (10_000_000, "(angle, wavelength) pairs"),
+}
+
+
+def synthetic_bunches(n, seed=11):
+    """Photon bunches with the value ranges of a CORSIKA IACT event at a
+    telescope: positions within 6 m, downward directions within 5 deg of the
+    zenith, 0.5-5 photons per bunch, half of them without a wavelength."""
+    g = np.random.default_rng(seed)
+    th = np.radians(5) * np.sqrt(g.uniform(0, 1, n))
+    ph = g.uniform(0, 2 * np.pi, n)
+    b = {"x": g.uniform(-600, 600, n), "y": g.uniform(-600, 600, n), "zem": g.uniform(5e5, 1.5e6, n),
+         "time": g.uniform(0, 30, n), "cx": np.sin(th) * np.cos(ph), "cy": np.sin(th) * np.sin(ph),
+         "cz": -np.cos(th), "lambda": np.where(g.uniform(0, 1, n) < 0.5, 0.0, g.uniform(300, 550, n)),
+         "photons": g.uniform(0.5, 5.0, n)}
+    return {k: v.astype(np.float32) for k, v in b.items()}
+
+
+def stage_line(args, name, n, metric, unit, value, ms, alg_bytes, launches, clocks, e2e, cb, extra):
+    hbm, how = peaks()
+    achieved = alg_bytes / (ms / 1e3) / 1e9
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": name, "units": n, "l2": "inputs and outputs > L2 (no flush)"},
+            "gpu_launches": launches * args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": None, "peak_source": how},
+            "e2e": e2e, "clocks": clocks, "cpu_baseline": cb}
+    line.update(extra)
+    print(json.dumps(line))
+
+
+def time_events(fn, steps, warmup, torch):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as ck:
+        e0, e1 = ev(), ev()
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, ck.summary()
+
+
+def run_corsika(args):
+    """ACorsikaIACTFile::GetRayArray (src/ACorsikaIACTFile.cxx:71-133) on
+    synthetic bunches: rays per second out of rbg_bunches_to_rays."""
+    import torch
+
+    import oracle_ref
+
+    from robast_gb300 import _native as N
+    from robast_gb300 import build
+    from robast_gb300.corsika import BUNCH_FIELDS
+    from robast_gb300.device import _ptr
+
+    build.build_library()
+    build.build_oracle()
+    nb = args.rays or STAGES["corsika"][0]
+    hb = synthetic_bunches(nb)
+    dev = {f: torch.as_tensor(hb[f]).cuda() for f in BUNCH_FIELDS}
+    fp, dp = C.POINTER(C.c_float), C.POINTER(C.c_double)
+
+    def bunches(src, ptr):
+        b = N.Bunches()
+        b.n = nb
+        for f in BUNCH_FIELDS:
+            setattr(b, "lambda_" if f == "lambda" else f, C.cast(ptr(src[f]), fp))
+        return b
+
+    db = bunches(dev, _ptr)
+    ws = torch.empty(int(N.lib().rbg_bunches_workspace_bytes(nb)), dtype=torch.uint8, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    z, tel_z, nidx, lmin, lmax, seed = 1500.0, 0.0, 1.0, 300.0, 550.0, 7
+    total = C.c_int64()
+    N.check(N.lib().rbg_bunches_to_rays(C.byref(db), z, tel_z, nidx, lmin, lmax, seed, _ptr(ws), None, 0,
+                                        C.byref(total), C.c_void_p(st)), "count")
+    m = total.value
+    names = ("x", "y", "z", "t", "dx", "dy", "dz", "lam")
+    out = {f: torch.empty(m, dtype=torch.float64, device="cuda") for f in names}
+    rs = N.Rays(m, *(C.cast(_ptr(out[f]), dp) for f in names))
+
+    def step():
+        N.check(N.lib().rbg_bunches_to_rays(C.byref(db), z, tel_z, nidx, lmin, lmax, seed, _ptr(ws), C.byref(rs), m,
+                                            C.byref(total), C.c_void_p(st)), "rbg_bunches_to_rays")
+
+    ms, clocks = time_events(step, args.steps, args.warmup, torch)
+    # end to end: bunches from pinned host memory, rays back to pinned host
+    # memory (ACorsikaIACTFile::GetRayArray returns host rays)
+    hpin = {f: torch.as_tensor(hb[f]).pin_memory() for f in BUNCH_FIELDS}
+    hout = {f: torch.empty(m, dtype=torch.float64).pin_memory() for f in names}
+
+    def e2e_step():
+        for f in BUNCH_FIELDS:
+            dev[f].copy_(hpin[f], non_blocking=True)
+        step()
+        for f in names:
+            hout[f].copy_(out[f], non_blocking=True)
+        torch.cuda.synchronize()
+
+    e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    # CPU: the oracle restatement, one thread, on the first 2e6 bunches
+    k = min(nb, 2_000_000)
+    sub = {f: hb[f][:k] for f in hb}
+    t0 = time.perf_counter()
+    ref = oracle_ref.bunches_to_rays(sub, z, tel_z, nidx, lmin, lmax, seed)
+    dt = time.perf_counter() - t0
+    n_cpu = len(ref["x"])
+    # parity of the first rays (the same Philox draws)
+    got = {f: out[f][:n_cpu].cpu().numpy() for f in names}
+    worst = max(float(np.max(np.abs(got[f] - ref[f]) / np.maximum(1.0, np.abs(ref[f])))) for f in names)
+    cb = {"value": n_cpu / dt, "unit": "rays/s", "cores": 1, "kind": "port",
+          "sample": f"first {k} of the {nb} bunches ({n_cpu} rays), oracle restatement, 1 thread"}
+    e2e = {"value": m / t_e2e, "unit": "rays/s", "h2d_bytes_per_step": nb * 4 * len(BUNCH_FIELDS),
+           "d2h_bytes_per_step": m * 8 * len(names)}
+    alg = nb * 32 + m * 64
+    stage_line(args, "corsika_bunches_to_rays", nb, "CORSIKA bunch -> ray expansion (ACorsikaIACTFile::GetRayArray)",
+               "rays/s", m / (ms / 1e3), ms, alg, 3, clocks, e2e, cb,
+               {"rays_per_step": m, "max_rel_diff_vs_oracle": worst,
+                "roofline_note": "algorithmic bytes = 32 B per bunch read + 64 B per ray written"})
+
+
+def run_thinfilm(args):
+    """AMultilayer::CoherentTMMMixed (src/AMultilayer.cxx:240-481) of the
+    20-layer TiO2/SiO2 quarter-wave stack of the Schmidt-Cassegrain
+    configuration over (angle, wavelength) pairs, and its
+    PreCalculateCoherentTMM table (include/AMultilayer.h:243-262)."""
+    import torch
+
+    import oracle_ref
+
+    from robast_gb300 import _native as N
+    from robast_gb300 import build, configs
+
+    build.build_library()
+    build.build_oracle()
+    n = args.rays or STAGES["thinfilm"][0]
+    man, _ = configs.schmidt_cassegrain(n_rays=16, n_samples=1)
+    scene = man._ensure_scene()
+    ml = 0
+    nm = 1e-7
+    g = np.random.default_rng(5)
+    th_h = g.uniform(0, np.radians(60), n)
+    lam_h = g.uniform(300 * nm, 700 * nm, n)
+    th = torch.as_tensor(th_h).cuda()
+    lam = torch.as_tensor(lam_h).cuda()
+    R_, T_ = torch.empty_like(th), torch.empty_like(th)
+    st = torch.cuda.current_stream().cuda_stream
+
+    def step():
+        N.check(N.lib().rbg_multilayer_rt(scene.handle, ml, 0, 2, n, th.data_ptr(), None, lam.data_ptr(),
+                                          R_.data_ptr(), T_.data_ptr(), C.c_void_p(st)), "rbg_multilayer_rt")
+
+    ms, clocks = time_events(step, args.steps, args.warmup, torch)
+    hin = {"th": torch.as_tensor(th_h).pin_memory(), "lam": torch.as_tensor(lam_h).pin_memory()}
+    hout = {"R": torch.empty(n, dtype=torch.float64).pin_memory(), "T": torch.empty(n, dtype=torch.float64).pin_memory()}
+
+    def e2e_step():
+        th.copy_(hin["th"], non_blocking=True)
+        lam.copy_(hin["lam"], non_blocking=True)
+        step()
+        hout["R"].copy_(R_, non_blocking=True)
+        hout["T"].copy_(T_, non_blocking=True)
+        torch.cuda.synchronize()
+
+    e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    k = 20_000
+    t0 = time.perf_counter()
+    ref = [oracle_ref.tmm(scene, ml, "mixed", th_h[i], lam_h[i]) for i in range(k)]
+    dt = time.perf_counter() - t0
+    r_gpu = R_[:k].cpu().numpy()
+    worst = float(np.max(np.abs(r_gpu - np.array([r for r, _ in ref]))))
+    cb = {"value": k / dt, "unit": "evaluations/s", "cores": 1, "kind": "port",
+          "sample": f"first {k} of the {n} pairs, oracle restatement through ctypes, 1 thread"}
+    e2e = {"value": n / t_e2e, "unit": "evaluations/s", "h2d_bytes_per_step": n * 16, "d2h_bytes_per_step": n * 16}
+    stage_line(args, "thinfilm_20layer_coherent_mixed", n,
+               "AMultilayer::CoherentTMMMixed evaluations (20-layer stack, s and p)", "evaluations/s",
+               n / (ms / 1e3), ms, n * 32, 1, clocks, e2e, cb,
+               {"max_abs_diff_R_vs_oracle": worst, "layers": 20,
+                "roofline_note": "algorithmic bytes = 16 B in + 16 B out per evaluation; the kernel is bound "
+                                 "by the FP64 pipe (complex transfer matrices), not by HBM"})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -269,13 +472,17 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-compare", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-grad", action="store_true", help="skip the gradient benchmark")
-    ap.add_argument("--workload", default="schwarzschild_couder", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="schwarzschild_couder", choices=sorted(WORKLOADS) + sorted(STAGES))
     ap.add_argument("--rays", type=int, default=0, help="rays per step (default: the workload's size)")
     ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE)
     ap.add_argument("--compaction", type=int, default=0, help="mixed tracer refill threshold (0: tuned)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "corsika":
+        return run_corsika(args)
+    if args.workload == "thinfilm":
+        return run_thinfilm(args)
 
     import torch
 

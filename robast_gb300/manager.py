@@ -80,6 +80,25 @@ class ARay:
     def IsSuspended(self):
         return self.status == ARay.kSuspend
 
+    def GetPoint(self, i):
+        """Point i (x, y, z, t); the start point is point 0."""
+        return np.array(self.points[i])
+
+    def FindNodeNumberStartWith(self, name: str) -> int:
+        """Index in the node history of the first node whose TGeoNode name
+        starts with `name`, -1 if none (src/ARay.cxx:55-64).  Node i of the
+        history was added together with point i + 1."""
+        names = getattr(self, "node_names", None) or []
+        for i, nd in enumerate(self.nodes):
+            if 0 <= nd < len(names) and names[nd].startswith(name):
+                return i
+        return -1
+
+    def FindNodeStartWith(self, name: str):
+        """Name of that node, None if none (src/ARay.cxx:42-53)."""
+        i = self.FindNodeNumberStartWith(name)
+        return None if i < 0 else self.node_names[self.nodes[i]]
+
 
 class ARayArray:
     """Batch of rays as structure-of-arrays.  After tracing, rays are binned
@@ -96,6 +115,7 @@ class ARayArray:
         self.last_node = np.full(n, -2, dtype=np.int32)
         self.hist_xyzt = None
         self.hist_node = None
+        self.node_names: List[str] = []
         self._pending: List[ARay] = []
 
     @classmethod
@@ -162,6 +182,63 @@ class ARayArray:
         self._flush()
         sel = slice(None) if idx is None else idx
         return np.stack([self.dx[sel], self.dy[sel], self.dz[sel]], axis=-1)
+
+    # -- per-ray histories (TraceNonSequential(..., history=H)) ------------
+    def _need_history(self):
+        if self.hist_node is None:
+            raise RuntimeError("no point/node history: trace with history > 0")
+
+    def GetPoint(self, i, n):
+        """Point n (x, y, z, t) of ray i; the start point is point 0.
+        Points past the traced history capacity were not kept (NaN)."""
+        self._need_history()
+        if n < 0 or n >= min(int(self.npoints[i]), self.hist_xyzt.shape[1]):
+            return np.full(4, np.nan)
+        return self.hist_xyzt[i, n].copy()
+
+    def GetNodeHistory(self, i):
+        """Physical node ids of ray i in ARay::fNodeHisotry order (node k was
+        added with point k + 1; -1 is a null node outside the top volume)."""
+        self._need_history()
+        m = min(int(self.npoints[i]), self.hist_node.shape[1])
+        return self.hist_node[i, 1:m].copy()
+
+    def FindNodeNumberStartWith(self, name: str, idx=None):
+        """ARay::FindNodeNumberStartWith for every selected ray at once
+        (src/ARay.cxx:55-64): the history index of the first node whose
+        TGeoNode name ("<volume>_<copy>") starts with `name`, -1 if none."""
+        self._need_history()
+        names = self.node_names
+        match = np.array([nm.startswith(name) for nm in names] + [False], dtype=bool)
+        sel = slice(None) if idx is None else idx
+        hn = self.hist_node[sel, 1:]
+        npts = self.npoints[sel]
+        k = np.arange(hn.shape[1])
+        valid = (k[None, :] < (npts[:, None] - 1)) & (hn >= 0)
+        hit = valid & match[np.where(valid, hn, len(names))]
+        first = np.argmax(hit, axis=1)
+        return np.where(hit.any(axis=1), first, -1).astype(np.int64)
+
+    def FindNodeStartWith(self, name: str, idx=None):
+        """Physical node id of that node per selected ray, -1 if none
+        (src/ARay.cxx:42-53 returns the TGeoNode; node_names maps ids to
+        names)."""
+        k = self.FindNodeNumberStartWith(name, idx)
+        sel = slice(None) if idx is None else idx
+        hn = self.hist_node[sel, 1:]
+        rows = np.arange(len(k))
+        return np.where(k >= 0, hn[rows, np.maximum(k, 0)], -1).astype(np.int32)
+
+    def NodeHitPoints(self, name: str, idx=None):
+        """For every selected ray whose history holds a node starting with
+        `name`: (ray index, the point recorded with that node).  The hit map
+        of tutorials/DaviesCotton.C:214-223 (GetPoint of the first
+        "mirror" node), with the point the node was added with."""
+        sel_idx = np.arange(len(self)) if idx is None else np.asarray(idx)
+        k = self.FindNodeNumberStartWith(name, sel_idx)
+        ok = k >= 0
+        rows = sel_idx[ok]
+        return rows, self.hist_xyzt[rows, k[ok] + 1]
 
     def Merge(self, other: "ARayArray"):
         self._flush()
@@ -441,6 +518,29 @@ class Scene:
             names.append(self.builder.volume_objs[self.flat.nodes[i].volume].name)
         return names
 
+    def node_root_names(self):
+        """Physical node id -> TGeoNode::GetName(), "<volume>_<copy number>"
+        (TGeoVolume::AddNode names its node so; the top node is "<top>_1").
+
+        Physical ids are the breadth-first expansion of the placements,
+        children of a node in insertion order; the copy numbers are
+        recovered by walking the same expansion."""
+        if getattr(self, "_root_names", None) is None:
+            vols = self.builder.volume_objs
+            names = [vols[self.flat.nodes[0].volume].name + "_1"]
+            copies = [None]
+            for i in range(self.flat.n_nodes):
+                nd = self.flat.nodes[i]
+                kids = vols[nd.volume].nodes
+                assert nd.child_count == len(kids)
+                for k, (child, copy_no, _, _) in enumerate(kids):
+                    cid = self.flat.children[nd.child_begin + k]
+                    assert cid == len(names)
+                    names.append(f"{child.name}_{copy_no}")
+                    copies.append(copy_no)
+            self._root_names = names
+        return self._root_names
+
     def __del__(self):
         h = getattr(self, "handle", None)
         if h is not None and h.value:
@@ -583,13 +683,20 @@ class AOpticsManager:
     def TraceNonSequential(self, rays, precision=None, history: int = 0):
         """Trace an ARayArray (in place), a single ARay, or a list of ARays."""
         if isinstance(rays, ARay):
+            # a single ray keeps its full history, as an ARay does
             arr = ARayArray()
             arr.Add(rays)
-            self.TraceNonSequential(arr, precision, history=max(history, 0))
+            cap = max(history, self.limit + 3)
+            self.TraceNonSequential(arr, precision, history=cap)
             rays.status = int(arr.status[0])
-            rays.npoints = int(arr.npoints[0])
+            rays.npoints = int(rays.npoints + arr.npoints[0] - 1)
             rays.last_node = int(arr.last_node[0])
-            rays.points.append(tuple(arr.points()[0]))
+            m = min(int(arr.npoints[0]), cap)
+            rays.points.extend(tuple(float(v) for v in arr.hist_xyzt[0, j]) for j in range(1, m))
+            if m < int(arr.npoints[0]):
+                rays.points.append(tuple(arr.points()[0]))
+            rays.nodes.extend(int(v) for v in arr.hist_node[0, 1:m])
+            rays.node_names = arr.node_names
             rays.direction = arr.directions()[0]
             return rays
         if isinstance(rays, (list, tuple)):
@@ -611,6 +718,7 @@ class AOpticsManager:
         rays.status, rays.npoints, rays.last_node = out["status"], out["npoints"], out["last_node"]
         if history:
             rays.hist_xyzt, rays.hist_node = out["hist_xyzt"], out["hist_node"]
+            rays.node_names = scene.node_root_names()
         rays.trace_status = st
         return rays
 

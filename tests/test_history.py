@@ -1,0 +1,115 @@
+"""Per-ray point/node histories and the ARay node queries
+(src/ARay.cxx:42-64, FindNodeStartWith / FindNodeNumberStartWith), used by
+the facet-hit map of tutorials/DaviesCotton.C:214-223."""
+import numpy as np
+import pytest
+
+import oracle_ref
+from robast_gb300 import (AMirror, AOpticalComponent, AOpticsManager, ARay, TGeoBBox, TGeoTranslation, configs)
+
+
+def _nested_manager():
+    man = AOpticsManager("m", "nested")
+    world = AOpticalComponent("world", TGeoBBox("w", 100, 100, 100))
+    man.SetTopVolume(world)
+    box = AOpticalComponent("holder", TGeoBBox("h", 10, 10, 10))
+    mir = AMirror("mirror", TGeoBBox("mb", 1, 1, 1))
+    box.AddNode(mir, 5, TGeoTranslation(0, 0, -2))
+    world.AddNode(box, 3, TGeoTranslation(0, 0, 0))
+    world.AddNode(box, 7, TGeoTranslation(50, 0, 0))
+    man.CloseGeometry()
+    return man
+
+
+def test_node_root_names():
+    """TGeoNode names are "<volume>_<copy>", physical ids breadth first."""
+    man = _nested_manager()
+    assert man.scene.node_root_names() == ["world_1", "holder_3", "holder_7", "mirror_5", "mirror_5"]
+
+
+def _scalar_find(hist_node, npoints, names, prefix):
+    out = np.full(len(npoints), -1, dtype=np.int64)
+    for i in range(len(npoints)):
+        for k in range(min(int(npoints[i]), hist_node.shape[1]) - 1):
+            nd = hist_node[i, k + 1]
+            if nd >= 0 and names[nd].startswith(prefix):
+                out[i] = k
+                break
+    return out
+
+
+def _dc_small(n_rays=3000):
+    return configs.davies_cotton(n_rays=n_rays, n_angles=2, n_facets=37)
+
+
+def test_find_node_number_vectorised_matches_ray_loop():
+    man, batch = _dc_small()
+    rays = configs.to_array(batch)
+    st, ref = oracle_ref.trace(man, rays, threads=4, history=8)
+    arr = configs.to_array(batch)
+    arr.status, arr.npoints, arr.last_node = ref["status"], ref["npoints"], ref["last_node"]
+    arr.hist_xyzt, arr.hist_node = ref["hist_xyzt"], ref["hist_node"]
+    arr.node_names = man.scene.node_root_names()
+    for prefix in ("mirror", "mirror_1", "focalPlane", "cameraBox", "nothing"):
+        got = arr.FindNodeNumberStartWith(prefix)
+        np.testing.assert_array_equal(got, _scalar_find(arr.hist_node, arr.npoints, arr.node_names, prefix))
+    k = arr.FindNodeNumberStartWith("mirror")
+    foc = arr.GetFocused()
+    assert len(foc) > 100
+    # every focused ray entered the world (the rays start outside it) and
+    # then reflected off a facet
+    assert (k[foc] == 1).all()
+    assert (arr.FindNodeNumberStartWith("world_1", foc) == 0).all()
+    nodes = arr.FindNodeStartWith("mirror", foc)
+    assert all(arr.node_names[nd].startswith("mirror_") for nd in nodes)
+    rows, pts = arr.NodeHitPoints("mirror")
+    assert set(foc) <= set(rows)
+    # facet hits lie on the dish: inside the 37-facet aperture and below
+    # the sagitta of its rim
+    r = np.hypot(pts[:, 0], pts[:, 1])
+    assert (r < 250).all() and (pts[:, 2] > -1).all() and (pts[:, 2] < 30).all()
+    # GetPoint / GetNodeHistory agree with the raw history
+    i = int(foc[0])
+    np.testing.assert_array_equal(arr.GetPoint(i, 1), arr.hist_xyzt[i, 1])
+    assert list(arr.GetNodeHistory(i))[1] == nodes[0]
+    assert np.isnan(arr.GetPoint(i, 50)).all()
+
+
+def test_history_required():
+    arr = ARayShooter_square()
+    with pytest.raises(RuntimeError):
+        arr.FindNodeNumberStartWith("mirror")
+
+
+def ARayShooter_square():
+    from robast_gb300 import ARayShooter
+    return ARayShooter.Square(400e-7, 10.0, 3)
+
+
+@pytest.mark.gpu
+def test_history_api_gpu_matches_oracle():
+    man, batch = _dc_small()
+    st, ref = oracle_ref.trace(man, configs.to_array(batch), threads=4, history=8)
+    arr = configs.to_array(batch)
+    man.TraceNonSequential(arr, history=8)
+    k_ref = _scalar_find(ref["hist_node"], ref["npoints"], man.scene.node_root_names(), "mirror")
+    k = arr.FindNodeNumberStartWith("mirror")
+    assert (k == k_ref).mean() >= 0.999
+    same = (k == k_ref) & (k >= 0)
+    rows, pts = arr.NodeHitPoints("mirror", np.nonzero(same)[0])
+    np.testing.assert_allclose(pts[:, :3], ref["hist_xyzt"][rows, k_ref[rows] + 1, :3], rtol=0, atol=1e-6)
+
+
+@pytest.mark.gpu
+def test_single_ray_keeps_full_history():
+    man, _ = configs.paraboloid(n_rays=4, angles=(0.0,))
+    ray = ARay(0, 400e-7, 30.0, 0.0, 1600.0, 0.0, 0.0, 0.0, -1.0)
+    man.TraceNonSequential(ray)
+    assert ray.IsFocused()
+    assert len(ray.points) == ray.GetNpoints() == len(ray.nodes) + 1
+    assert ray.FindNodeStartWith("mirror") == "mirror_1"
+    k = ray.FindNodeNumberStartWith("mirror")
+    assert k >= 0 and ray.FindNodeNumberStartWith("focal") > k
+    # the mirror hit is on the paraboloid z = r^2 / 4f below the focus
+    x, y, z, _ = ray.GetPoint(k + 1)
+    assert abs(z - (x * x + y * y) / (4 * 800.0)) < 1e-3
