@@ -378,8 +378,10 @@ int rbg_corsika_get_bunches(const rbg_corsika* file, int32_t tel, int32_t array,
  * upper wavelength (:125).  Rays go to DEVICE arrays `out` of capacity
  * `capacity` (out->n is set); *n_rays receives the count.  With out == NULL
  * or too small a capacity only *n_rays is set (RBG_ERR_TOO_LARGE for the
- * latter).  `workspace` is a DEVICE buffer of rbg_bunches_workspace_bytes(n)
- * bytes; nothing is allocated.  Synchronises `stream`. */
+ * latter).  At most 2^31 - 1 bunches per call, and a bunch counts at most
+ * 2^32 rays.  `workspace` is a DEVICE buffer of
+ * rbg_bunches_workspace_bytes(n) bytes; nothing is allocated.  Synchronises
+ * `stream`. */
 size_t rbg_bunches_workspace_bytes(int64_t n_bunches);
 int rbg_bunches_to_rays(const rbg_bunches* b, double z, double tel_z, double refractive_index,
                         double lambda_min, double lambda_max, uint64_t seed, void* workspace,

@@ -6,8 +6,12 @@
 //   1. per tile of kTile bunches: photon counts, their exclusive scan
 //      inside the tile (shared memory) and the tile total;
 //   2. one block: exclusive scan of the tile totals, and the grand total;
-//   3. one thread per output ray: binary search of its bunch in the
-//      global offsets, back-projection, write (coalesced).
+//   3. one warp per 32 consecutive bunches: each lane back-projects its
+//      bunch once (the reference's per-bunch quantities, :112-117), a warp
+//      scan of the ray counts places the warp's rays, and the lanes then
+//      write those rays 32 at a time, each taking its bunch's values from
+//      the owning lane by shuffle (a 5-step search over the warp scan), so
+//      every store of a field is 32 consecutive doubles.
 // All scratch lives in the caller's workspace.
 #include <cuda_runtime.h>
 
@@ -24,10 +28,15 @@ constexpr double kSpeedOfLightCm = 2.99792458e10;
 constexpr double kNs = 1e-9;  // s
 constexpr double kNm = 1e-7;  // cm
 
+constexpr float kMaxBunchRays = 4294967296.f;  // 2^32
+
 __device__ __forceinline__ int64_t bunch_rays(float photons) {
   // j < photons for j = 0, 1, ...: ceil(photons) iterations; none for
-  // photons <= 0 or NaN
-  return photons > 0.f ? (int64_t)ceilf(photons) : 0;
+  // photons <= 0 or NaN.  Counts are capped at 2^32 (with at most 2^31
+  // bunches the sum stays below 2^63; such a total then exceeds any
+  // capacity and the call fails instead of writing)
+  if (!(photons > 0.f)) return 0;
+  return photons >= kMaxBunchRays ? (int64_t)kMaxBunchRays : (int64_t)ceilf(photons);
 }
 
 __global__ void __launch_bounds__(kTile) count_scan_kernel(const float* photons, int64_t n, int64_t* offsets,
@@ -73,40 +82,72 @@ __global__ void __launch_bounds__(kTile) tile_scan_kernel(int64_t* tile_sum, int
   if (threadIdx.x == 0) tile_sum[ntiles] = carry;
 }
 
-__global__ void expand_kernel(rbg_bunches b, const int64_t* offsets, const int64_t* tile_off, int64_t total,
-                              double z, double tel_z, double speed, double inv_lmin, double inv_lmax,
-                              uint64_t seed, double* x, double* y, double* zz, double* t, double* dx, double* dy,
-                              double* dz, double* lam) {
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= total) return;
-  // last bunch i whose global offset is <= r (bunches of zero rays share
-  // their successor's offset; the search skips them)
-  int64_t lo = 0, hi = b.n - 1;
-  while (lo < hi) {
-    const int64_t mid = (lo + hi + 1) >> 1;
-    const int64_t off = tile_off[mid / kTile] + offsets[mid];
-    if (off <= r) lo = mid;
-    else hi = mid - 1;
+constexpr int kExpandThreads = 256;
+
+__global__ void __launch_bounds__(kExpandThreads)
+    expand_kernel(rbg_bunches b, const int64_t* offsets, const int64_t* tile_off, double z, double tel_z,
+                  double speed, double inv_lmin, double inv_lmax, uint64_t seed, double* x, double* y, double* zz,
+                  double* t, double* dx, double* dy, double* dz, double* lam) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int64_t first = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) << 5;
+  if (first >= b.n) return;  // warp-uniform
+  const int64_t i = first + lane;
+  const bool valid = i < b.n;
+  const int64_t c = valid ? bunch_rays(b.photons[i]) : 0;
+  // inclusive scan of the warp's ray counts
+  int64_t incl = c;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int64_t v = __shfl_up_sync(full, incl, d);
+    if (lane >= d) incl += v;
   }
-  const int64_t i = lo;
-  const double cx = b.cx[i], cy = b.cy[i], cz = b.cz[i];
-  // air-mass back-projection to height z (:112-117)
-  const double airmass = -1. / cz;
-  const double tel_dist = (z - tel_z) * airmass;
-  double l = b.lambda[i];
-  if (l == 0) {
-    RayRng g;
-    g.init(seed, (uint64_t)r, 2u);
-    l = 1. / (inv_lmin - g.uniform() * (inv_lmin - inv_lmax));
+  const int64_t wtotal = __shfl_sync(full, incl, 31);
+  // global offset of the warp's first ray (kTile is a multiple of 32, so
+  // the warp's bunches share one tile)
+  const int64_t base = tile_off[first / kTile] + offsets[first];
+  // this lane's bunch, back-projected to height z (:112-117)
+  double px = 0, py = 0, pt = 0, cx = 0, cy = 0, cz = 0, l = 0;
+  if (c > 0) {
+    cx = b.cx[i];
+    cy = b.cy[i];
+    cz = b.cz[i];
+    const double airmass = -1. / cz;
+    const double tel_dist = (z - tel_z) * airmass;
+    px = (double)b.x[i] - tel_dist * cx;
+    py = (double)b.y[i] - tel_dist * cy;
+    pt = (double)b.time[i] * kNs - tel_dist / speed;
+    l = b.lambda[i];
   }
-  x[r] = (double)b.x[i] - tel_dist * cx;
-  y[r] = (double)b.y[i] - tel_dist * cy;
-  zz[r] = z;
-  t[r] = (double)b.time[i] * kNs - tel_dist / speed;
-  dx[r] = cx;
-  dy[r] = cy;
-  dz[r] = cz;
-  lam[r] = l * kNm;
+  for (int64_t r0 = 0; r0 < wtotal; r0 += 32) {
+    const int64_t rl = r0 + lane;
+    // owning lane: the number of lanes whose inclusive count is <= rl
+    int s = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+      const int64_t v = __shfl_sync(full, incl, s + step - 1);
+      if (v <= rl) s += step;
+    }
+    const double vx = __shfl_sync(full, px, s), vy = __shfl_sync(full, py, s), vt = __shfl_sync(full, pt, s);
+    const double vcx = __shfl_sync(full, cx, s), vcy = __shfl_sync(full, cy, s), vcz = __shfl_sync(full, cz, s);
+    double vl = __shfl_sync(full, l, s);
+    if (rl < wtotal) {
+      const int64_t r = base + rl;
+      if (vl == 0) {
+        RayRng g;
+        g.init(seed, (uint64_t)r, 2u);
+        vl = 1. / (inv_lmin - g.uniform() * (inv_lmin - inv_lmax));
+      }
+      x[r] = vx;
+      y[r] = vy;
+      zz[r] = z;
+      t[r] = vt;
+      dx[r] = vcx;
+      dy[r] = vcy;
+      dz[r] = vcz;
+      lam[r] = vl * kNm;
+    }
+  }
 }
 
 }  // namespace
@@ -134,8 +175,8 @@ extern "C" int rbg_bunches_to_rays(const rbg_bunches* b, double z, double tel_z,
   if (!(lambda_min > 0) || !(lambda_max > 0)) return RBG_ERR_ARG;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int64_t n = b->n;
+  if (n > 0x7fffffff) return RBG_ERR_TOO_LARGE;
   const int64_t ntiles = (n + kTile - 1) / kTile;
-  if (ntiles > 0x7fffffff) return RBG_ERR_TOO_LARGE;
   int64_t* offsets = static_cast<int64_t*>(workspace);
   int64_t* tile_sum = offsets + n;
   count_scan_kernel<<<(unsigned)ntiles, kTile, 0, st>>>(b->photons, n, offsets, tile_sum);
@@ -151,11 +192,11 @@ extern "C" int rbg_bunches_to_rays(const rbg_bunches* b, double z, double tel_z,
   if (total > 0) {
     if (!out->x || !out->y || !out->z || !out->t || !out->dx || !out->dy || !out->dz || !out->lambda)
       return RBG_ERR_ARG;
-    const int threads = 256;
-    const int64_t blocks = (total + threads - 1) / threads;
+    // one warp per 32 bunches
+    const int64_t blocks = (n + kExpandThreads - 1) / kExpandThreads;
     if (blocks > 0x7fffffff) return RBG_ERR_TOO_LARGE;
-    expand_kernel<<<(unsigned)blocks, threads, 0, st>>>(
-        *b, offsets, tile_sum, total, z, tel_z, kSpeedOfLightCm / refractive_index, 1. / lambda_min,
+    expand_kernel<<<(unsigned)blocks, kExpandThreads, 0, st>>>(
+        *b, offsets, tile_sum, z, tel_z, kSpeedOfLightCm / refractive_index, 1. / lambda_min,
         1. / lambda_max, seed, const_cast<double*>(out->x), const_cast<double*>(out->y), const_cast<double*>(out->z),
         const_cast<double*>(out->t), const_cast<double*>(out->dx), const_cast<double*>(out->dy),
         const_cast<double*>(out->dz), const_cast<double*>(out->lambda));

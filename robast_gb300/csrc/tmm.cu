@@ -20,6 +20,14 @@ namespace {
 RBG_D void stack_rt(const DevScene& S, int ml, int mode, int pol, cplxT<double> th, double lam, double& R,
                     double& T) {
   const rbg_multilayer_desc& M = S.multilayers[ml];
+  if (mode == 0 && pol == 2) {
+    // both polarisations in one pass, summed p then s as the loop below
+    double r[2], t[2];
+    tmm_coherent_n<double, 2>(S, M.layer_offset, 0, M.n_layers, 1, 0, th, lam, r, t);
+    R = (r[1] + r[0]) / 2.;
+    T = (t[1] + t[0]) / 2.;
+    return;
+  }
   R = 0;
   T = 0;
   const int first = pol == 2 ? 1 : pol, last = pol == 2 ? 0 : pol;

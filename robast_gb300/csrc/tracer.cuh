@@ -578,79 +578,112 @@ RBG_D bool is_forward_angle(cplxT<T> n, cplxT<T> th) {
   return nc.re > 0;
 }
 
-// AMultilayer::CoherentTMM (src/AMultilayer.cxx:240-481), pol 0 = s, 1 = p,
-// in precision T, for the m media S.layers[base + a + k dir], k = 0..m-1
-// (dir = +1 front to back, -1 reversed as CoherentTMM's `reverse`), light
-// incident from medium k = 0 at the (possibly complex) angle th0.  The
-// transfer-matrix product is built on the fly, front to back.
-template <typename T>
-RBG_D void tmm_coherent(const DevScene& S, int base, int a, int m, int dir, int pol, cplxT<T> th0, double lam,
-                        double& R, double& Tr) {
+// AMultilayer::CoherentTMM (src/AMultilayer.cxx:240-481) in precision T,
+// for the m media S.layers[base + a + k dir], k = 0..m-1 (dir = +1 front to
+// back, -1 reversed as CoherentTMM's `reverse`), light incident from medium
+// k = 0 at the (possibly complex) angle th0.  The transfer-matrix product is
+// built on the fly, front to back.  NP = 1 evaluates polarisation `pol1`
+// (0 = s, 1 = p) into R[0], Tr[0]; NP = 2 evaluates s into [0] and p into
+// [1] in one pass: the indices, Snell angles, cosines and phase factors of
+// the layers do not depend on the polarisation and are computed once, the
+// interface coefficients and the two matrix products per polarisation
+// (CoherentTMMMixed, include/AMultilayer.h:114-132, calls CoherentTMM once
+// per polarisation and so evaluates them twice).
+template <typename T, int NP>
+RBG_D void tmm_coherent_n(const DevScene& S, int base, int a, int m, int dir, int pol1, cplxT<T> th0, double lam,
+                          double* R, double* Tr) {
   typedef cplxT<T> C;
   auto layer = [&](int k) -> const rbg_layer_desc& { return S.layers[base + a + k * dir]; };
   auto nidx = [&](int k) {
     const rbg_layer_desc& L = layer(k);
     return cx<T>((T)index_n(S, L.index, lam), (T)index_k(S, L.index, lam));
   };
+  auto pol_of = [&](int q) { return NP == 2 ? q : pol1; };
   const T pi = T(kPi);
   C n0 = nidx(0);
   C n0s = n0 * csin_(th0);
   // ListSnell (:178-209): the first and the last angle are the forward ones
   C th_first = casin_(cdiv(n0s, n0));
   if (!is_forward_angle(n0, th_first)) th_first = cx<T>(pi) - th_first;
-  C a00 = cx<T>(1), a01 = cx<T>(0), a10 = cx<T>(0), a11 = cx<T>(1);
+  C a00[NP], a01[NP], a10[NP], a11[NP], r0[NP], t0[NP];
+#pragma unroll
+  for (int q = 0; q < NP; ++q) {
+    a00[q] = cx<T>(1);
+    a01[q] = cx<T>(0);
+    a10[q] = cx<T>(0);
+    a11[q] = cx<T>(1);
+    r0[q] = cx<T>(0);
+    t0[q] = cx<T>(1);
+  }
   C n_prev = n0, ct_prev = ccos_(th_first);
-  C r0 = cx<T>(0), t0 = cx<T>(1);
   for (int i = 1; i < m; ++i) {
     C ni = nidx(i);
     C thi = casin_(cdiv(n0s, ni));
     if (i == m - 1 && !is_forward_angle(ni, thi)) thi = cx<T>(pi) - thi;
     C cti = ccos_(thi);
-    // interface (i-1) -> i, interface_rt (:26-56)
-    C ii = n_prev * ct_prev, r, t;
-    if (pol == 0) {
-      C ff = ni * cti;
-      r = cdiv(ii - ff, ii + ff);
-      t = cdiv(T(2) * ii, ii + ff);
-    } else {
-      C fi = ni * ct_prev, iff = n_prev * cti;
-      r = cdiv(fi - iff, fi + iff);
-      t = cdiv(T(2) * ii, fi + iff);
-    }
-    if (i == 1) {
-      r0 = r;
-      t0 = t;
-    } else {
-      // layer i-1: (1/t) diag(e^{-i delta}, e^{i delta}) [[1, r],[r, 1]]
+    C ii = n_prev * ct_prev;
+    // phase of layer i-1 (not for the incidence medium)
+    C em = cx<T>(1), ep = cx<T>(1);
+    if (i > 1) {
       C kz = (T(2) * pi / (T)lam) * (n_prev * ct_prev);
       C delta = (T)layer(i - 1).thickness * kz;
       if (delta.im > 35) delta.im = 35;
-      C em = cexp_(C{delta.im, -delta.re});
-      C ep = cexp_(C{-delta.im, delta.re});
-      C it = cdiv(cx<T>(1), t);
-      C m00 = em * it, m01 = em * r * it, m10 = ep * r * it, m11 = ep * it;
-      C na = a00 * m00 + a01 * m10, nb = a00 * m01 + a01 * m11;
-      C nc = a10 * m00 + a11 * m10, nd = a10 * m01 + a11 * m11;
-      a00 = na;
-      a01 = nb;
-      a10 = nc;
-      a11 = nd;
+      em = cexp_(C{delta.im, -delta.re});
+      ep = cexp_(C{-delta.im, delta.re});
+    }
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      // interface (i-1) -> i, interface_rt (:26-56)
+      C r, t;
+      if (pol_of(q) == 0) {
+        C ff = ni * cti;
+        r = cdiv(ii - ff, ii + ff);
+        t = cdiv(T(2) * ii, ii + ff);
+      } else {
+        C fi = ni * ct_prev, iff = n_prev * cti;
+        r = cdiv(fi - iff, fi + iff);
+        t = cdiv(T(2) * ii, fi + iff);
+      }
+      if (i == 1) {
+        r0[q] = r;
+        t0[q] = t;
+      } else {
+        // layer i-1: (1/t) diag(e^{-i delta}, e^{i delta}) [[1, r],[r, 1]]
+        C it = cdiv(cx<T>(1), t);
+        C m00 = em * it, m01 = em * r * it, m10 = ep * r * it, m11 = ep * it;
+        C na = a00[q] * m00 + a01[q] * m10, nb = a00[q] * m01 + a01[q] * m11;
+        C nc = a10[q] * m00 + a11[q] * m10, nd = a10[q] * m01 + a11[q] * m11;
+        a00[q] = na;
+        a01[q] = nb;
+        a10[q] = nc;
+        a11[q] = nd;
+      }
     }
     n_prev = ni;
     ct_prev = cti;
   }
-  // prepend the first interface: (1/t0) [[1, r0],[r0, 1]] * Mtilde
-  C it0 = cdiv(cx<T>(1), t0);
-  C A = (a00 + r0 * a10) * it0, Cc = (r0 * a00 + a10) * it0;
-  C rr = cdiv(Cc, A), tt = cdiv(cx<T>(1), A);
-  T ar = cabs_(rr);
-  R = (double)(ar * ar);
   // transmitted power with the incident angle th0 itself (:466-479)
   C ct0 = ccos_(th0);
   C nf = n_prev, ctf = ct_prev;
-  T tt2 = cabs_(tt * tt);
-  if (pol == 0) Tr = (double)(tt2 * ((nf * ctf).re / (n0 * ct0).re));
-  else Tr = (double)(tt2 * ((nf * C{ctf.re, -ctf.im}).re / (n0 * C{ct0.re, -ct0.im}).re));
+#pragma unroll
+  for (int q = 0; q < NP; ++q) {
+    // prepend the first interface: (1/t0) [[1, r0],[r0, 1]] * Mtilde
+    C it0 = cdiv(cx<T>(1), t0[q]);
+    C A = (a00[q] + r0[q] * a10[q]) * it0, Cc = (r0[q] * a00[q] + a10[q]) * it0;
+    C rr = cdiv(Cc, A), tt = cdiv(cx<T>(1), A);
+    T ar = cabs_(rr);
+    R[q] = (double)(ar * ar);
+    T tt2 = cabs_(tt * tt);
+    if (pol_of(q) == 0) Tr[q] = (double)(tt2 * ((nf * ctf).re / (n0 * ct0).re));
+    else Tr[q] = (double)(tt2 * ((nf * C{ctf.re, -ctf.im}).re / (n0 * C{ct0.re, -ct0.im}).re));
+  }
+}
+
+// one polarisation, pol 0 = s, 1 = p
+template <typename T>
+RBG_D void tmm_coherent(const DevScene& S, int base, int a, int m, int dir, int pol, cplxT<T> th0, double lam,
+                        double& R, double& Tr) {
+  tmm_coherent_n<T, 1>(S, base, a, m, dir, pol, th0, lam, &R, &Tr);
 }
 
 template <typename T>
@@ -794,16 +827,12 @@ RBG_D void coherent_tmm_mixed(const DevScene& S, int ml, double th0, double lam,
     T = th2_interpolate(tab + cells, M.lam_nbins, M.lam_min, M.lam_max, M.th_nbins, M.th_min, M.th_max, lam, th0);
     return;
   }
-  double rp, tp, rs, ts;
-  if (MIXED) {
-    coherent_tmm<float>(S, ml, 1, th0, lam, rp, tp);
-    coherent_tmm<float>(S, ml, 0, th0, lam, rs, ts);
-  } else {
-    coherent_tmm<double>(S, ml, 1, th0, lam, rp, tp);
-    coherent_tmm<double>(S, ml, 0, th0, lam, rs, ts);
-  }
-  R = (rp + rs) / 2.;
-  T = (tp + ts) / 2.;
+  // [0] = s, [1] = p
+  double r[2], t[2];
+  if (MIXED) tmm_coherent_n<float, 2>(S, M.layer_offset, 0, M.n_layers, 1, 0, cx<float>((float)th0), lam, r, t);
+  else tmm_coherent_n<double, 2>(S, M.layer_offset, 0, M.n_layers, 1, 0, cx<double>(th0), lam, r, t);
+  R = (r[1] + r[0]) / 2.;
+  T = (t[1] + t[0]) / 2.;
 }
 
 // --------------------------------------------------------------------

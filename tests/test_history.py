@@ -103,7 +103,8 @@ def test_history_api_gpu_matches_oracle():
 @pytest.mark.gpu
 def test_single_ray_keeps_full_history():
     man, _ = configs.paraboloid(n_rays=4, angles=(0.0,))
-    ray = ARay(0, 400e-7, 30.0, 0.0, 1600.0, 0.0, 0.0, 0.0, -1.0)
+    # outside the 30 cm obscuration disk in front of the focal plane
+    ray = ARay(0, 400e-7, 50.0, 0.0, 1600.0, 0.0, 0.0, 0.0, -1.0)
     man.TraceNonSequential(ray)
     assert ray.IsFocused()
     assert len(ray.points) == ray.GetNpoints() == len(ray.nodes) + 1
