@@ -21,6 +21,9 @@ constexpr double kBig = RBG_BIG;
 constexpr int kMaxNodes = 1 << 24;
 constexpr int kMaxDepth = 64;
 constexpr int kBvhLeaf = 4;
+// SAH splits only while the tree stays shallower than this (the device
+// traverses with a 32-entry stack)
+constexpr int kBvhSahDepth = 28;
 constexpr int kBvhMinChildren = 9;
 constexpr int kMaxCompositeDepth = 6;
 
@@ -490,9 +493,22 @@ struct Builder {
     return RBG_OK;
   }
 
-  // Binary BVH over item ids [b, e) of `items`, median split on the widest
-  // centroid axis.  Returns the index of the created BVH node.
-  int bvh_build(std::vector<int>& items, int b, int e) {
+  // Binary BVH over item ids [b, e) of `items`.  Splits minimise the
+  // surface-area cost SA(left) n_left + SA(right) n_right over every
+  // centroid-sorted split on each axis (SAH, full sweep).  A median split on
+  // the widest centroid axis would cut a telescope's mirror field into
+  // rings when a camera far above it stretches the z extent: every ring box
+  // spans the whole dish and a vertical ray then overlaps most leaves.
+  // Where the remaining items might not fit the device's 32-entry
+  // traversal stack under further unbalanced splits, the median split
+  // (depth log2 of the items) takes over.  Returns the created node's index.
+  static double box_area(const double* lo, const double* hi) {
+    const double x = std::max(0.0, hi[0] - lo[0]), y = std::max(0.0, hi[1] - lo[1]),
+                 z = std::max(0.0, hi[2] - lo[2]);
+    return 2.0 * (x * y + y * z + z * x);
+  }
+
+  int bvh_build(std::vector<int>& items, int b, int e, int depth = 0) {
     rbg_bvh_node bn{};
     double lo[3] = {kBig, kBig, kBig}, hi[3] = {-kBig, -kBig, -kBig};
     double clo[3] = {kBig, kBig, kBig}, chi[3] = {-kBig, -kBig, -kBig};
@@ -515,25 +531,63 @@ struct Builder {
     }
     int self = (int)s->bvh.size();
     s->bvh.push_back(bn);
-    if (e - b <= kBvhLeaf) {
+    const int n = e - b;
+    if (n <= kBvhLeaf) {
       s->bvh[self].left = -1;
-      s->bvh[self].right = e - b;
+      s->bvh[self].right = n;
       s->bvh[self].item_begin = (int)s->bvh_items.size();
       for (int i = b; i < e; ++i) s->bvh_items.push_back(items[i]);
       return self;
     }
-    int axis = 0;
-    for (int k = 1; k < 3; ++k)
-      if (chi[k] - clo[k] > chi[axis] - clo[axis]) axis = k;
-    int mid = (b + e) / 2;
-    std::nth_element(items.begin() + b, items.begin() + mid, items.begin() + e, [&](int x, int y) {
-      const rbg_node& nx = s->nodes[x];
-      const rbg_node& ny = s->nodes[y];
-      double cx = nx.lo[axis] + nx.hi[axis], cy = ny.lo[axis] + ny.hi[axis];
-      return cx < cy || (cx == cy && x < y);
-    });
-    int l = bvh_build(items, b, mid);
-    int r = bvh_build(items, mid, e);
+    auto by_axis = [&](int axis) {
+      return [&, axis](int x, int y) {
+        const rbg_node& nx = s->nodes[x];
+        const rbg_node& ny = s->nodes[y];
+        double cx = nx.lo[axis] + nx.hi[axis], cy = ny.lo[axis] + ny.hi[axis];
+        return cx < cy || (cx == cy && x < y);
+      };
+    };
+    int median_depth = 0;
+    for (int m = n; m > kBvhLeaf; m = (m + 1) / 2) ++median_depth;
+    int axis = 0, mid = (b + e) / 2;
+    if (depth + 1 + median_depth < kBvhSahDepth) {
+      double best_cost = std::numeric_limits<double>::infinity();
+      std::vector<double> right_area(n);
+      for (int k = 0; k < 3; ++k) {
+        if (!(chi[k] > clo[k])) continue;
+        std::sort(items.begin() + b, items.begin() + e, by_axis(k));
+        double rlo[3] = {kBig, kBig, kBig}, rhi[3] = {-kBig, -kBig, -kBig};
+        for (int i = n - 1; i > 0; --i) {
+          const rbg_node& nd = s->nodes[items[b + i]];
+          for (int q = 0; q < 3; ++q) {
+            rlo[q] = std::min(rlo[q], nd.lo[q]);
+            rhi[q] = std::max(rhi[q], nd.hi[q]);
+          }
+          right_area[i] = box_area(rlo, rhi);
+        }
+        double llo[3] = {kBig, kBig, kBig}, lhi[3] = {-kBig, -kBig, -kBig};
+        for (int i = 1; i < n; ++i) {
+          const rbg_node& nd = s->nodes[items[b + i - 1]];
+          for (int q = 0; q < 3; ++q) {
+            llo[q] = std::min(llo[q], nd.lo[q]);
+            lhi[q] = std::max(lhi[q], nd.hi[q]);
+          }
+          const double cost = box_area(llo, lhi) * i + right_area[i] * (n - i);
+          if (cost < best_cost) {
+            best_cost = cost;
+            axis = k;
+            mid = b + i;
+          }
+        }
+      }
+      std::sort(items.begin() + b, items.begin() + e, by_axis(axis));
+    } else {
+      for (int k = 1; k < 3; ++k)
+        if (chi[k] - clo[k] > chi[axis] - clo[axis]) axis = k;
+      std::nth_element(items.begin() + b, items.begin() + mid, items.begin() + e, by_axis(axis));
+    }
+    int l = bvh_build(items, b, mid, depth + 1);
+    int r = bvh_build(items, mid, e, depth + 1);
     s->bvh[self].left = l;
     s->bvh[self].right = r;
     s->bvh[self].item_begin = -1;
