@@ -190,7 +190,18 @@ RBG_D int first_child_containing_f(const DevScene& S, int k, d3 p, f3 pf) {
     }
     return -1;
   }
+  // collect the daughters whose float boxes hold the point, then run the
+  // shape tests over the list (the lanes of a warp test candidate j
+  // together); the lowest containing id wins whatever the order
+  constexpr int kCand = 8;
+  int cand[kCand];
+  int nc = 0;
   int best = -1;
+  auto test = [&](int c) {
+    if ((best < 0 || c < best) &&
+        shape_contains_f<F>(S, S.nodes[c].shape, local_point(S, c, p, pf), S.aux[c].flags & RBG_AUX_ASPH_TWIN_FACES))
+      best = c;
+  };
   int stack[32];
   int sp = 0;
   stack[sp++] = N.bvh_root;
@@ -199,14 +210,20 @@ RBG_D int first_child_containing_f(const DevScene& S, int k, d3 p, f3 pf) {
     if (!in_fbox3(b.lo, b.hi, pf)) continue;
     if (b.left < 0) {
       for (int i = 0; i < b.right; ++i) {
-        int c = S.bvh_items[b.item_begin + i];
-        if ((best < 0 || c < best) && node_contains_f<F>(S, c, p, pf)) best = c;
+        const int c = S.bvh_items[b.item_begin + i];
+        if (!in_fbox3(S.aux[c].lo, S.aux[c].hi, pf)) continue;
+        if (nc == kCand) {
+          for (int j = 0; j < kCand; ++j) test(cand[j]);
+          nc = 0;
+        }
+        cand[nc++] = c;
       }
     } else if (sp + 2 <= 32) {
       stack[sp++] = b.left;
       stack[sp++] = b.right;
     }
   }
+  for (int j = 0; j < nc; ++j) test(cand[j]);
   return best;
 }
 
@@ -421,6 +438,16 @@ RBG_D int find_next_boundary_and_step_f(const DevScene& S, Nav& nv, double& step
         }
       }
     } else {
+      // two phases: the traversal only collects the daughters whose boxes
+      // the segment reaches, then the shape distances run over the list.
+      // Lanes whose traversals take different turns thus still call the
+      // (FP64, often composite) distance together, candidate j at once,
+      // instead of one lane at a time from inside the loop.  visit re-checks
+      // each box against the distance found so far; the lowest-id tie rule
+      // makes the result independent of the order.
+      constexpr int kCand = 8;
+      int cand[kCand];
+      int nc = 0;
       int stack[32];
       int sp = 0;
       stack[sp++] = N.bvh_root;
@@ -428,7 +455,16 @@ RBG_D int find_next_boundary_and_step_f(const DevScene& S, Nav& nv, double& step
         const rbg_bvh_node& b = S.bvh[stack[--sp]];
         if (!reach(b.lo, b.hi)) continue;
         if (b.left < 0) {
-          for (int i = 0; i < b.right; ++i) visit(S.bvh_items[b.item_begin + i]);
+          for (int i = 0; i < b.right; ++i) {
+            const int k = S.bvh_items[b.item_begin + i];
+            const rbg_node_aux& A = S.aux[k];
+            if (!reach(A.lo, A.hi)) continue;
+            if (nc == kCand) {
+              for (int j = 0; j < kCand; ++j) visit(cand[j]);
+              nc = 0;
+            }
+            cand[nc++] = k;
+          }
         } else if (sp + 2 <= 32) {
           stack[sp++] = b.right;
           stack[sp++] = b.left;
@@ -436,6 +472,7 @@ RBG_D int find_next_boundary_and_step_f(const DevScene& S, Nav& nv, double& step
           err |= ERR_BIT_CAP;
         }
       }
+      for (int j = 0; j < nc; ++j) visit(cand[j]);
     }
     if (lazy && !(enter && best < (double)exit_lo)) {
       d3 en = mk(0, 0, 1);
@@ -924,6 +961,42 @@ RBG_D d3 rotate_uz(d3 v, d3 u) {
 }
 
 // GetFacetNormal (:250-301)
+// The rejection sampling of GetFacetNormal (src/AOpticsManager.cxx:266-298,
+// after G4OpBoundaryProcess): alpha ~ N(0, sigma) accepted when
+// U * min(1, 4 sigma) <= sin(alpha) < 1, phi uniform, the facet normal
+// rotated onto `normal`, repeated while it faces away from `dir`.  Out of
+// line: it runs only on rough reflections, and its FP64 transcendentals
+// would otherwise enlarge every trace kernel.  Draws advance `rng`; after
+// RBG_ROUGH_MAX_TRIES rejections `normal` is returned with ERR_BIT_CAP.
+RBG_NOINLINE d3 sample_facet_normal(d3 normal, d3 dir, double sigma, RayRng& rng, unsigned& err) {
+  const double f_max = fmin(1., 4. * sigma);
+  int tries = 0;
+  for (;;) {
+    double alpha;
+    for (;;) {
+      const Philox4 g = rng.next();
+      const double a = u53(g.v[0], g.v[1]), c = u53(g.v[2], g.v[3]);
+      alpha = sigma * sqrt(-2.0 * log(1.0 - a)) * cos(2.0 * kPi * c);
+      const double u = f_max * rng.uniform();
+      if (!(u > sin(alpha) || alpha >= kPi / 2)) break;
+      if (++tries > RBG_ROUGH_MAX_TRIES) {
+        err |= ERR_BIT_CAP;
+        return normal;
+      }
+    }
+    const double phi = 2 * kPi * rng.uniform();
+    double sa, ca, sp, cp;
+    sincos(alpha, &sa, &ca);
+    sincos(phi, &sp, &cp);
+    const d3 facet = rotate_uz(mk(sa * cp, sa * sp, ca), normal);
+    if (dot(dir, facet) > 0.0) return facet;
+    if (++tries > RBG_ROUGH_MAX_TRIES) {
+      err |= ERR_BIT_CAP;
+      return normal;
+    }
+  }
+}
+
 template <bool MIXED, unsigned F = kFeatAll>
 RBG_D d3 get_facet_normal(const DevScene& S, const Nav& nv, Ray& r, int cur, int next) {
   d3 normal = find_normal<MIXED, F>(S, nv);
@@ -933,31 +1006,7 @@ RBG_D d3 get_facet_normal(const DevScene& S, const Nav& nv, Ray& r, int cur, int
   const rbg_border_desc B = S.borders[bi];
   if (B.lambertian) return normal;
   if (B.sigma == 0) return normal;
-  const double sigma = B.sigma;
-  const double f_max = fmin(1., 4. * sigma);
-  int tries = 0;
-  for (;;) {
-    double alpha;
-    for (;;) {
-      alpha = rng_gaus(r, sigma);
-      double u = f_max * rng_u(r);
-      if (!(u > sin(alpha) || alpha >= kPi / 2)) break;
-      if (++tries > RBG_ROUGH_MAX_TRIES) {
-        r.err |= ERR_BIT_CAP;
-        return normal;
-      }
-    }
-    double phi = 2 * kPi * rng_u(r);
-    double sa, ca, sp, cp;
-    sincos(alpha, &sa, &ca);
-    sincos(phi, &sp, &cp);
-    d3 facet = rotate_uz(mk(sa * cp, sa * sp, ca), normal);
-    if (dot(nv.d, facet) > 0.0) return facet;
-    if (++tries > RBG_ROUGH_MAX_TRIES) {
-      r.err |= ERR_BIT_CAP;
-      return normal;
-    }
-  }
+  return sample_facet_normal(normal, nv.d, B.sigma, r.rng, r.err);
 }
 
 // TGeoRotation(phi, theta, psi) in degrees applied to v
