@@ -300,8 +300,17 @@ typedef struct {
    * (rbg_scene_autotune), else the library default.  Results do not depend
    * on it. */
   int32_t compaction;
-  int32_t reserved;       /* 0 */
+  /* mixed tracer: the order in which the rays are taken up.
+   * RBG_ORDER_SPATIAL (default) groups the rays of each chunk of 2^20 or
+   * more consecutive rays by a 3D Morton cell of their start point, so the
+   * lanes of a warp follow neighbouring paths; RBG_ORDER_INPUT takes them
+   * in input order.  Every ray keeps its index for its inputs, outputs and
+   * random draws: results do not depend on it.  Batches under 2^14 rays,
+   * and rbg_trace_noalloc, always use input order. */
+  int32_t ray_order;
 } rbg_trace_opts;
+
+enum { RBG_ORDER_SPATIAL = 0, RBG_ORDER_INPUT = 1 };
 
 /* ---- CORSIKA IACT photon bunches (ACorsikaIACTFile) ------------------- */
 /* One photon bunch per element (struct bunch of CORSIKA's IACT option, as

@@ -32,6 +32,7 @@ TABLE_1D, TABLE_2D = 1, 2
 INDEX_TABLE, INDEX_SELLMEIER, INDEX_CAUCHY, INDEX_SCHOTT, INDEX_MIXED = 1, 2, 3, 4, 5
 
 PREC_FP64, PREC_MIXED = 0, 1
+ORDER_SPATIAL, ORDER_INPUT = 0, 1
 
 
 class ShapeDesc(C.Structure):
@@ -145,7 +146,7 @@ class Bunches(C.Structure):
 class TraceOpts(C.Structure):
     _fields_ = [("limit", C.c_int32), ("disable_fresnel", C.c_int32), ("seed", C.c_uint64),
                 ("ray_id_offset", C.c_uint64), ("precision", C.c_int32),
-                ("block_size", C.c_int32), ("compaction", C.c_int32), ("reserved", C.c_int32)]
+                ("block_size", C.c_int32), ("compaction", C.c_int32), ("ray_order", C.c_int32)]
 
 
 class NativeError(RuntimeError):

@@ -45,11 +45,14 @@ void release_device(rbg_scene* s) {
     if (st) cudaStreamDestroy(st);
   for (void* p : s->dev->allocations) cudaFree(p);
   if (s->workspace) cudaFree(s->workspace);
+  if (s->order_ws) cudaFree(s->order_ws);
   if (prev >= 0) cudaSetDevice(prev);
   delete s->dev;
   s->dev = nullptr;
   s->workspace = nullptr;
   s->workspace_bytes = 0;
+  s->order_ws = nullptr;
+  s->order_ws_bytes = 0;
   s->dev_id = -1;
 }
 
@@ -160,6 +163,14 @@ extern "C" int rbg_last_launch_count(const rbg_scene* s) { return s ? s->last_la
 namespace rbg {
 int launch_mixed(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o,
                  cudaStream_t st, unsigned* err_flags, unsigned long long* counter, int* launches);
+size_t ray_order_bytes(int64_t n);
+int build_ray_order(const KernelRays& in, int64_t n, void* ws, const int32_t** order, cudaStream_t st);
+// below this many rays the mixed tracer takes rays up in input order
+constexpr int64_t kOrderMinRays = 1 << 14;
+bool want_ray_order(const rbg_trace_opts& o, int64_t n) {
+  return o.precision == RBG_PREC_MIXED && o.ray_order == RBG_ORDER_SPATIAL && n >= kOrderMinRays &&
+         ray_order_bytes(n) > 0;
+}
 int launch_fp64(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o,
                 cudaStream_t st, unsigned* err_flags, int* launches);
 }
@@ -184,6 +195,24 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
     int launches = 0;
     rbg_trace_opts o = *opts;
     if (o.compaction == 0) o.compaction = s->tuned_compaction;
+    if (want_ray_order(o, in->n)) {
+      const size_t need = ray_order_bytes(in->n);
+      if (s->order_ws_bytes < need) {
+        // the previous workspace may still be read by work queued earlier
+        // on another stream: wait for the device before freeing it
+        if (s->order_ws && (cudaDeviceSynchronize() != cudaSuccess || cudaFree(s->order_ws) != cudaSuccess))
+          return RBG_ERR_CUDA;
+        s->order_ws = nullptr;
+        s->order_ws_bytes = 0;
+        if (cudaMalloc(&s->order_ws, need) != cudaSuccess) {
+          s->order_ws = nullptr;
+          return RBG_ERR_NOMEM;
+        }
+        s->order_ws_bytes = need;
+      }
+      if ((rc = build_ray_order(kr, in->n, s->order_ws, &kr.order, st))) return rc;
+      launches += 5;
+    }
     rc = launch_mixed(s->dev->view, kr, ko, in->n, o, st, s->dev->err_flags, s->dev->counter, &launches);
     if (rc) return rc;
     s->last_launches = launches;
@@ -282,7 +311,8 @@ int grow_workspace(rbg_scene* s, size_t bytes, char** out) {
 
 // One pipeline slot: its own queue head and error word (a 256-byte
 // header), the chunk's 8 input and 7 output arrays, fates, point counts,
-// last nodes and optional histories, for up to `cap` rays.
+// last nodes, optional histories and the ray-order workspace, for up to
+// `cap` rays.
 struct Slot {
   unsigned* err;
   unsigned long long* counter;
@@ -293,10 +323,11 @@ struct Slot {
   uint8_t* status;
   double* hist;
   int32_t* hist_node;
+  void* order_ws;
 };
 
 size_t slot_bytes(int64_t cap, int hist_cap) {
-  return 256 + (size_t)cap * (15 * 8 + 2 * 4 + 8) + (size_t)cap * hist_cap * (4 * 8 + 4);
+  return 256 + (size_t)cap * (15 * 8 + 2 * 4 + 8) + (size_t)cap * hist_cap * (4 * 8 + 4) + ray_order_bytes(cap);
 }
 
 Slot slot_at(char* base, int64_t cap, int hist_cap) {
@@ -315,6 +346,8 @@ Slot slot_at(char* base, int64_t cap, int hist_cap) {
   sl.hist = hist_cap ? reinterpret_cast<double*>(p) : nullptr;
   p += (size_t)cap * hist_cap * 32;
   sl.hist_node = hist_cap ? reinterpret_cast<int32_t*>(p) : nullptr;
+  p += (size_t)cap * hist_cap * 4;
+  sl.order_ws = p;
   return sl;
 }
 
@@ -373,6 +406,10 @@ extern "C" int rbg_trace_host(rbg_scene* s, const rbg_rays* in, rbg_result* out,
     o.ray_id_offset = opts->ray_id_offset + (uint64_t)off;
     if (o.compaction == 0) o.compaction = s->tuned_compaction;
     int nl = 0;
+    if (want_ray_order(o, m)) {
+      if ((rc = build_ray_order(kr, m, sl.order_ws, &kr.order, st))) return rc;
+      nl += 5;
+    }
     if ((rc = launch_trace(s, kr, ko, m, o, st, sl.err, sl.counter, &nl))) return rc;
     launches += nl;
     if (out->status && cudaMemcpyAsync(out->status + off, sl.status, m, cudaMemcpyDeviceToHost, st) != cudaSuccess)

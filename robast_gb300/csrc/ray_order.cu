@@ -1,0 +1,221 @@
+// ray_order.cu -- the order in which the mixed tracer takes up the rays of a
+// batch.
+//
+// Sources draw their rays at random over an aperture, so 32 consecutive
+// rays of a batch start anywhere on it: one lane's ray hits the central
+// hole, the next the secondary's shadow, the next a mirror edge, and the
+// warp serialises their paths.  The persistent kernel therefore takes the
+// rays up in the order of a spatial counting sort: the batch is cut into
+// chunks of at least 2^20 consecutive rays (a chunk of a batch built
+// field by field holds one field's rays), and within a chunk the rays are
+// grouped by a 3D Morton cell of their start point on a 64^3 grid over the
+// batch's bounding box.  Every ray keeps its own index for its inputs, its
+// outputs and its random draws, so the results are those of input order;
+// only which rays share a warp changes.
+//
+// Kernels: bounding box (ordered-integer atomics), cell keys and counts,
+// a two-level exclusive scan of the counts, and the scatter of the ray
+// indices.  Within a cell the order is whatever the atomics give.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "robast_gb.h"
+#include "tracer.cuh"
+
+namespace rbg {
+namespace {
+
+constexpr int kCellBits = 18;  // 6 bits per axis
+constexpr int kScanTile = 1024;
+constexpr int64_t kMinChunk = int64_t(1) << 20;
+constexpr int kMaxChunks = 16;
+constexpr int kThreads = 256;
+
+// doubles as unsigned integers in the same order (non-finite values are
+// left out of the box by the caller)
+__device__ __forceinline__ unsigned long long ordered_bits(double v) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double from_ordered(unsigned long long k) {
+  const unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
+// box[0..2] = min, box[3..5] = max (ordered bits); min words start at ~0,
+// max words at 0
+__global__ void __launch_bounds__(kThreads) bbox_kernel(const double* x, const double* y, const double* z, int64_t n,
+                                                        unsigned long long* box) {
+  unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
+  const double* v[3] = {x, y, z};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double c = v[a][i];
+      if (!isfinite(c)) continue;
+      const unsigned long long k = ordered_bits(c);
+      lo[a] = k < lo[a] ? k : lo[a];
+      hi[a] = k > hi[a] ? k : hi[a];
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) {
+      const unsigned long long l = __shfl_down_sync(0xffffffffu, lo[a], d);
+      const unsigned long long h = __shfl_down_sync(0xffffffffu, hi[a], d);
+      lo[a] = l < lo[a] ? l : lo[a];
+      hi[a] = h > hi[a] ? h : hi[a];
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      atomicMin(&box[a], lo[a]);
+      atomicMax(&box[3 + a], hi[a]);
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+  // 6 bits -> every third bit of 18
+  v &= 0x3fu;
+  v = (v | (v << 8)) & 0x0300f00fu;
+  v = (v | (v << 4)) & 0x030c30c3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+__device__ __forceinline__ uint32_t axis_cell(double c, double lo, double scale) {
+  if (!(c >= lo)) return 0u;  // below the box or NaN
+  const double q = (c - lo) * scale;
+  return q >= 63.0 ? 63u : (uint32_t)q;
+}
+
+__global__ void __launch_bounds__(kThreads) key_kernel(const double* x, const double* y, const double* z, int64_t n,
+                                                       int64_t chunk, const unsigned long long* box, uint32_t* keys,
+                                                       uint32_t* counts) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* v[3] = {x, y, z};
+  uint32_t cell = 0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    uint32_t q = 0;
+    if (box[a] <= box[3 + a]) {
+      const double lo = from_ordered(box[a]), hi = from_ordered(box[3 + a]);
+      const double scale = hi > lo ? 64.0 / (hi - lo) : 0.0;
+      q = axis_cell(v[a][i], lo, scale);
+    }
+    cell |= spread3(q) << a;
+  }
+  const uint32_t key = ((uint32_t)(i / chunk) << kCellBits) | cell;
+  keys[i] = key;
+  atomicAdd(&counts[key], 1u);
+}
+
+// exclusive scan inside tiles of kScanTile counts, tile totals to tile_sum
+__global__ void __launch_bounds__(kScanTile) tile_scan_counts(uint32_t* counts, int64_t m, uint32_t* tile_sum) {
+  __shared__ uint32_t s[kScanTile];
+  const int64_t i = (int64_t)blockIdx.x * kScanTile + threadIdx.x;
+  const uint32_t c = i < m ? counts[i] : 0u;
+  s[threadIdx.x] = c;
+  __syncthreads();
+  for (int d = 1; d < kScanTile; d <<= 1) {
+    const uint32_t v = threadIdx.x >= d ? s[threadIdx.x - d] : 0u;
+    __syncthreads();
+    s[threadIdx.x] += v;
+    __syncthreads();
+  }
+  if (i < m) counts[i] = s[threadIdx.x] - c;
+  if (threadIdx.x == kScanTile - 1) tile_sum[blockIdx.x] = s[kScanTile - 1];
+}
+
+// exclusive scan of the tile totals in one block
+__global__ void __launch_bounds__(kScanTile) scan_tile_sums(uint32_t* tile_sum, int64_t ntiles) {
+  __shared__ uint32_t s[kScanTile];
+  __shared__ uint32_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int64_t base = 0; base < ntiles; base += kScanTile) {
+    const int64_t i = base + threadIdx.x;
+    const uint32_t c = i < ntiles ? tile_sum[i] : 0u;
+    s[threadIdx.x] = c;
+    __syncthreads();
+    for (int d = 1; d < kScanTile; d <<= 1) {
+      const uint32_t v = threadIdx.x >= d ? s[threadIdx.x - d] : 0u;
+      __syncthreads();
+      s[threadIdx.x] += v;
+      __syncthreads();
+    }
+    if (i < ntiles) tile_sum[i] = carry + s[threadIdx.x] - c;
+    __syncthreads();
+    if (threadIdx.x == kScanTile - 1) carry += s[kScanTile - 1];
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) scatter_kernel(const uint32_t* keys, int64_t n, uint32_t* cursor,
+                                                           const uint32_t* tile_sum, int32_t* order) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t key = keys[i];
+  const uint32_t pos = tile_sum[key / kScanTile] + atomicAdd(&cursor[key], 1u);
+  if (pos < (uint64_t)n) order[pos] = (int32_t)i;
+}
+
+struct Layout {
+  int64_t chunk, chunks, buckets, tiles;
+  size_t box, keys, counts, tile_sum, order, total;
+};
+
+Layout layout(int64_t n) {
+  Layout L;
+  L.chunk = n / kMaxChunks + 1;
+  if (L.chunk < kMinChunk) L.chunk = kMinChunk;
+  L.chunks = (n + L.chunk - 1) / L.chunk;
+  L.buckets = L.chunks << kCellBits;
+  L.tiles = (L.buckets + kScanTile - 1) / kScanTile;
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  L.box = 0;
+  L.keys = L.box + 256;
+  L.counts = L.keys + up((size_t)n * 4);
+  L.tile_sum = L.counts + up((size_t)L.buckets * 4);
+  L.order = L.tile_sum + up((size_t)L.tiles * 4);
+  L.total = L.order + up((size_t)n * 4);
+  return L;
+}
+
+}  // namespace
+
+size_t ray_order_bytes(int64_t n) { return n > 0 && n <= 0x7fffffff ? layout(n).total : 0; }
+
+// Write the order of rays 0..n-1 into `ws` (ray_order_bytes(n) bytes) on
+// stream st; *order points at it.  n must fit in an int32.
+int build_ray_order(const KernelRays& in, int64_t n, void* ws, const int32_t** order, cudaStream_t st) {
+  if (n <= 0 || n > 0x7fffffff || !ws) return RBG_ERR_ARG;
+  const Layout L = layout(n);
+  char* base = static_cast<char*>(ws);
+  auto* box = reinterpret_cast<unsigned long long*>(base + L.box);
+  auto* keys = reinterpret_cast<uint32_t*>(base + L.keys);
+  auto* counts = reinterpret_cast<uint32_t*>(base + L.counts);
+  auto* tile_sum = reinterpret_cast<uint32_t*>(base + L.tile_sum);
+  auto* out = reinterpret_cast<int32_t*>(base + L.order);
+  if (cudaMemsetAsync(box, 0xff, 3 * sizeof(unsigned long long), st) != cudaSuccess ||
+      cudaMemsetAsync(box + 3, 0, 3 * sizeof(unsigned long long), st) != cudaSuccess ||
+      cudaMemsetAsync(counts, 0, (size_t)L.buckets * 4, st) != cudaSuccess)
+    return RBG_ERR_CUDA;
+  const int64_t blocks = (n + kThreads - 1) / kThreads;
+  const int box_blocks = (int)(blocks < 4096 ? blocks : 4096);
+  bbox_kernel<<<box_blocks, kThreads, 0, st>>>(in.x, in.y, in.z, n, box);
+  key_kernel<<<(unsigned)blocks, kThreads, 0, st>>>(in.x, in.y, in.z, n, L.chunk, box, keys, counts);
+  tile_scan_counts<<<(unsigned)L.tiles, kScanTile, 0, st>>>(counts, L.buckets, tile_sum);
+  scan_tile_sums<<<1, kScanTile, 0, st>>>(tile_sum, L.tiles);
+  scatter_kernel<<<(unsigned)blocks, kThreads, 0, st>>>(keys, n, counts, tile_sum, out);
+  if (cudaGetLastError() != cudaSuccess) return RBG_ERR_CUDA;
+  *order = out;
+  return RBG_OK;
+}
+
+}  // namespace rbg

@@ -47,6 +47,9 @@ struct rbg_scene {
   int tuned_compaction = 0;  // rbg_scene_autotune's choice, 0: none yet
   void* workspace = nullptr;
   size_t workspace_bytes = 0;
+  // rbg_trace's ray-order workspace (grown on demand, freed with the scene)
+  void* order_ws = nullptr;
+  size_t order_ws_bytes = 0;
 };
 
 // host helpers shared with the C-ABI implementation

@@ -31,7 +31,7 @@ int launch_fp64(const DevScene& S, const KernelRays& in, const KernelOut& out, i
   trace_fp64_kernel<<<blocks, block, 0, st>>>(S, in, out, n, o.limit, o.disable_fresnel, o.seed, o.ray_id_offset,
                                               err_flags);
   if (cudaGetLastError() != cudaSuccess) return RBG_ERR_CUDA;
-  *launches = 1;
+  *launches += 1;
   return RBG_OK;
 }
 

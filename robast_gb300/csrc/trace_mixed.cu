@@ -41,7 +41,7 @@ int launch_mixed(const DevScene& S, const KernelRays& in, const KernelOut& out, 
   for (const Instance& inst : kInstances) {
     if (S.features & ~inst.features) continue;
     const int rc = inst.launch(S, in, out, n, o, st, err_flags, counter);
-    if (rc == RBG_OK) *launches = 1;
+    if (rc == RBG_OK) *launches += 1;
     return rc;
   }
   return RBG_ERR_UNSUPPORTED;

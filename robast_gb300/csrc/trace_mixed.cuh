@@ -56,8 +56,12 @@ __global__ void __launch_bounds__(kMixedBlock) trace_mixed_kernel(DevScene S, Ke
       if (!active) {
         unsigned long long mine = base + __popc(need & lanes_below);
         if (mine < (unsigned long long)n) {
-          idx = (int64_t)mine;
-          if (load_ray_f(in, out, idx, seed, id_offset, r)) {
+          // queue slot -> ray: the ray keeps its own index (inputs,
+          // outputs, random draws) whatever the take-up order
+          idx = in.order ? (int64_t)in.order[mine] : (int64_t)mine;
+          if ((uint64_t)idx >= (uint64_t)n) {
+            err |= ERR_BIT_CAP;  // not a permutation of the batch: never expected
+          } else if (load_ray_f(in, out, idx, seed, id_offset, r)) {
             trace_begin<true, F>(S, r, nv);
             active = true;
           } else {

@@ -1252,6 +1252,8 @@ RBG_D void trace_ray(const DevScene& S, Ray& r, int limit, bool disable_fresnel)
 // ---------------------------------------------------------------------
 struct KernelRays {
   const double *x, *y, *z, *t, *dx, *dy, *dz, *lambda;
+  // the mixed tracer's take-up order (ray_order.cu); NULL: input order
+  const int32_t* order;
 };
 struct KernelOut {
   uint8_t* status;

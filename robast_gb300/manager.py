@@ -569,6 +569,7 @@ class AOpticsManager:
         self.precision = N.PREC_FP64
         self.ray_id_offset = 0
         self.compaction = 0  # mixed tracer refill threshold, 0: the scene's tuned value
+        self.ray_order = N.ORDER_SPATIAL  # mixed tracer take-up order (results do not depend on it)
 
     # units (include/AOpticsManager.h:59-71)
     @staticmethod
@@ -673,6 +674,7 @@ class AOpticsManager:
         o.ray_id_offset = self.ray_id_offset
         o.precision = self.precision if precision is None else precision
         o.compaction = int(self.compaction)
+        o.ray_order = int(self.ray_order)
         return o
 
     def _ensure_scene(self) -> Scene:
