@@ -8,10 +8,12 @@
 // rays up in the order of a spatial counting sort: the batch is cut into
 // chunks of at least 2^20 consecutive rays (a chunk of a batch built
 // field by field holds one field's rays), and within a chunk the rays are
-// grouped by a 3D Morton cell of their start point on a 64^3 grid over the
-// batch's bounding box.  Every ray keeps its own index for its inputs, its
-// outputs and its random draws, so the results are those of input order;
-// only which rays share a warp changes.
+// grouped by a cell of their start point: 2^20 cells over the batch's
+// bounding box, numbered along a Morton curve whose bits go one at a time
+// to the axis whose cells are then longest (a batch that starts on a
+// tilted plane spends few bits on its thin axis).  Every ray keeps its own
+// index for its inputs, its outputs and its random draws, so the results
+// are those of input order; only which rays share a warp changes.
 //
 // Kernels: bounding box (ordered-integer atomics), cell keys and counts,
 // a two-level exclusive scan of the counts, and the scatter of the ray
@@ -26,7 +28,7 @@
 namespace rbg {
 namespace {
 
-constexpr int kCellBits = 18;  // 6 bits per axis
+constexpr int kCellBits = 20;
 constexpr int kScanTile = 1024;
 constexpr int64_t kMinChunk = int64_t(1) << 20;
 constexpr int kMaxChunks = 16;
@@ -78,37 +80,48 @@ __global__ void __launch_bounds__(kThreads) bbox_kernel(const double* x, const d
   }
 }
 
-__device__ __forceinline__ uint32_t spread3(uint32_t v) {
-  // 6 bits -> every third bit of 18
-  v &= 0x3fu;
-  v = (v | (v << 8)) & 0x0300f00fu;
-  v = (v | (v << 4)) & 0x030c30c3u;
-  v = (v | (v << 2)) & 0x09249249u;
-  return v;
-}
-
-__device__ __forceinline__ uint32_t axis_cell(double c, double lo, double scale) {
-  if (!(c >= lo)) return 0u;  // below the box or NaN
-  const double q = (c - lo) * scale;
-  return q >= 63.0 ? 63u : (uint32_t)q;
-}
-
 __global__ void __launch_bounds__(kThreads) key_kernel(const double* x, const double* y, const double* z, int64_t n,
                                                        int64_t chunk, const unsigned long long* box, uint32_t* keys,
                                                        uint32_t* counts) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double* v[3] = {x, y, z};
-  uint32_t cell = 0;
+  double lo[3], ext[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    uint32_t q = 0;
-    if (box[a] <= box[3 + a]) {
-      const double lo = from_ordered(box[a]), hi = from_ordered(box[3 + a]);
-      const double scale = hi > lo ? 64.0 / (hi - lo) : 0.0;
-      q = axis_cell(v[a][i], lo, scale);
+    const bool ok = box[a] <= box[3 + a];
+    lo[a] = ok ? from_ordered(box[a]) : 0.0;
+    ext[a] = ok ? from_ordered(box[3 + a]) - lo[a] : 0.0;
+  }
+  // bits per axis: each of the kCellBits goes to the axis with the
+  // longest cells so far (ties to the lower axis); every thread derives
+  // the same assignment from the box
+  int bits[3] = {0, 0, 0};
+  uint64_t seq = 0;  // 2 bits per key bit: its axis, most significant first
+  {
+    double size[3] = {ext[0], ext[1], ext[2]};
+    for (int b = 0; b < kCellBits; ++b) {
+      const int a = size[0] >= size[1] ? (size[0] >= size[2] ? 0 : 2) : (size[1] >= size[2] ? 1 : 2);
+      size[a] *= 0.5;
+      ++bits[a];
+      seq |= (uint64_t)a << (2 * b);
     }
-    cell |= spread3(q) << a;
+  }
+  uint32_t q[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const double c = v[a][i];
+    const double cells = (double)(1u << bits[a]);
+    double f = ext[a] > 0 ? (c - lo[a]) / ext[a] * cells : 0.0;
+    if (!(f >= 0)) f = 0;  // below the box or NaN
+    q[a] = f >= cells - 1 ? (1u << bits[a]) - 1u : (uint32_t)f;
+  }
+  uint32_t cell = 0;
+  int used[3] = {0, 0, 0};
+  for (int b = 0; b < kCellBits; ++b) {
+    const int a = (int)((seq >> (2 * b)) & 3u);
+    const int k = bits[a] - 1 - used[a]++;
+    cell = (cell << 1) | ((q[a] >> k) & 1u);
   }
   const uint32_t key = ((uint32_t)(i / chunk) << kCellBits) | cell;
   keys[i] = key;
