@@ -301,10 +301,9 @@ typedef struct {
    * on it. */
   int32_t compaction;
   /* mixed tracer: the order in which the rays are taken up.
-   * RBG_ORDER_SPATIAL (default) groups the rays of each chunk of 2^20 or
-   * more consecutive rays by a 3D Morton cell of their start point, so the
-   * lanes of a warp follow neighbouring paths; RBG_ORDER_INPUT takes them
-   * in input order.  Every ray keeps its index for its inputs, outputs and
+   * RBG_ORDER_SPATIAL (default) groups the rays by a cell of their
+   * direction and, within it, of their start point, so the lanes of a warp
+   * follow neighbouring paths; RBG_ORDER_INPUT takes them in input order.  Every ray keeps its index for its inputs, outputs and
    * random draws: results do not depend on it.  Batches under 2^14 rays,
    * and rbg_trace_noalloc, always use input order. */
   int32_t ray_order;

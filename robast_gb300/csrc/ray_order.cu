@@ -5,17 +5,17 @@
 // rays of a batch start anywhere on it: one lane's ray hits the central
 // hole, the next the secondary's shadow, the next a mirror edge, and the
 // warp serialises their paths.  The persistent kernel therefore takes the
-// rays up in the order of a spatial counting sort: the batch is cut into
-// chunks of at least 2^20 consecutive rays (a chunk of a batch built
-// field by field holds one field's rays), and within a chunk the rays are
-// grouped by a cell of their start point: 2^20 cells over the batch's
-// bounding box, numbered along a Morton curve whose bits go one at a time
-// to the axis whose cells are then longest (a batch that starts on a
-// tilted plane spends few bits on its thin axis).  Every ray keeps its own
-// index for its inputs, its outputs and its random draws, so the results
-// are those of input order; only which rays share a warp changes.
+// rays up in the order of a counting sort by a cell key: the high bits a
+// cell of the ray's direction, the low bits a cell of its start point,
+// each numbered along a Morton curve whose bits go one at a time to the
+// axis whose cells are then longest, over the bounding box of the batch's
+// directions or start points (a batch that starts on a tilted plane spends
+// few bits on its thin axis; rays of different field angles never share a
+// cell).  Every ray keeps its own index for its inputs, its outputs and its
+// random draws, so the results are those of input order; only which rays
+// share a warp changes.
 //
-// Kernels: bounding box (ordered-integer atomics), cell keys and counts,
+// Kernels: bounding boxes (ordered-integer atomics), cell keys and counts,
 // a two-level exclusive scan of the counts, and the scatter of the ray
 // indices.  Within a cell the order is whatever the atomics give.
 #include <cuda_runtime.h>
@@ -28,10 +28,10 @@
 namespace rbg {
 namespace {
 
-constexpr int kCellBits = 20;
+// key bits: about 4 cells per ray, at most 2^24 cells; a quarter of the
+// bits (at most 6) number the direction cell
+constexpr int kMinKeyBits = 12, kMaxKeyBits = 24, kMaxDirBits = 6;
 constexpr int kScanTile = 1024;
-constexpr int64_t kMinChunk = int64_t(1) << 20;
-constexpr int kMaxChunks = 16;
 constexpr int kThreads = 256;
 
 // doubles as unsigned integers in the same order (non-finite values are
@@ -45,15 +45,19 @@ __device__ __forceinline__ double from_ordered(unsigned long long k) {
   return __longlong_as_double((long long)u);
 }
 
-// box[0..2] = min, box[3..5] = max (ordered bits); min words start at ~0,
-// max words at 0
-__global__ void __launch_bounds__(kThreads) bbox_kernel(const double* x, const double* y, const double* z, int64_t n,
-                                                        unsigned long long* box) {
-  unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
-  const double* v[3] = {x, y, z};
+// box[0..5] = min, box[6..11] = max (ordered bits) of x, y, z, dx, dy, dz;
+// min words start at ~0, max words at 0
+__global__ void __launch_bounds__(kThreads) bbox_kernel(KernelRays in, int64_t n, unsigned long long* box) {
+  unsigned long long lo[6], hi[6];
+  const double* v[6] = {in.x, in.y, in.z, in.dx, in.dy, in.dz};
+#pragma unroll
+  for (int a = 0; a < 6; ++a) {
+    lo[a] = ~0ull;
+    hi[a] = 0ull;
+  }
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
+    for (int a = 0; a < 6; ++a) {
       const double c = v[a][i];
       if (!isfinite(c)) continue;
       const unsigned long long k = ordered_bits(c);
@@ -62,7 +66,7 @@ __global__ void __launch_bounds__(kThreads) bbox_kernel(const double* x, const d
     }
   }
 #pragma unroll
-  for (int a = 0; a < 3; ++a) {
+  for (int a = 0; a < 6; ++a) {
 #pragma unroll
     for (int d = 16; d >= 1; d >>= 1) {
       const unsigned long long l = __shfl_down_sync(0xffffffffu, lo[a], d);
@@ -73,57 +77,58 @@ __global__ void __launch_bounds__(kThreads) bbox_kernel(const double* x, const d
   }
   if ((threadIdx.x & 31) == 0) {
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
+    for (int a = 0; a < 6; ++a) {
       atomicMin(&box[a], lo[a]);
-      atomicMax(&box[3 + a], hi[a]);
+      atomicMax(&box[6 + a], hi[a]);
     }
   }
 }
 
-__global__ void __launch_bounds__(kThreads) key_kernel(const double* x, const double* y, const double* z, int64_t n,
-                                                       int64_t chunk, const unsigned long long* box, uint32_t* keys,
-                                                       uint32_t* counts) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double* v[3] = {x, y, z};
-  double lo[3], ext[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    const bool ok = box[a] <= box[3 + a];
-    lo[a] = ok ? from_ordered(box[a]) : 0.0;
-    ext[a] = ok ? from_ordered(box[3 + a]) - lo[a] : 0.0;
-  }
-  // bits per axis: each of the kCellBits goes to the axis with the
-  // longest cells so far (ties to the lower axis); every thread derives
-  // the same assignment from the box
+// Morton cell of the point c[0..2] in `nbits` bits over the box lo + ext:
+// each bit goes to the axis whose cells are then longest (ties to the
+// lower axis); every thread derives the same assignment from the box
+__device__ uint32_t morton_cell(const double* c, const double* lo, const double* ext, int nbits) {
   int bits[3] = {0, 0, 0};
   uint64_t seq = 0;  // 2 bits per key bit: its axis, most significant first
-  {
-    double size[3] = {ext[0], ext[1], ext[2]};
-    for (int b = 0; b < kCellBits; ++b) {
-      const int a = size[0] >= size[1] ? (size[0] >= size[2] ? 0 : 2) : (size[1] >= size[2] ? 1 : 2);
-      size[a] *= 0.5;
-      ++bits[a];
-      seq |= (uint64_t)a << (2 * b);
-    }
+  double size[3] = {ext[0], ext[1], ext[2]};
+  for (int b = 0; b < nbits; ++b) {
+    const int a = size[0] >= size[1] ? (size[0] >= size[2] ? 0 : 2) : (size[1] >= size[2] ? 1 : 2);
+    size[a] *= 0.5;
+    ++bits[a];
+    seq |= (uint64_t)a << (2 * b);
   }
   uint32_t q[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const double c = v[a][i];
     const double cells = (double)(1u << bits[a]);
-    double f = ext[a] > 0 ? (c - lo[a]) / ext[a] * cells : 0.0;
+    double f = ext[a] > 0 ? (c[a] - lo[a]) / ext[a] * cells : 0.0;
     if (!(f >= 0)) f = 0;  // below the box or NaN
     q[a] = f >= cells - 1 ? (1u << bits[a]) - 1u : (uint32_t)f;
   }
   uint32_t cell = 0;
   int used[3] = {0, 0, 0};
-  for (int b = 0; b < kCellBits; ++b) {
+  for (int b = 0; b < nbits; ++b) {
     const int a = (int)((seq >> (2 * b)) & 3u);
     const int k = bits[a] - 1 - used[a]++;
     cell = (cell << 1) | ((q[a] >> k) & 1u);
   }
-  const uint32_t key = ((uint32_t)(i / chunk) << kCellBits) | cell;
+  return cell;
+}
+
+__global__ void __launch_bounds__(kThreads) key_kernel(KernelRays in, int64_t n, int dir_bits, int pos_bits,
+                                                       const unsigned long long* box, uint32_t* keys,
+                                                       uint32_t* counts) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double lo[6], ext[6];
+#pragma unroll
+  for (int a = 0; a < 6; ++a) {
+    const bool ok = box[a] <= box[6 + a];
+    lo[a] = ok ? from_ordered(box[a]) : 0.0;
+    ext[a] = ok ? from_ordered(box[6 + a]) - lo[a] : 0.0;
+  }
+  const double p[3] = {in.x[i], in.y[i], in.z[i]}, d[3] = {in.dx[i], in.dy[i], in.dz[i]};
+  const uint32_t key = (morton_cell(d, lo + 3, ext + 3, dir_bits) << pos_bits) | morton_cell(p, lo, ext, pos_bits);
   keys[i] = key;
   atomicAdd(&counts[key], 1u);
 }
@@ -179,16 +184,18 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(const uint32_t* keys,
 }
 
 struct Layout {
-  int64_t chunk, chunks, buckets, tiles;
+  int dir_bits, pos_bits;
+  int64_t buckets, tiles;
   size_t box, keys, counts, tile_sum, order, total;
 };
 
 Layout layout(int64_t n) {
   Layout L;
-  L.chunk = n / kMaxChunks + 1;
-  if (L.chunk < kMinChunk) L.chunk = kMinChunk;
-  L.chunks = (n + L.chunk - 1) / L.chunk;
-  L.buckets = L.chunks << kCellBits;
+  int kb = kMinKeyBits;
+  while (kb < kMaxKeyBits && (int64_t(1) << kb) < 4 * n) ++kb;
+  L.dir_bits = kb / 4 < kMaxDirBits ? kb / 4 : kMaxDirBits;
+  L.pos_bits = kb - L.dir_bits;
+  L.buckets = int64_t(1) << kb;
   L.tiles = (L.buckets + kScanTile - 1) / kScanTile;
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
   L.box = 0;
@@ -215,14 +222,14 @@ int build_ray_order(const KernelRays& in, int64_t n, void* ws, const int32_t** o
   auto* counts = reinterpret_cast<uint32_t*>(base + L.counts);
   auto* tile_sum = reinterpret_cast<uint32_t*>(base + L.tile_sum);
   auto* out = reinterpret_cast<int32_t*>(base + L.order);
-  if (cudaMemsetAsync(box, 0xff, 3 * sizeof(unsigned long long), st) != cudaSuccess ||
-      cudaMemsetAsync(box + 3, 0, 3 * sizeof(unsigned long long), st) != cudaSuccess ||
+  if (cudaMemsetAsync(box, 0xff, 6 * sizeof(unsigned long long), st) != cudaSuccess ||
+      cudaMemsetAsync(box + 6, 0, 6 * sizeof(unsigned long long), st) != cudaSuccess ||
       cudaMemsetAsync(counts, 0, (size_t)L.buckets * 4, st) != cudaSuccess)
     return RBG_ERR_CUDA;
   const int64_t blocks = (n + kThreads - 1) / kThreads;
   const int box_blocks = (int)(blocks < 4096 ? blocks : 4096);
-  bbox_kernel<<<box_blocks, kThreads, 0, st>>>(in.x, in.y, in.z, n, box);
-  key_kernel<<<(unsigned)blocks, kThreads, 0, st>>>(in.x, in.y, in.z, n, L.chunk, box, keys, counts);
+  bbox_kernel<<<box_blocks, kThreads, 0, st>>>(in, n, box);
+  key_kernel<<<(unsigned)blocks, kThreads, 0, st>>>(in, n, L.dir_bits, L.pos_bits, box, keys, counts);
   tile_scan_counts<<<(unsigned)L.tiles, kScanTile, 0, st>>>(counts, L.buckets, tile_sum);
   scan_tile_sums<<<1, kScanTile, 0, st>>>(tile_sum, L.tiles);
   scatter_kernel<<<(unsigned)blocks, kThreads, 0, st>>>(keys, n, counts, tile_sum, out);
