@@ -164,7 +164,7 @@ namespace rbg {
 int launch_mixed(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o,
                  cudaStream_t st, unsigned* err_flags, unsigned long long* counter, int* launches);
 size_t ray_order_bytes(int64_t n);
-int build_ray_order(const KernelRays& in, int64_t n, void* ws, const int32_t** order, cudaStream_t st);
+int build_ray_order(const KernelRays& in, int64_t n, void* ws, KernelRays* sorted, cudaStream_t st);
 // below this many rays the mixed tracer takes rays up in input order
 constexpr int64_t kOrderMinRays = 1 << 14;
 bool want_ray_order(const rbg_trace_opts& o, int64_t n) {
@@ -210,8 +210,8 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
         }
         s->order_ws_bytes = need;
       }
-      if ((rc = build_ray_order(kr, in->n, s->order_ws, &kr.order, st))) return rc;
-      launches += 5;
+      if ((rc = build_ray_order(kr, in->n, s->order_ws, &kr, st))) return rc;
+      launches += 6;
     }
     rc = launch_mixed(s->dev->view, kr, ko, in->n, o, st, s->dev->err_flags, s->dev->counter, &launches);
     if (rc) return rc;
@@ -407,8 +407,8 @@ extern "C" int rbg_trace_host(rbg_scene* s, const rbg_rays* in, rbg_result* out,
     if (o.compaction == 0) o.compaction = s->tuned_compaction;
     int nl = 0;
     if (want_ray_order(o, m)) {
-      if ((rc = build_ray_order(kr, m, sl.order_ws, &kr.order, st))) return rc;
-      nl += 5;
+      if ((rc = build_ray_order(kr, m, sl.order_ws, &kr, st))) return rc;
+      nl += 6;
     }
     if ((rc = launch_trace(s, kr, ko, m, o, st, sl.err, sl.counter, &nl))) return rc;
     launches += nl;

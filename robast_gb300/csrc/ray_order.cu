@@ -16,8 +16,10 @@
 // share a warp changes.
 //
 // Kernels: bounding boxes (ordered-integer atomics), cell keys and counts,
-// a two-level exclusive scan of the counts, and the scatter of the ray
-// indices.  Within a cell the order is whatever the atomics give.
+// a two-level exclusive scan of the counts, the scatter of the ray indices
+// and a gather of the rays into that order, so the trace reads its inputs
+// coalesced (its outputs go to each ray's own index).  Within a cell the
+// order is whatever the atomics give.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -174,6 +176,23 @@ __global__ void __launch_bounds__(kScanTile) scan_tile_sums(uint32_t* tile_sum, 
   }
 }
 
+// the rays in queue order: slot q <- ray order[q] (coalesced stores; the
+// trace then reads its inputs coalesced)
+struct Dst {
+  double* a[8];
+};
+
+__global__ void __launch_bounds__(kThreads) gather_kernel(KernelRays in, int64_t n, const int32_t* order, Dst dst) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int64_t i = order[q];
+  if ((uint64_t)i >= (uint64_t)n) return;
+  const double* src[8] = {in.x, in.y, in.z, in.t, in.dx, in.dy, in.dz, in.lambda};
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+    if (src[a]) dst.a[a][q] = src[a][i];
+}
+
 __global__ void __launch_bounds__(kThreads) scatter_kernel(const uint32_t* keys, int64_t n, uint32_t* cursor,
                                                            const uint32_t* tile_sum, int32_t* order) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -186,7 +205,7 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(const uint32_t* keys,
 struct Layout {
   int dir_bits, pos_bits;
   int64_t buckets, tiles;
-  size_t box, keys, counts, tile_sum, order, total;
+  size_t box, keys, counts, tile_sum, order, sorted, total;
 };
 
 Layout layout(int64_t n) {
@@ -203,7 +222,8 @@ Layout layout(int64_t n) {
   L.counts = L.keys + up((size_t)n * 4);
   L.tile_sum = L.counts + up((size_t)L.buckets * 4);
   L.order = L.tile_sum + up((size_t)L.tiles * 4);
-  L.total = L.order + up((size_t)n * 4);
+  L.sorted = L.order + up((size_t)n * 4);  // 8 arrays of n doubles
+  L.total = L.sorted + 8 * up((size_t)n * 8);
   return L;
 }
 
@@ -211,10 +231,11 @@ Layout layout(int64_t n) {
 
 size_t ray_order_bytes(int64_t n) { return n > 0 && n <= 0x7fffffff ? layout(n).total : 0; }
 
-// Write the order of rays 0..n-1 into `ws` (ray_order_bytes(n) bytes) on
-// stream st; *order points at it.  n must fit in an int32.
-int build_ray_order(const KernelRays& in, int64_t n, void* ws, const int32_t** order, cudaStream_t st) {
-  if (n <= 0 || n > 0x7fffffff || !ws) return RBG_ERR_ARG;
+// Write the take-up order of rays 0..n-1 and the rays in that order into
+// `ws` (ray_order_bytes(n) bytes) on stream st; *sorted describes them
+// (gathered, with the order).  n must fit in an int32.
+int build_ray_order(const KernelRays& in, int64_t n, void* ws, KernelRays* sorted, cudaStream_t st) {
+  if (n <= 0 || n > 0x7fffffff || !ws || !sorted) return RBG_ERR_ARG;
   const Layout L = layout(n);
   char* base = static_cast<char*>(ws);
   auto* box = reinterpret_cast<unsigned long long*>(base + L.box);
@@ -222,6 +243,9 @@ int build_ray_order(const KernelRays& in, int64_t n, void* ws, const int32_t** o
   auto* counts = reinterpret_cast<uint32_t*>(base + L.counts);
   auto* tile_sum = reinterpret_cast<uint32_t*>(base + L.tile_sum);
   auto* out = reinterpret_cast<int32_t*>(base + L.order);
+  const size_t arr = (L.total - L.sorted) / 8;
+  Dst dst;
+  for (int a = 0; a < 8; ++a) dst.a[a] = reinterpret_cast<double*>(base + L.sorted + a * arr);
   if (cudaMemsetAsync(box, 0xff, 6 * sizeof(unsigned long long), st) != cudaSuccess ||
       cudaMemsetAsync(box + 6, 0, 6 * sizeof(unsigned long long), st) != cudaSuccess ||
       cudaMemsetAsync(counts, 0, (size_t)L.buckets * 4, st) != cudaSuccess)
@@ -233,8 +257,10 @@ int build_ray_order(const KernelRays& in, int64_t n, void* ws, const int32_t** o
   tile_scan_counts<<<(unsigned)L.tiles, kScanTile, 0, st>>>(counts, L.buckets, tile_sum);
   scan_tile_sums<<<1, kScanTile, 0, st>>>(tile_sum, L.tiles);
   scatter_kernel<<<(unsigned)blocks, kThreads, 0, st>>>(keys, n, counts, tile_sum, out);
+  gather_kernel<<<(unsigned)blocks, kThreads, 0, st>>>(in, n, out, dst);
   if (cudaGetLastError() != cudaSuccess) return RBG_ERR_CUDA;
-  *order = out;
+  *sorted = KernelRays{dst.a[0], dst.a[1], dst.a[2], in.t ? dst.a[3] : nullptr, dst.a[4], dst.a[5], dst.a[6],
+                       dst.a[7], out, 1};
   return RBG_OK;
 }
 

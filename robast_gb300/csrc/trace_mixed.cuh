@@ -59,9 +59,10 @@ __global__ void __launch_bounds__(kMixedBlock) trace_mixed_kernel(DevScene S, Ke
           // queue slot -> ray: the ray keeps its own index (inputs,
           // outputs, random draws) whatever the take-up order
           idx = in.order ? (int64_t)in.order[mine] : (int64_t)mine;
+          const int64_t src = in.gathered ? (int64_t)mine : idx;
           if ((uint64_t)idx >= (uint64_t)n) {
             err |= ERR_BIT_CAP;  // not a permutation of the batch: never expected
-          } else if (load_ray_f(in, out, idx, seed, id_offset, r)) {
+          } else if (load_ray_f(in, out, src, idx, seed, id_offset, r)) {
             trace_begin<true, F>(S, r, nv);
             active = true;
           } else {

@@ -1252,8 +1252,12 @@ RBG_D void trace_ray(const DevScene& S, Ray& r, int limit, bool disable_fresnel)
 // ---------------------------------------------------------------------
 struct KernelRays {
   const double *x, *y, *z, *t, *dx, *dy, *dz, *lambda;
-  // the mixed tracer's take-up order (ray_order.cu); NULL: input order
+  // the mixed tracer's take-up order (ray_order.cu): queue slot q traces
+  // ray order[q]; NULL: input order.  With `gathered` set the arrays above
+  // hold the rays in queue order (slot q at q) and order[q] is the ray's
+  // index for its outputs and random draws.
   const int32_t* order;
+  int32_t gathered;
 };
 struct KernelOut {
   uint8_t* status;
@@ -1300,12 +1304,13 @@ RBG_D bool load_ray(const KernelRays& in, const KernelOut& out, int64_t i, uint6
 RBG_D bool finite_bits(double v) {
   return (__double_as_longlong(v) & 0x7ff0000000000000LL) != 0x7ff0000000000000LL;
 }
-RBG_D bool load_ray_f(const KernelRays& in, const KernelOut& out, int64_t i, uint64_t seed, uint64_t id_offset,
-                      Ray& r) {
-  r.x = mk(in.x[i], in.y[i], in.z[i]);
-  r.t = in.t ? in.t[i] : 0.0;
-  r.lambda = in.lambda[i];
-  d3 dd = mk(in.dx[i], in.dy[i], in.dz[i]);
+// Ray i of the batch, its inputs read at position `src` of `in`.
+RBG_D bool load_ray_f(const KernelRays& in, const KernelOut& out, int64_t src, int64_t i, uint64_t seed,
+                      uint64_t id_offset, Ray& r) {
+  r.x = mk(in.x[src], in.y[src], in.z[src]);
+  r.t = in.t ? in.t[src] : 0.0;
+  r.lambda = in.lambda[src];
+  d3 dd = mk(in.dx[src], in.dy[src], in.dz[src]);
   r.status = RBG_RUN;
   r.npoints = 0;
   r.last_node = -2;
