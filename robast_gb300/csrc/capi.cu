@@ -211,7 +211,7 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
         s->order_ws_bytes = need;
       }
       if ((rc = build_ray_order(kr, in->n, s->order_ws, &kr, st))) return rc;
-      launches += 6;
+      launches += 7;
     }
     rc = launch_mixed(s->dev->view, kr, ko, in->n, o, st, s->dev->err_flags, s->dev->counter, &launches);
     if (rc) return rc;
@@ -408,7 +408,7 @@ extern "C" int rbg_trace_host(rbg_scene* s, const rbg_rays* in, rbg_result* out,
     int nl = 0;
     if (want_ray_order(o, m)) {
       if ((rc = build_ray_order(kr, m, sl.order_ws, &kr, st))) return rc;
-      nl += 6;
+      nl += 7;
     }
     if ((rc = launch_trace(s, kr, ko, m, o, st, sl.err, sl.counter, &nl))) return rc;
     launches += nl;

@@ -15,7 +15,8 @@
 // random draws, so the results are those of input order; only which rays
 // share a warp changes.
 //
-// Kernels: bounding boxes (ordered-integer atomics), cell keys and counts,
+// Kernels: bounding boxes (ordered-integer atomics), the key plan (one
+// thread), cell keys and counts,
 // a two-level exclusive scan of the counts, the scatter of the ray indices
 // and a gather of the rays into that order, so the trace reads its inputs
 // coalesced (its outputs go to each ray's own index).  Within a cell the
@@ -23,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 
 #include "robast_gb.h"
 #include "tracer.cuh"
@@ -36,46 +38,53 @@ constexpr int kMinKeyBits = 12, kMaxKeyBits = 24, kMaxDirBits = 6;
 constexpr int kScanTile = 1024;
 constexpr int kThreads = 256;
 
-// doubles as unsigned integers in the same order (non-finite values are
-// left out of the box by the caller)
-__device__ __forceinline__ unsigned long long ordered_bits(double v) {
+// The high 32 bits of a double as an unsigned integer in the same order
+// (non-decreasing with the value; sign, exponent and 20 mantissa bits).
+// Non-finite values give 0 and are left out of the box.
+__device__ __forceinline__ uint32_t ordered_hi(double v, bool& finite) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(v);
-  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+  finite = ((u >> 52) & 0x7ffull) != 0x7ffull;
+  const uint32_t h = (uint32_t)(u >> 32);
+  return (h >> 31) ? ~h : (h | 0x80000000u);
 }
-__device__ __forceinline__ double from_ordered(unsigned long long k) {
-  const unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
-  return __longlong_as_double((long long)u);
+// a double not above (low = true) / not below every value whose ordered
+// high word is k
+__host__ __device__ inline double from_ordered_hi(uint32_t k, bool low) {
+  const uint32_t h = (k >> 31) ? (k & 0x7fffffffu) : ~k;
+  // the low word that moves the value down (low) or up: for a positive
+  // value 0 is the smallest magnitude, for a negative one the largest
+  const bool neg = (h >> 31) != 0;
+  const unsigned long long lw = (low != neg) ? 0ull : 0xffffffffull;
+  const unsigned long long u = ((unsigned long long)h << 32) | lw;
+  double d;
+  memcpy(&d, &u, sizeof(d));
+  return d;
 }
 
-// box[0..5] = min, box[6..11] = max (ordered bits) of x, y, z, dx, dy, dz;
-// min words start at ~0, max words at 0
-__global__ void __launch_bounds__(kThreads) bbox_kernel(KernelRays in, int64_t n, unsigned long long* box) {
-  unsigned long long lo[6], hi[6];
+// box[0..5] = min, box[6..11] = max ordered high words of x, y, z, dx, dy,
+// dz; min words start at ~0, max words at 0
+__global__ void __launch_bounds__(kThreads) bbox_kernel(KernelRays in, int64_t n, uint32_t* box) {
+  uint32_t lo[6], hi[6];
   const double* v[6] = {in.x, in.y, in.z, in.dx, in.dy, in.dz};
 #pragma unroll
   for (int a = 0; a < 6; ++a) {
-    lo[a] = ~0ull;
-    hi[a] = 0ull;
+    lo[a] = ~0u;
+    hi[a] = 0u;
   }
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
 #pragma unroll
     for (int a = 0; a < 6; ++a) {
-      const double c = v[a][i];
-      if (!isfinite(c)) continue;
-      const unsigned long long k = ordered_bits(c);
+      bool fin;
+      const uint32_t k = ordered_hi(v[a][i], fin);
+      if (!fin) continue;
       lo[a] = k < lo[a] ? k : lo[a];
       hi[a] = k > hi[a] ? k : hi[a];
     }
   }
 #pragma unroll
   for (int a = 0; a < 6; ++a) {
-#pragma unroll
-    for (int d = 16; d >= 1; d >>= 1) {
-      const unsigned long long l = __shfl_down_sync(0xffffffffu, lo[a], d);
-      const unsigned long long h = __shfl_down_sync(0xffffffffu, hi[a], d);
-      lo[a] = l < lo[a] ? l : lo[a];
-      hi[a] = h > hi[a] ? h : hi[a];
-    }
+    lo[a] = __reduce_min_sync(0xffffffffu, lo[a]);
+    hi[a] = __reduce_max_sync(0xffffffffu, hi[a]);
   }
   if ((threadIdx.x & 31) == 0) {
 #pragma unroll
@@ -86,51 +95,70 @@ __global__ void __launch_bounds__(kThreads) bbox_kernel(KernelRays in, int64_t n
   }
 }
 
-// Morton cell of the point c[0..2] in `nbits` bits over the box lo + ext:
-// each bit goes to the axis whose cells are then longest (ties to the
-// lower axis); every thread derives the same assignment from the box
-__device__ uint32_t morton_cell(const double* c, const double* lo, const double* ext, int nbits) {
-  int bits[3] = {0, 0, 0};
-  uint64_t seq = 0;  // 2 bits per key bit: its axis, most significant first
-  double size[3] = {ext[0], ext[1], ext[2]};
-  for (int b = 0; b < nbits; ++b) {
-    const int a = size[0] >= size[1] ? (size[0] >= size[2] ? 0 : 2) : (size[1] >= size[2] ? 1 : 2);
+// How a ray's cell key is formed, worked out once from the box: per axis
+// (x, y, z, dx, dy, dz) the low edge and the cells per unit in FP32, the
+// largest cell index, and the key bit each of its index bits lands on.
+struct Plan {
+  float lo[6], scale[6];
+  uint32_t qmax[6];
+  int32_t bits[6];
+  int8_t pos[6][kMaxKeyBits];
+};
+
+// Key bits go one at a time, most significant first, to the axis whose
+// cells are then longest (ties to the lower axis): dir_bits among the
+// direction axes, then pos_bits among the start-point axes.
+__global__ void plan_kernel(const uint32_t* box, int dir_bits, int pos_bits, Plan* plan) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  Plan P;
+  double size[6];
+  for (int a = 0; a < 6; ++a) {
+    const bool ok = box[a] <= box[6 + a];
+    const double lo = ok ? from_ordered_hi(box[a], true) : 0.0;
+    const double hi = ok ? from_ordered_hi(box[6 + a], false) : 0.0;
+    P.lo[a] = (float)lo;
+    size[a] = hi > lo ? hi - lo : 0.0;
+    P.bits[a] = 0;
+  }
+  const double ext[6] = {size[0], size[1], size[2], size[3], size[4], size[5]};
+  int seq[kMaxKeyBits];
+  const int total = dir_bits + pos_bits;
+  for (int b = 0; b < total; ++b) {
+    const int base = b < dir_bits ? 3 : 0;
+    int a = base;
+    for (int k = base + 1; k < base + 3; ++k)
+      if (size[k] > size[a]) a = k;
     size[a] *= 0.5;
-    ++bits[a];
-    seq |= (uint64_t)a << (2 * b);
+    ++P.bits[a];
+    seq[b] = a;
   }
-  uint32_t q[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    const double cells = (double)(1u << bits[a]);
-    double f = ext[a] > 0 ? (c[a] - lo[a]) / ext[a] * cells : 0.0;
-    if (!(f >= 0)) f = 0;  // below the box or NaN
-    q[a] = f >= cells - 1 ? (1u << bits[a]) - 1u : (uint32_t)f;
+  int used[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = 0; b < total; ++b) {
+    const int a = seq[b];
+    const int j = P.bits[a] - 1 - used[a]++;  // index bit j of axis a ...
+    P.pos[a][j] = (int8_t)(total - 1 - b);     // ... lands on this key bit
   }
-  uint32_t cell = 0;
-  int used[3] = {0, 0, 0};
-  for (int b = 0; b < nbits; ++b) {
-    const int a = (int)((seq >> (2 * b)) & 3u);
-    const int k = bits[a] - 1 - used[a]++;
-    cell = (cell << 1) | ((q[a] >> k) & 1u);
+  for (int a = 0; a < 6; ++a) {
+    P.qmax[a] = P.bits[a] ? (1u << P.bits[a]) - 1u : 0u;
+    P.scale[a] = ext[a] > 0 ? (float)((double)(1u << P.bits[a]) / ext[a]) : 0.f;
   }
-  return cell;
+  *plan = P;
 }
 
-__global__ void __launch_bounds__(kThreads) key_kernel(KernelRays in, int64_t n, int dir_bits, int pos_bits,
-                                                       const unsigned long long* box, uint32_t* keys,
+__global__ void __launch_bounds__(kThreads) key_kernel(KernelRays in, int64_t n, const Plan* plan, uint32_t* keys,
                                                        uint32_t* counts) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double lo[6], ext[6];
+  const double* v[6] = {in.x, in.y, in.z, in.dx, in.dy, in.dz};
+  uint32_t key = 0;
 #pragma unroll
   for (int a = 0; a < 6; ++a) {
-    const bool ok = box[a] <= box[6 + a];
-    lo[a] = ok ? from_ordered(box[a]) : 0.0;
-    ext[a] = ok ? from_ordered(box[6 + a]) - lo[a] : 0.0;
+    const float f = ((float)v[a][i] - plan->lo[a]) * plan->scale[a];
+    const uint32_t qmax = plan->qmax[a];
+    uint32_t q = 0u;  // below the box or NaN: 0
+    if (f >= 1.f) q = f >= (float)qmax ? qmax : (uint32_t)f;
+    for (int j = 0; j < plan->bits[a]; ++j) key |= ((q >> j) & 1u) << plan->pos[a][j];
   }
-  const double p[3] = {in.x[i], in.y[i], in.z[i]}, d[3] = {in.dx[i], in.dy[i], in.dz[i]};
-  const uint32_t key = (morton_cell(d, lo + 3, ext + 3, dir_bits) << pos_bits) | morton_cell(p, lo, ext, pos_bits);
   keys[i] = key;
   atomicAdd(&counts[key], 1u);
 }
@@ -205,7 +233,7 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(const uint32_t* keys,
 struct Layout {
   int dir_bits, pos_bits;
   int64_t buckets, tiles;
-  size_t box, keys, counts, tile_sum, order, sorted, total;
+  size_t box, plan, keys, counts, tile_sum, order, sorted, total;
 };
 
 Layout layout(int64_t n) {
@@ -218,7 +246,8 @@ Layout layout(int64_t n) {
   L.tiles = (L.buckets + kScanTile - 1) / kScanTile;
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
   L.box = 0;
-  L.keys = L.box + 256;
+  L.plan = 256;
+  L.keys = L.plan + up(sizeof(Plan));
   L.counts = L.keys + up((size_t)n * 4);
   L.tile_sum = L.counts + up((size_t)L.buckets * 4);
   L.order = L.tile_sum + up((size_t)L.tiles * 4);
@@ -238,7 +267,8 @@ int build_ray_order(const KernelRays& in, int64_t n, void* ws, KernelRays* sorte
   if (n <= 0 || n > 0x7fffffff || !ws || !sorted) return RBG_ERR_ARG;
   const Layout L = layout(n);
   char* base = static_cast<char*>(ws);
-  auto* box = reinterpret_cast<unsigned long long*>(base + L.box);
+  auto* box = reinterpret_cast<uint32_t*>(base + L.box);
+  auto* plan = reinterpret_cast<Plan*>(base + L.plan);
   auto* keys = reinterpret_cast<uint32_t*>(base + L.keys);
   auto* counts = reinterpret_cast<uint32_t*>(base + L.counts);
   auto* tile_sum = reinterpret_cast<uint32_t*>(base + L.tile_sum);
@@ -246,14 +276,15 @@ int build_ray_order(const KernelRays& in, int64_t n, void* ws, KernelRays* sorte
   const size_t arr = (L.total - L.sorted) / 8;
   Dst dst;
   for (int a = 0; a < 8; ++a) dst.a[a] = reinterpret_cast<double*>(base + L.sorted + a * arr);
-  if (cudaMemsetAsync(box, 0xff, 6 * sizeof(unsigned long long), st) != cudaSuccess ||
-      cudaMemsetAsync(box + 6, 0, 6 * sizeof(unsigned long long), st) != cudaSuccess ||
+  if (cudaMemsetAsync(box, 0xff, 6 * sizeof(uint32_t), st) != cudaSuccess ||
+      cudaMemsetAsync(box + 6, 0, 6 * sizeof(uint32_t), st) != cudaSuccess ||
       cudaMemsetAsync(counts, 0, (size_t)L.buckets * 4, st) != cudaSuccess)
     return RBG_ERR_CUDA;
   const int64_t blocks = (n + kThreads - 1) / kThreads;
   const int box_blocks = (int)(blocks < 4096 ? blocks : 4096);
   bbox_kernel<<<box_blocks, kThreads, 0, st>>>(in, n, box);
-  key_kernel<<<(unsigned)blocks, kThreads, 0, st>>>(in, n, L.dir_bits, L.pos_bits, box, keys, counts);
+  plan_kernel<<<1, 32, 0, st>>>(box, L.dir_bits, L.pos_bits, plan);
+  key_kernel<<<(unsigned)blocks, kThreads, 0, st>>>(in, n, plan, keys, counts);
   tile_scan_counts<<<(unsigned)L.tiles, kScanTile, 0, st>>>(counts, L.buckets, tile_sum);
   scan_tile_sums<<<1, kScanTile, 0, st>>>(tile_sum, L.tiles);
   scatter_kernel<<<(unsigned)blocks, kThreads, 0, st>>>(keys, n, counts, tile_sum, out);
