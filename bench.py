@@ -43,9 +43,10 @@ BYTES_PER_RAY = 88
 BYTES_PER_SEGMENT = 104
 # DRAM bytes per ray of the mixed tracer on the Schwarzschild-Couder batch:
 # dram__bytes_read.sum + dram__bytes_write.sum of one ncu-captured launch
-# over 3e6 rays (203.8 MB + 167.1 MB); traffic grows with the ray count
-# (every byte is ray I/O), so a launch's traffic is this times its rays
-DRAM_BYTES_PER_RAY_SC = (203.792128e6 + 167.089408e6) / 3e6
+# over 3e6 rays (364.1 MB + 339.1 MB: the rays read in take-up order, the
+# results written back to each ray's own index); traffic grows with the ray
+# count (every byte is ray I/O), so a launch's traffic is this times its rays
+DRAM_BYTES_PER_RAY_SC = (364.103424e6 + 339.134976e6) / 3e6
 
 
 # workload name -> (default rays, description); Schwarzschild-Couder is the
@@ -641,7 +642,7 @@ def main():
                          "peak_source": how,
                          "note": "algorithmic bytes = 88 B per ray + 104 B per segment (wavefront ray state); "
                                  "the kernel keeps ray state in registers and is bound by the FP64 pipe "
-                                 "(64 % busy under ncu), not by HBM"},
+                                 "(56 % busy, 30 of 32 lanes active under ncu), not by HBM"},
             "e2e": e2e, "clocks": clocks, "vs_plain_fp64": compare}
     if not args.no_grad and ws == 1 and args.workload == "schwarzschild_couder":
         line["grad"] = grad_bench(batch, rays, max(1, min(args.steps, 3)), device, N, torch)

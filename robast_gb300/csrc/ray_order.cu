@@ -81,17 +81,26 @@ __global__ void __launch_bounds__(kThreads) bbox_kernel(KernelRays in, int64_t n
       hi[a] = k > hi[a] ? k : hi[a];
     }
   }
+  // warp, then block, then one atomic per word and block
+  constexpr int kWarps = kThreads / 32;
+  __shared__ uint32_t part[12][kWarps];
+  const int warp = threadIdx.x >> 5;
 #pragma unroll
   for (int a = 0; a < 6; ++a) {
     lo[a] = __reduce_min_sync(0xffffffffu, lo[a]);
     hi[a] = __reduce_max_sync(0xffffffffu, hi[a]);
-  }
-  if ((threadIdx.x & 31) == 0) {
-#pragma unroll
-    for (int a = 0; a < 6; ++a) {
-      atomicMin(&box[a], lo[a]);
-      atomicMax(&box[6 + a], hi[a]);
+    if ((threadIdx.x & 31) == 0) {
+      part[a][warp] = lo[a];
+      part[6 + a][warp] = hi[a];
     }
+  }
+  __syncthreads();
+  if (threadIdx.x < 12) {
+    const int w = threadIdx.x;
+    uint32_t r = part[w][0];
+    for (int k = 1; k < kWarps; ++k) r = w < 6 ? (part[w][k] < r ? part[w][k] : r) : (part[w][k] > r ? part[w][k] : r);
+    if (w < 6) atomicMin(&box[w], r);
+    else atomicMax(&box[w], r);
   }
 }
 
@@ -281,7 +290,7 @@ int build_ray_order(const KernelRays& in, int64_t n, void* ws, KernelRays* sorte
       cudaMemsetAsync(counts, 0, (size_t)L.buckets * 4, st) != cudaSuccess)
     return RBG_ERR_CUDA;
   const int64_t blocks = (n + kThreads - 1) / kThreads;
-  const int box_blocks = (int)(blocks < 4096 ? blocks : 4096);
+  const int box_blocks = (int)(blocks < 1216 ? blocks : 1216);
   bbox_kernel<<<box_blocks, kThreads, 0, st>>>(in, n, box);
   plan_kernel<<<1, 32, 0, st>>>(box, L.dir_bits, L.pos_bits, plan);
   key_kernel<<<(unsigned)blocks, kThreads, 0, st>>>(in, n, plan, keys, counts);
