@@ -341,8 +341,12 @@ int rbg_scene_flat(const rbg_scene* scene, rbg_flat_scene* out);
 int rbg_scene_upload(rbg_scene* scene);
 
 /* AOpticsManager::TraceNonSequential over n rays whose buffers live in
- * DEVICE memory; asynchronous on `stream` (a cudaStream_t, NULL = legacy
- * default).  The per-ray fates, points and directions land in `out`. */
+ * DEVICE memory, on `stream` (a cudaStream_t, NULL = legacy default); the
+ * call waits for the stream to read the trace's status back.  The per-ray
+ * fates, points and directions land in `out`.  A scene's queue head, error
+ * word and ray-order workspace serve one trace at a time: traces of the
+ * same scene must not overlap (give each concurrent stream its own
+ * scene). */
 int rbg_trace(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
               const rbg_trace_opts* opts, void* stream);
 
