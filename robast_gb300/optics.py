@@ -14,6 +14,7 @@ Objects only record parameters; evaluation happens in the native library.
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
 import os
 from typing import List, Optional
@@ -21,7 +22,7 @@ from typing import List, Optional
 import numpy as np
 
 from . import _native as N
-from .geometry import TGeoMatrix, TGeoShape
+from .geometry import TGeoBBox, TGeoMatrix, TGeoShape
 
 
 # ---------------------------------------------------------------------------
@@ -359,6 +360,118 @@ class AMultilayer:
 
     def GetThickness(self, i):
         return self.layers[i][1]
+
+    # -- evaluation (src/AMultilayer.cxx:240-731, include/AMultilayer.h:114-225) --
+    # Every call below runs on the GPU through rbg_multilayer_rt, in FP64.
+    # Angles may be complex; wavelengths are in the unit of the thicknesses.
+    # Reflectance and transmittance are returned, and also stored into
+    # ctypes.c_double out-arguments (or list-like ones for the vector forms)
+    # when given, as the reference's PyROOT calls pass them.
+    def _state(self):
+        return (tuple((id(ix), d, c) for ix, d, c in self.layers), self.precalc)
+
+    def _scene(self, reverse=False):
+        """(scene, multilayer id) of a one-mirror scene whose border
+        condition holds this stack (reversed: the layers bottom to top,
+        which is CoherentTMM's `reverse`); rebuilt when the stack changes."""
+        key = (self._state(), bool(reverse))
+        cache = self.__dict__.setdefault("_scenes", {})
+        if key not in cache:
+            from .manager import AOpticsManager
+
+            ml = self
+            if reverse:
+                ml = AMultilayer(self.layers[-1][0], self.layers[0][0])
+                ml.layers = list(reversed(self.layers))
+            man = AOpticsManager("multilayer", "multilayer evaluation")
+            world = AOpticalComponent("world", TGeoBBox("world_box", 10.0, 10.0, 10.0))
+            man.SetTopVolume(world)
+            mirror = AMirror("coating", TGeoBBox("coating_box", 1.0, 1.0, 1.0))
+            world.AddNode(mirror, 1)
+            ABorderSurfaceCondition(world, mirror).SetMultilayer(ml)
+            scene = man.CloseGeometry()
+            cache.clear()
+            cache[key] = (man, scene, scene.builder.multilayer_ids[id(ml)])
+        _, scene, mid = cache[key]
+        return scene, mid
+
+    def _eval(self, mode, pol, th, lam, reverse=False):
+        import torch
+
+        scene, mid = self._scene(reverse)
+        th = np.atleast_1d(np.asarray(th, dtype=complex))
+        lam = np.atleast_1d(np.asarray(lam, dtype=float))
+        th, lam = np.broadcast_arrays(th, lam)
+        n = th.size
+        dev = torch.device("cuda", torch.cuda.current_device())
+        t_re = torch.tensor(np.ascontiguousarray(th.real.ravel()), dtype=torch.float64, device=dev)
+        t_im = torch.tensor(np.ascontiguousarray(th.imag.ravel()), dtype=torch.float64, device=dev)
+        lv = torch.tensor(np.ascontiguousarray(lam.ravel()), dtype=torch.float64, device=dev)
+        R = torch.empty(n, dtype=torch.float64, device=dev)
+        T = torch.empty(n, dtype=torch.float64, device=dev)
+        st = torch.cuda.current_stream().cuda_stream
+        N.check(N.lib().rbg_multilayer_rt(scene.handle, mid, mode, pol, n, t_re.data_ptr(), t_im.data_ptr(),
+                                          lv.data_ptr(), R.data_ptr(), T.data_ptr(), C.c_void_p(st)),
+                "rbg_multilayer_rt")
+        return R.cpu().numpy(), T.cpu().numpy()
+
+    @staticmethod
+    def _out(scalar, R, T, reflectance, transmittance):
+        if scalar:
+            r, t = float(R[0]), float(T[0])
+            for o, v in ((reflectance, r), (transmittance, t)):
+                if o is not None:
+                    o.value = v
+            return r, t
+        for o, v in ((reflectance, R), (transmittance, T)):
+            if o is not None:
+                if hasattr(o, "clear"):
+                    o.clear()
+                for x in v:
+                    (o.append if hasattr(o, "append") else o.push_back)(float(x))
+        return R, T
+
+    def CoherentTMM(self, polarization, th_0, lam_vac, reflectance=None, transmittance=None, reverse=False):
+        """R and T of one polarisation (kS, kP); `reverse` traverses the
+        stack from the bottom (src/AMultilayer.cxx:240-481)."""
+        R, T = self._eval(0, int(polarization), th_0, lam_vac, reverse)
+        return self._out(True, R, T, reflectance, transmittance)
+
+    def CoherentTMMS(self, th_0, lam_vac, reflectance=None, transmittance=None):
+        return self.CoherentTMM(self.kS, th_0, lam_vac, reflectance, transmittance)
+
+    def CoherentTMMP(self, th_0, lam_vac, reflectance=None, transmittance=None):
+        return self.CoherentTMM(self.kP, th_0, lam_vac, reflectance, transmittance)
+
+    def CoherentTMMMixed(self, th_0, lam_vac, reflectance=None, transmittance=None):
+        """Mean of p and s, or the precalculated table when one was declared
+        (include/AMultilayer.h:114-131).  Either argument may be a sequence
+        (the reference's vector overloads, :132-225); the results are then
+        arrays."""
+        scalar = np.ndim(th_0) == 0 and np.ndim(lam_vac) == 0 and not hasattr(th_0, "__len__") \
+            and not hasattr(lam_vac, "__len__")
+        R, T = self._eval(2, 2, list(th_0) if hasattr(th_0, "__len__") else th_0,
+                          list(lam_vac) if hasattr(lam_vac, "__len__") else lam_vac)
+        return self._out(scalar, R, T, reflectance, transmittance)
+
+    def IncoherentTMM(self, polarization, th_0, lam_vac, reflectance=None, transmittance=None):
+        """R and T of one polarisation with incoherent layers
+        (src/AMultilayer.cxx:555-731)."""
+        R, T = self._eval(1, int(polarization), th_0, lam_vac)
+        return self._out(True, R, T, reflectance, transmittance)
+
+    def IncoherentTMMS(self, th_0, lam_vac, reflectance=None, transmittance=None):
+        return self.IncoherentTMM(self.kS, th_0, lam_vac, reflectance, transmittance)
+
+    def IncoherentTMMP(self, th_0, lam_vac, reflectance=None, transmittance=None):
+        return self.IncoherentTMM(self.kP, th_0, lam_vac, reflectance, transmittance)
+
+    def IncoherentTMMMixed(self, th_0, lam_vac, reflectance=None, transmittance=None):
+        """Mean of p and s, or the precalculated table when one was declared
+        (include/AMultilayer.h:133-149)."""
+        mode = 2 if self.precalc is not None else 1
+        R, T = self._eval(mode, 2, th_0, lam_vac)
+        return self._out(True, R, T, reflectance, transmittance)
 
 
 # ---------------------------------------------------------------------------
