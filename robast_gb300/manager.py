@@ -15,7 +15,7 @@ import numpy as np
 
 from . import _native as N
 from .geometry import TGeoCompositeShape, TGeoMatrix, TGeoShape
-from .optics import (AFocalSurface, ALens, AMirror, AMultilayer, AOpticalComponent, ARefractiveIndex,
+from .optics import (AFocalSurface, ALens, AMirror, AMultilayer, AObscuration, AOpticalComponent, ARefractiveIndex,
                      TGraph, TGraph2D, TGeoVolume, TH2)
 
 SPEED_OF_LIGHT = 299792458.0  # m/s
@@ -83,6 +83,38 @@ class ARay:
     def GetPoint(self, i):
         """Point i (x, y, z, t); the start point is point 0."""
         return np.array(self.points[i])
+
+    def SetLambda(self, lam):
+        self.lam = float(lam)
+
+    # fate setters (include/ARay.h:47-52)
+    def Absorb(self):
+        self.status = ARay.kAbsorb
+
+    def Exit(self):
+        self.status = ARay.kExit
+
+    def Focus(self):
+        self.status = ARay.kFocus
+
+    def Stop(self):
+        self.status = ARay.kStop
+
+    def Suspend(self):
+        self.status = ARay.kSuspend
+
+    def FindNode(self, name: str):
+        """The node of the history named exactly `name` ("<volume>_<copy>"),
+        None if none (include/ARay.h:46-48, TObjArray::FindObject)."""
+        names = getattr(self, "node_names", None) or []
+        for nd in self.nodes:
+            if 0 <= nd < len(names) and names[nd] == name:
+                return name
+        return None
+
+    def GetNodeHistory(self):
+        """Physical node ids of the history (-1: outside the top volume)."""
+        return list(self.nodes)
 
     def FindNodeNumberStartWith(self, name: str) -> int:
         """Index in the node history of the first node whose TGeoNode name
@@ -664,6 +696,15 @@ class AOpticsManager:
 
     def IsFocalSurface(self, vol):
         return isinstance(vol, AFocalSurface)
+
+    def IsObscuration(self, vol):
+        return isinstance(vol, AObscuration)
+
+    def IsOpticalComponent(self, vol):
+        """An AOpticalComponent that is none of the four special kinds
+        (include/AOpticsManager.h:82-90)."""
+        return isinstance(vol, AOpticalComponent) and not isinstance(vol, (ALens, AMirror, AFocalSurface,
+                                                                           AObscuration))
 
     def trace_options(self, precision=None) -> N.TraceOpts:
         o = N.TraceOpts()

@@ -603,6 +603,12 @@ class ABorderSurfaceCondition:
         if component1 is not None:
             component1.AddBorderSurfaceCondition(self)
 
+    def GetComponent1(self):
+        return self.component1
+
+    def GetComponent2(self):
+        return self.component2
+
     def SetGaussianRoughness(self, sigma):
         self.sigma = abs(float(sigma))
 

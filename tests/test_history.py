@@ -114,3 +114,31 @@ def test_single_ray_keeps_full_history():
     # the mirror hit is on the paraboloid z = r^2 / 4f below the focus
     x, y, z, _ = ray.GetPoint(k + 1)
     assert abs(z - (x * x + y * y) / (4 * 800.0)) < 1e-3
+
+
+def test_ray_setters_and_node_lookup():
+    ray = ARay(0, 400e-7, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, -1.0)
+    for set_, check in ((ray.Absorb, ray.IsAbsorbed), (ray.Exit, ray.IsExited), (ray.Focus, ray.IsFocused),
+                        (ray.Stop, ray.IsStopped), (ray.Suspend, ray.IsSuspended)):
+        set_()
+        assert check()
+    ray.SetLambda(500e-7)
+    assert ray.GetLambda() == 500e-7
+    ray.node_names = ["world_1", "mirror_3"]
+    ray.nodes = [0, 1, -1]
+    assert ray.FindNode("mirror_3") == "mirror_3" and ray.FindNode("mirror") is None
+    assert ray.FindNodeStartWith("mir") == "mirror_3" and ray.FindNodeNumberStartWith("mir") == 1
+    assert ray.GetNodeHistory() == [0, 1, -1]
+
+
+def test_manager_classification_and_border_components():
+    from robast_gb300 import ABorderSurfaceCondition, AFocalSurface, ALens, AObscuration
+    man = _nested_manager()
+    world = man.GetTopVolume()
+    mir = AMirror("m2", TGeoBBox("b2", 1, 1, 1))
+    obs = AObscuration("o", TGeoBBox("b3", 1, 1, 1))
+    plain = AOpticalComponent("c", TGeoBBox("b4", 1, 1, 1))
+    assert man.IsObscuration(obs) and not man.IsObscuration(mir)
+    assert man.IsOpticalComponent(plain) and not man.IsOpticalComponent(mir)
+    cond = ABorderSurfaceCondition(world, mir)
+    assert cond.GetComponent1() is world and cond.GetComponent2() is mir
