@@ -176,6 +176,11 @@ class OpticsManager {
   void SetSeed(uint64_t seed) { opts_.seed = seed; }
   void SetRayIdOffset(uint64_t first_id) { opts_.ray_id_offset = first_id; }
   void SetPrecision(int precision) { opts_.precision = precision; }
+  // mixed tracer: refill threshold (0: the scene's tuned value) and the
+  // take-up order (RBG_ORDER_SPATIAL / RBG_ORDER_INPUT); neither changes
+  // a result
+  void SetCompaction(int threshold) { opts_.compaction = threshold; }
+  void SetRayOrder(int order) { opts_.ray_order = order; }
   const rbg_trace_opts& options() const { return opts_; }
 
   // Traces the rays still running in `rays` (host buffers) and updates them

@@ -112,6 +112,9 @@ static void check_cpu() {
   man.SetLimit(7);
   man.DisableFresnelReflection(true);
   EXPECT(man.GetLimit() == 7 && man.IsFresnelReflectionDisabled());
+  man.SetCompaction(32);
+  man.SetRayOrder(RBG_ORDER_INPUT);
+  man.SetRayOrder(RBG_ORDER_SPATIAL);
 }
 
 static void check_gpu() {
