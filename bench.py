@@ -152,10 +152,11 @@ def grad_bench(batch, rays, steps, device, N, torch):
     """Gradient evaluations per second of the summed per-field RMS spot
     radius w.r.t. the 22 Schwarzschild-Couder parameters: adjoint (mixed
     forward with hit records + one backward) vs central finite differences
-    with the plain FP64 tracer (2 x 22 traces), same rays.  Both losses run
-    over the rays whose fate is the same in all 45 traces: a ray that turns
-    from focused to obscured between the +h and -h traces is a jump that
-    finite differences see and a derivative does not."""
+    (2 x 22 traces) with the plain FP64 tracer and with the mixed tracer,
+    same rays.  The losses run over the rays whose fate is the same in all
+    89 traces: a ray that turns from focused to obscured between the +h and
+    -h traces is a jump that finite differences see and a derivative does
+    not.  The FP64 differences are the accuracy reference."""
     from robast_gb300 import adjoint as A
 
     build = A.sc_builder()
@@ -171,23 +172,26 @@ def grad_bench(batch, rays, steps, device, N, torch):
     res = device.alloc_result(rays["x"].numel(), rays["x"].device)
     outs = []
 
-    def trace_fp64(p):
-        man, _ = build(p)
-        device.trace(man, rays, res, precision=N.PREC_FP64)
-        f = res["status"] == N.RBG_FOCUS
-        outs.append(f)
-        return res["x"].clone(), res["y"].clone()
+    def fd(precision):
+        def trace(p):
+            man, _ = build(p)
+            device.trace(man, rays, res, precision=precision)
+            outs.append(res["status"] == N.RBG_FOCUS)
+            return res["x"].clone(), res["y"].clone()
 
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    pts = []
-    for k in range(len(p0)):
-        pp, pm = p0.copy(), p0.copy()
-        pp[k] += h[k]
-        pm[k] -= h[k]
-        pts.append((trace_fp64(pp), trace_fp64(pm)))
-    torch.cuda.synchronize()
-    t_fd = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pts = []
+        for k in range(len(p0)):
+            pp, pm = p0.copy(), p0.copy()
+            pp[k] += h[k]
+            pm[k] -= h[k]
+            pts.append((trace(pp), trace(pm)))
+        torch.cuda.synchronize()
+        return pts, time.perf_counter() - t0
+
+    pts64, t_fd64 = fd(N.PREC_FP64)
+    ptsmx, t_fdmx = fd(N.PREC_MIXED)
     stable = outs[0].clone()
     for f in outs[1:]:
         stable &= f
@@ -206,15 +210,27 @@ def grad_bench(batch, rays, steps, device, N, torch):
     torch.cuda.synchronize()
     t_adj = (time.perf_counter() - t0) / steps
 
-    fd = np.array([(float(loss_of(*a, stable)) - float(loss_of(*b, stable))) / (2 * h[k])
-                   for k, (a, b) in enumerate(pts)])
+    def central(pts):
+        return np.array([(float(loss_of(*a, stable)) - float(loss_of(*b, stable))) / (2 * h[k])
+                         for k, (a, b) in enumerate(pts)])
+
+    fd64, fdmx = central(pts64), central(ptsmx)
     ga = g_adj.cpu().numpy()
-    scale = np.abs(fd * h).max()
-    rel = np.abs((ga - fd) * h) / np.maximum(np.abs(fd * h), 1e-3 * scale)
+    # relative error per parameter in the loss change over one FD step
+    # (d loss/d p * h), floored at 1e-3 of the largest such change, and the
+    # plain relative error beside it
+    scale = np.abs(fd64 * h).max()
+    rel = np.abs((ga - fd64) * h) / np.maximum(np.abs(fd64 * h), 1e-3 * scale)
+    rel_plain = np.abs(ga - fd64) / np.maximum(np.abs(fd64), 1e-300)
     return {"unit": "grad-evals/s", "params": len(p0), "rays": int(rays["x"].numel()),
             "rays_in_loss": int(stable.sum().item()),
-            "adjoint": 1.0 / t_adj, "finite_differences_fp64": 1.0 / t_fd, "speedup": t_fd / t_adj,
+            "adjoint": 1.0 / t_adj, "finite_differences_fp64": 1.0 / t_fd64,
+            "finite_differences_mixed": 1.0 / t_fdmx,
+            "speedup_vs_fd_fp64": t_fd64 / t_adj, "speedup_vs_fd_mixed": t_fdmx / t_adj,
             "max_rel_err_vs_fd": float(rel.max()), "rel_err_vs_fd": [float(v) for v in rel],
+            "max_plain_rel_err_vs_fd": float(rel_plain.max()),
+            "plain_rel_err_vs_fd": [float(v) for v in rel_plain],
+            "fd_mixed_vs_fd_fp64_max_rel": float(np.max(np.abs(fdmx - fd64) * h) / scale),
             "loss": "sum over the 5 field angles of the RMS spot radius, rays with a stable fate"}
 
 
@@ -234,6 +250,89 @@ def cpu_baseline(man, batch, sample):
     return {"value": sample / dt, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"{sample} rays spread evenly over the {len(batch['x'])}-ray batch (every group), oracle FP64, "
                       f"{cores} threads, contiguous chunks"}, st
+
+
+def spot_r80(device, res, group, g, lims, nbins=500):
+    """r80 of group g's focused rays: the device histogram through the
+    device ContainmentRadius."""
+    h = device.focal_histogram(res, nbins, lims[0], lims[1], nbins, lims[2], lims[3], mask=group == g)
+    return device.containment_radius(h, lims[0], lims[1], lims[2], lims[3], 0.8)[0]
+
+
+def oracle_r80(x, y, lims, nbins=500):
+    """r80 from host focal points: TH2D::Fill's bins, the oracle's search."""
+    import oracle_ref
+
+    fx = (x - lims[0]) / (lims[1] - lims[0]) * nbins
+    fy = (y - lims[2]) / (lims[3] - lims[2]) * nbins
+    ok = (fx >= 0) & (fy >= 0) & (fx < nbins) & (fy < nbins)
+    h = np.zeros((nbins, nbins))
+    np.add.at(h, (fx[ok].astype(np.int64), fy[ok].astype(np.int64)), 1.0)
+    return oracle_ref.containment_radius(h, lims[0], lims[1], lims[2], lims[3], 0.8)[0]
+
+
+def field_limits(x, y, focus, group, n_groups):
+    """Per field: a histogram window of +-6 sigma about the spot centroid."""
+    lims = []
+    for g in range(n_groups):
+        sel = focus & (group == g)
+        if sel.sum() < 10:
+            lims.append(None)
+            continue
+        mx, my = x[sel].mean(), y[sel].mean()
+        hw = 6 * max(np.sqrt(x[sel].var() + y[sel].var()), 1e-6)
+        lims.append((mx - hw, mx + hw, my - hw, my + hw))
+    return lims
+
+
+def parity_vs_oracle(man, batch, res, device, N, cores):
+    """The whole batch traced by the FP64 oracle on all host cores: ray by
+    ray agreement of the GPU result (fates, point counts and last nodes
+    exactly; positions and directions), and r80 of every field from the GPU
+    (device histogram + device ContainmentRadius) against r80 from the
+    oracle's own focal points (oracle ContainmentRadius).  The oracle's wall
+    time is the CPU baseline."""
+    import oracle_ref
+
+    from robast_gb300 import configs
+
+    arr = configs.to_array(batch)
+    t0 = time.perf_counter()
+    st, ref = oracle_ref.trace(man, arr, threads=cores)
+    dt = time.perf_counter() - t0
+    gpu = {k: res[k].cpu().numpy() for k in ("status", "npoints", "last_node", "x", "y", "z", "dx", "dy", "dz")}
+    same = (gpu["status"] == ref["status"]) & (gpu["npoints"] == ref["npoints"]) & \
+           (gpu["last_node"] == ref["last_node"])
+    bad = np.nonzero(~same)[0]
+    pos = max(float(np.max(np.abs(gpu[k][same] - ref[k][same]) / np.maximum(1.0, np.abs(ref[k][same])),
+                           initial=0)) for k in ("x", "y", "z"))
+    dirs = max(float(np.max(np.abs(gpu[k][same] - ref[k][same]), initial=0)) for k in ("dx", "dy", "dz"))
+    group = batch["group"]
+    n_groups = int(group.max()) + 1
+    focus = ref["status"] == N.RBG_FOCUS
+    lims = field_limits(ref["x"], ref["y"], focus, group, n_groups)
+    import torch
+
+    gdev = torch.as_tensor(np.ascontiguousarray(group, dtype=np.int32)).to(res["x"].device)
+    r_gpu, r_orc = [], []
+    for g, lm in enumerate(lims):
+        if lm is None:
+            continue
+        r_gpu.append(spot_r80(device, res, gdev, g, lm))
+        sel = focus & (group == g)
+        r_orc.append(oracle_r80(ref["x"][sel], ref["y"][sel], lm))
+    rel = [abs(a - b) / b for a, b in zip(r_gpu, r_orc) if b > 0]
+    block = {"rays": int(len(same)), "oracle_status": int(st),
+             "fate_mismatches": int(bad.size), "fate_mismatch_rays": [int(i) for i in bad[:10]],
+             "max_pos_rel_err": pos, "max_dir_abs_err": dirs,
+             "r80_cm_gpu": r_gpu, "r80_cm_oracle": r_orc, "r80_max_rel_diff": max(rel) if rel else None,
+             "compared": "status, npoints and last_node exactly; x, y, z relative to max(1, |x|); "
+                         "r80 = 80 % containment radius (AGeoUtil::ContainmentRadius) of each field's "
+                         "500 x 500 focal-plane histogram over +-6 sigma"}
+    cb = {"value": len(same) / dt, "unit": UNIT, "cores": cores, "kind": "port",
+          "sample": f"the whole {len(same)}-ray batch, oracle FP64, {cores} threads, contiguous chunks "
+                    "(the trace the parity check uses)"}
+    return block, cb
 
 
 def run_reference(args):
@@ -477,6 +576,8 @@ def main():
     ap.add_argument("--rays", type=int, default=0, help="rays per step (default: the workload's size)")
     ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE)
     ap.add_argument("--compaction", type=int, default=0, help="mixed tracer refill threshold (0: tuned)")
+    ap.add_argument("--no-parity", dest="parity", action="store_false",
+                    help="skip the whole-batch oracle trace (the CPU baseline then times a sample)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -555,6 +656,9 @@ def main():
             t = float(tt.item())
         return t, nl, ck.summary()
 
+    # every device allocation of the trace made up front (scene tables,
+    # take-up order workspace, host pipeline slots)
+    device.reserve(man, n)
     # autotune the mixed tracer's compaction threshold on this batch (outside
     # the timed region, like the warm-up) unless one was given
     tuned = None
@@ -567,27 +671,33 @@ def main():
     n_groups = int(batch["group"].max()) + 1
     compare = None
     if not args.no_compare and prec != N.PREC_FP64:
+        # the plain FP64 tracer: one thread per ray in input order (the
+        # metric's denominator), and the same tracer in the chosen form's
+        # take-up order, which separates the precision gain from the order's
         res64 = device.alloc_result(n, f"cuda:{local}")
+        man.ray_order = N.ORDER_INPUT
         ms64, _, _ = timed(N.PREC_FP64, res64)
-        agree = float((res64["status"] == res["status"]).double().mean().item())
-        d80 = {"chosen": [], "fp64": []}
-        mom = device.focal_moments(res64, group, n_groups).cpu().numpy()
-        # every group up to 16; beyond that 16 spread over the range
-        for g in sorted(set(np.linspace(0, n_groups - 1, min(n_groups, 16)).astype(int).tolist())):
-            cnt = mom[g, 0]
-            if cnt < 10:
+        man.ray_order = N.ORDER_SPATIAL
+        ms64o, _, _ = timed(N.PREC_FP64, res64)
+        same = (res64["status"] == res["status"]) & (res64["npoints"] == res["npoints"]) & \
+               (res64["last_node"] == res["last_node"])
+        agree = float(same.double().mean().item())
+        h64 = {k: res64[k].cpu().numpy() for k in ("status", "x", "y")}
+        lims = field_limits(h64["x"], h64["y"], h64["status"] == N.RBG_FOCUS, batch["group"], n_groups)
+        r80 = {"chosen": [], "fp64": []}
+        for g, lm in enumerate(lims):
+            if lm is None:
                 continue
-            mx, my = mom[g, 1] / cnt, mom[g, 2] / cnt
-            sd = max(np.sqrt(max(mom[g, 3] / cnt - mx * mx, 0) + max(mom[g, 4] / cnt - my * my, 0)), 1e-6)
-            hw = 6 * sd
-            for key, rr in (("chosen", res), ("fp64", res64)):
-                h = device.focal_histogram(rr, 500, mx - hw, mx + hw, 500, my - hw, my + hw, mask=group == g)
-                d80[key].append(device.containment_radius(h, mx - hw, mx + hw, my - hw, my + hw, 0.8)[0])
-        rel = [abs(a - b) / b for a, b in zip(d80["chosen"], d80["fp64"]) if b > 0]
+            r80["chosen"].append(spot_r80(device, res, group, g, lm))
+            r80["fp64"].append(spot_r80(device, res64, group, g, lm))
+        rel = [abs(a - b) / b for a, b in zip(r80["chosen"], r80["fp64"]) if b > 0]
         compare = {"plain_fp64_rays_per_s": n * ws / (ms64 / 1e3), "plain_fp64_ms_per_step": ms64,
-                   "speedup_vs_plain_fp64": ms64 / ms, "fate_agreement": agree,
-                   "d80_cm_chosen": d80["chosen"], "d80_cm_fp64": d80["fp64"],
-                   "d80_max_rel_diff": max(rel) if rel else None}
+                   "speedup_vs_plain_fp64": ms64 / ms,
+                   "plain_fp64_ordered_rays_per_s": n * ws / (ms64o / 1e3),
+                   "speedup_vs_plain_fp64_ordered": ms64o / ms,
+                   "fate_agreement": agree, "fate_mismatches": int((~same).sum().item()),
+                   "r80_cm_chosen": r80["chosen"], "r80_cm_fp64": r80["fp64"],
+                   "r80_max_rel_diff": max(rel) if rel else None}
         del res64
 
     # end to end through the host-buffer C ABI call
@@ -646,7 +756,11 @@ def main():
             "e2e": e2e, "clocks": clocks, "vs_plain_fp64": compare}
     if not args.no_grad and ws == 1 and args.workload == "schwarzschild_couder":
         line["grad"] = grad_bench(batch, rays, max(1, min(args.steps, 3)), device, N, torch)
-    cb, _ = cpu_baseline(man, batch, args.cpu_sample)
+    if args.parity and ws == 1:
+        block, cb = parity_vs_oracle(man, batch, res, device, N, os.cpu_count() or 1)
+        line["parity_vs_oracle"] = block
+    else:
+        cb, _ = cpu_baseline(man, batch, args.cpu_sample)
     line["cpu_baseline"] = cb
     print(json.dumps(line))
 

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define RBG_ABI_VERSION 1
+#define RBG_ABI_VERSION 2
 
 /* ---- status codes (every entry point returns one) --------------------- */
 enum {
@@ -300,13 +300,23 @@ typedef struct {
    * (rbg_scene_autotune), else the library default.  Results do not depend
    * on it. */
   int32_t compaction;
-  /* mixed tracer: the order in which the rays are taken up.
+  /* the order in which the rays are taken up.
    * RBG_ORDER_SPATIAL (default) groups the rays by a cell of their
    * direction and, within it, of their start point, so the lanes of a warp
-   * follow neighbouring paths; RBG_ORDER_INPUT takes them in input order.  Every ray keeps its index for its inputs, outputs and
-   * random draws: results do not depend on it.  Batches under 2^14 rays,
-   * and rbg_trace_noalloc, always use input order. */
+   * follow neighbouring paths; RBG_ORDER_INPUT takes them in input order.
+   * Every ray keeps its index for its inputs, outputs and random draws:
+   * results do not depend on it.  Both tracers honour it.  Batches under
+   * 2^14 rays, batches beyond the scene's reserved workspace
+   * (rbg_scene_reserve) without a workspace of their own (below), and
+   * rbg_trace_noalloc use input order. */
   int32_t ray_order;
+  /* Optional DEVICE workspace of the caller (256-byte aligned) for the
+   * take-up order of rbg_trace: used when workspace_bytes >=
+   * rbg_trace_workspace_bytes(n), otherwise the scene's reserved one is
+   * (NULL / 0: the scene's).  It lets callers that rebuild scenes
+   * (parameter scans, gradient steps) keep one buffer for all of them. */
+  void* workspace;
+  uint64_t workspace_bytes;
 } rbg_trace_opts;
 
 enum { RBG_ORDER_SPATIAL = 0, RBG_ORDER_INPUT = 1 };
@@ -339,14 +349,30 @@ int rbg_scene_flat(const rbg_scene* scene, rbg_flat_scene* out);
 /* Copy the flattened tables to the current CUDA device (done lazily by
  * rbg_trace when needed). */
 int rbg_scene_upload(rbg_scene* scene);
+/* Make, on the current device, every device allocation the scene needs to
+ * trace batches of up to max_rays rays: the scene tables (as
+ * rbg_scene_upload), the take-up order workspace of rbg_trace, and the two
+ * pipeline slots of rbg_trace_host for hist_cap history points per ray (no
+ * counterpart in the reference, whose AOpticsManager allocates per ray on
+ * the heap).  After it, rbg_trace allocates nothing; a reservation smaller
+ * than an earlier one keeps the larger workspaces.  Waits for the device
+ * when a workspace grows. */
+int rbg_scene_reserve(rbg_scene* scene, int64_t max_rays, int32_t hist_cap);
+/* Bytes of the take-up order workspace rbg_trace uses for n rays (0 for
+ * batches it takes up in input order). */
+size_t rbg_trace_workspace_bytes(int64_t n_rays);
 
 /* AOpticsManager::TraceNonSequential over n rays whose buffers live in
  * DEVICE memory, on `stream` (a cudaStream_t, NULL = legacy default); the
  * call waits for the stream to read the trace's status back.  The per-ray
- * fates, points and directions land in `out`.  A scene's queue head, error
- * word and ray-order workspace serve one trace at a time: traces of the
- * same scene must not overlap (give each concurrent stream its own
- * scene). */
+ * fates, points and directions land in `out`.  It allocates no device
+ * memory: a scene not yet on the current device is uploaded first (as
+ * rbg_scene_upload), and the spatial take-up order runs only when
+ * rbg_scene_reserve sized its workspace for at least n rays (otherwise the
+ * rays are taken up in input order, with the same results).  A scene's
+ * queue head, error word and ray-order workspace serve one trace at a time:
+ * traces of the same scene must not overlap (give each concurrent stream
+ * its own scene). */
 int rbg_trace(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
               const rbg_trace_opts* opts, void* stream);
 
@@ -421,7 +447,9 @@ int rbg_scene_autotune(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
 
 /* Same, with HOST buffers: copies the rays in, traces, copies the results
  * out and synchronises (the call a ROOT-side AOpticsManager binding makes,
- * src/AOpticsManager.cxx:523). */
+ * src/AOpticsManager.cxx:523).  Its device staging (two pipeline slots of
+ * up to 2^21 rays) is the scene's workspace: sized by rbg_scene_reserve, or
+ * grown by the call itself when the reservation is smaller. */
 int rbg_trace_host(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
                    const rbg_trace_opts* opts);
 
@@ -436,8 +464,11 @@ int rbg_trace_host(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
  * RBG_ERR_TOO_LARGE.  Buffers as rbg_trace (DEVICE rays and results); only
  * opts->precision == RBG_PREC_MIXED is accepted.  Calls share the array and
  * it keeps the last call's contents: calls that overlap on the GPU race.
- * The first call on a device looks up the array's address with that device
- * current; make it before any stream capture begins. */
+ * Each call copies the scene tables in from host memory and waits for its
+ * stream to read the error word back.  The first call on a device looks up
+ * the array's address with that device current; make it before any stream
+ * capture begins.  It sets no device limit: no tracer kernel recurses, and
+ * the driver sizes each launch's stack to the kernel's static need. */
 int rbg_trace_noalloc(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
                       const rbg_trace_opts* opts, void* stream);
 
@@ -463,12 +494,22 @@ int rbg_focal_histogram(int64_t n, const uint8_t* status, const double* x,
                         void* stream);
 
 /* AGeoUtil::ContainmentRadius (src/AGeoUtil.cxx:198-308) on a DEVICE
- * histogram counts[ix*ny+iy]; r, x, y are host outputs.  The O(nbins^2)
- * SumInRadius probes (src/AGeoUtil.cxx:18-42) run as device reductions. */
+ * histogram counts[ix*ny+iy] with TH2 bin centres; r, x, y are host
+ * outputs.  The whole search, its initial moments and every SumInRadius
+ * probe (src/AGeoUtil.cxx:18-42) run on the GPU in one launch of one
+ * thread-block cluster; nothing is allocated.  The call waits for
+ * `stream`; concurrent calls are serialised.  RBG_ERR_CAP if the search
+ * ran past 200000 histogram passes (never expected). */
 int rbg_containment_radius(const double* counts, int32_t nx, double xlo,
                            double xhi, int32_t ny, double ylo, double yhi,
                            double fraction, double* r, double* x, double* y,
                            void* stream);
+/* The same, stream-ordered: out (DEVICE, 4 doubles) receives r, x, y and a
+ * status (0, or -1 for the pass cap); the call returns after the launch. */
+int rbg_containment_radius_async(const double* counts, int32_t nx,
+                                 double xlo, double xhi, int32_t ny,
+                                 double ylo, double yhi, double fraction,
+                                 double* out, void* stream);
 
 /* ---- gradients ---------------------------------------------------------- */
 /* Parameters the adjoint differentiates.  Shifts and rotations are small

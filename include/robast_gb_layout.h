@@ -118,5 +118,9 @@
  * lists; exceeding them sets RBG_ERR_CAP for the ray's trace call */
 #define RBG_ROUGH_MAX_TRIES 1000
 #define RBG_MAX_XINGS 48
+/* deepest TGeoCompositeShape tree the flattener accepts (a composite of two
+ * primitives has depth 1); the device walks deeper trees with explicit
+ * stacks of this many frames plus one, so no kernel recurses */
+#define RBG_MAX_COMPOSITE_DEPTH 6
 
 #endif /* ROBAST_GB_LAYOUT_H */

@@ -146,7 +146,8 @@ class Bunches(C.Structure):
 class TraceOpts(C.Structure):
     _fields_ = [("limit", C.c_int32), ("disable_fresnel", C.c_int32), ("seed", C.c_uint64),
                 ("ray_id_offset", C.c_uint64), ("precision", C.c_int32),
-                ("block_size", C.c_int32), ("compaction", C.c_int32), ("ray_order", C.c_int32)]
+                ("block_size", C.c_int32), ("compaction", C.c_int32), ("ray_order", C.c_int32),
+                ("workspace", C.c_void_p), ("workspace_bytes", C.c_uint64)]
 
 
 class NativeError(RuntimeError):
@@ -185,6 +186,9 @@ def _declare(L):
     L.rbg_scene_destroy.restype = None
     L.rbg_scene_flat.argtypes = [vp, C.POINTER(FlatScene)]
     L.rbg_scene_upload.argtypes = [vp]
+    L.rbg_scene_reserve.argtypes = [vp, C.c_int64, C.c_int32]
+    L.rbg_trace_workspace_bytes.argtypes = [C.c_int64]
+    L.rbg_trace_workspace_bytes.restype = C.c_size_t
     L.rbg_trace.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts), vp]
     L.rbg_trace_host.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts)]
     L.rbg_scene_autotune.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts), vp,
@@ -196,6 +200,8 @@ def _declare(L):
                                       C.c_int32, C.c_double, C.c_double, vp, vp]
     L.rbg_containment_radius.argtypes = [vp, C.c_int32, C.c_double, C.c_double, C.c_int32,
                                          C.c_double, C.c_double, C.c_double, _dp, _dp, _dp, vp]
+    L.rbg_containment_radius_async.argtypes = [vp, C.c_int32, C.c_double, C.c_double, C.c_int32,
+                                               C.c_double, C.c_double, C.c_double, vp, vp]
     L.rbg_shoot.argtypes = [C.c_int32, _dp, C.c_int64, _dp, _dp, _dp, C.c_uint64, C.c_uint64,
                             C.c_double, C.POINTER(Rays)]
     fp = C.POINTER(C.c_float)

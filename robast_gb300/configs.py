@@ -382,7 +382,10 @@ def _sct_unit(world, tag, origin, corrector_index, coating, decenter=(0.0, 0.0),
 
 
 def schmidt_cassegrain(n_rays: int = 100_000_000, n_samples: int = 256, seed: int = 5,
-                       decenter_sigma: float = 0.02 * cm, tilt_sigma: float = 0.1e-3):
+                       decenter_sigma: float = 0.02 * cm, tilt_sigma: float = 0.1e-3, coating_table=None):
+    """coating_table: None (per-ray CoherentTMMMixed of the stack), or the
+    (lam_nbins, lam_min, lam_max, th_nbins, th_min, th_max) arguments of
+    AMultilayer::PreCalculateCoherentTMM for the stack."""
     man = AOpticsManager("manager", "Schmidt-Cassegrain")
     man.DisableFresnelReflection(True)
     side = int(math.ceil(math.sqrt(n_samples)))
@@ -393,6 +396,8 @@ def schmidt_cassegrain(n_rays: int = 100_000_000, n_samples: int = 256, seed: in
     air = ARefractiveIndex(1.0, 0.0)
     silica = ASellmeierFormula(*LITHOSIL_Q)
     coating = _quarter_wave_stack(air, silica)
+    if coating_table is not None:
+        coating.PreCalculateCoherentTMM(*coating_table)
     rng = np.random.default_rng(seed)
     units = []
     for v in range(n_samples):

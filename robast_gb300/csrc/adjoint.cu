@@ -16,6 +16,8 @@
 // change the path and are collapsed.  Rays that refract are skipped.
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include "scene_internal.h"
 #include "device_state.cuh"
 #include "tracer.cuh"
@@ -269,12 +271,17 @@ RBG_D bool param_terms(const DevScene& S, const rbg_adjoint_param& p, int node, 
   return false;
 }
 
+// the parameter list travels by value in the launch's parameter space
+struct AdjParams {
+  rbg_adjoint_param p[kAdjMaxParams];
+};
+
 __global__ void adjoint_kernel(DevScene S, int64_t n, const uint8_t* status, const int32_t* npoints,
                                int32_t hist_cap, const double* hist_xyzt, const int32_t* hist_node,
                                const double* gx, const double* gy, const double* gz, int n_params,
-                               const rbg_adjoint_param* params_g, double* out, unsigned long long* skipped) {
+                               const AdjParams params_v, double* out, unsigned long long* skipped) {
   __shared__ rbg_adjoint_param params[kAdjMaxParams];
-  for (int k = threadIdx.x; k < n_params; k += blockDim.x) params[k] = params_g[k];
+  for (int k = threadIdx.x; k < n_params; k += blockDim.x) params[k] = params_v.p[k];
   __syncthreads();
   double acc[kAdjMaxParams];
   for (int k = 0; k < n_params; ++k) acc[k] = 0;
@@ -414,28 +421,18 @@ extern "C" int rbg_trace_adjoint(rbg_scene* s, int64_t n, const rbg_result* fwd,
     return RBG_OK;
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  // parameters and the skip counter travel in one small device block that
-  // the scene keeps for this purpose
-  size_t need = sizeof(rbg_adjoint_param) * kAdjMaxParams + 16;
-  if (s->workspace_bytes < need) {
-    if (s->workspace) cudaFree(s->workspace);
-    s->workspace = nullptr;
-    s->workspace_bytes = 0;
-    if (cudaMalloc(&s->workspace, need) != cudaSuccess) return RBG_ERR_NOMEM;
-    s->workspace_bytes = need;
-  }
-  auto* dparams = static_cast<rbg_adjoint_param*>(s->workspace);
-  auto* dskip = reinterpret_cast<unsigned long long*>(static_cast<char*>(s->workspace) +
-                                                      sizeof(rbg_adjoint_param) * kAdjMaxParams);
-  if (cudaMemcpyAsync(dparams, params, sizeof(rbg_adjoint_param) * n_params, cudaMemcpyHostToDevice, st) !=
-          cudaSuccess ||
-      cudaMemsetAsync(dskip, 0, sizeof(unsigned long long), st) != cudaSuccess)
-    return RBG_ERR_CUDA;
+  // the parameters go by value with the launch; the skip counter is a word
+  // of the scene's own error block (allocated with its tables)
+  AdjParams pv;
+  std::memset(&pv, 0, sizeof(pv));
+  for (int k = 0; k < n_params; ++k) pv.p[k] = params[k];
+  unsigned long long* dskip = s->dev->adj_skip;
+  if (cudaMemsetAsync(dskip, 0, sizeof(unsigned long long), st) != cudaSuccess) return RBG_ERR_CUDA;
   int block = 128;
   int blocks = (int)std::min<int64_t>((n + block - 1) / block, (int64_t)sm_count() * 8);
   adjoint_kernel<<<blocks, block, 0, st>>>(s->dev->view, n, fwd->status, fwd->npoints, fwd->hist_cap,
-                                            fwd->hist_xyzt, fwd->hist_node, gx, gy, gz, n_params, dparams,
-                                            dL_dparams, dskip);
+                                            fwd->hist_xyzt, fwd->hist_node, gx, gy, gz, n_params, pv, dL_dparams,
+                                            dskip);
   if (cudaGetLastError() != cudaSuccess) return RBG_ERR_CUDA;
   unsigned long long sk = 0;
   if (cudaMemcpyAsync(&sk, dskip, sizeof(sk), cudaMemcpyDeviceToHost, st) != cudaSuccess ||

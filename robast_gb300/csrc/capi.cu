@@ -1,5 +1,5 @@
-// capi.cu -- C ABI of the tracer: device upload of a flattened scene,
-// device- and host-buffer tracing and focal-plane reductions.
+// capi.cu -- C ABI of the tracer: device upload of a flattened scene, its
+// workspace reservation, and device- and host-buffer tracing.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -88,8 +88,10 @@ int ensure_device(rbg_scene* s) {
     delete d;
     return rc;
   }
+  // one 256-byte block: the error word at 0, the persistent kernel's queue
+  // head at 8, the adjoint's skip counter at 16
   void* ef = nullptr;
-  if (cudaMalloc(&ef, 16) != cudaSuccess) {
+  if (cudaMalloc(&ef, 256) != cudaSuccess) {
     for (void* p : d->allocations) cudaFree(p);
     delete d;
     return RBG_ERR_NOMEM;
@@ -97,6 +99,7 @@ int ensure_device(rbg_scene* s) {
   d->allocations.push_back(ef);
   d->err_flags = static_cast<unsigned*>(ef);
   d->counter = reinterpret_cast<unsigned long long*>(static_cast<char*>(ef) + 8);
+  d->adj_skip = reinterpret_cast<unsigned long long*>(static_cast<char*>(ef) + 16);
   v.n_nodes = (int32_t)s->nodes.size();
   v.n_borders = (int32_t)s->borders.size();
   v.n_multilayers = (int32_t)s->multilayers.size();
@@ -119,26 +122,19 @@ int ensure_device(rbg_scene* s) {
   return RBG_OK;
 }
 
-int sm_count() {
-  static int cached = 0;
-  if (cached == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev);
-    if (cached <= 0) cached = 1;
-  }
-  return cached;
-}
+// Per-device cache: a process may drive several GPUs.
+constexpr int kMaxDevices = 64;
 
-int stack_ready() {
-  static int done = 0;
-  if (!done) {
-    // the CSG walk and the rejection loops recurse/branch deeply: give each
-    // thread enough local stack for composite trees of depth <= 6
-    if (cudaDeviceSetLimit(cudaLimitStackSize, 8192) != cudaSuccess) return RBG_ERR_CUDA;
-    done = 1;
+int sm_count() {
+  static int cached[kMaxDevices] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 1;
+  if (cached[dev] == 0) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    cached[dev] = v > 0 ? v : 1;
   }
-  return RBG_OK;
+  return cached[dev];
 }
 
 int read_errors(rbg_scene* s, cudaStream_t st, unsigned* bits) {
@@ -168,11 +164,43 @@ int build_ray_order(const KernelRays& in, int64_t n, void* ws, KernelRays* sorte
 // below this many rays the mixed tracer takes rays up in input order
 constexpr int64_t kOrderMinRays = 1 << 14;
 bool want_ray_order(const rbg_trace_opts& o, int64_t n) {
-  return o.precision == RBG_PREC_MIXED && o.ray_order == RBG_ORDER_SPATIAL && n >= kOrderMinRays &&
-         ray_order_bytes(n) > 0;
+  return o.ray_order == RBG_ORDER_SPATIAL && n >= kOrderMinRays && ray_order_bytes(n) > 0;
 }
 int launch_fp64(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o,
                 cudaStream_t st, unsigned* err_flags, int* launches);
+}
+
+namespace rbg {
+int host_workspace_reserve(rbg_scene* s, int64_t max_rays, int32_t hist_cap);  // below
+}
+
+extern "C" size_t rbg_trace_workspace_bytes(int64_t n) { return n >= kOrderMinRays ? ray_order_bytes(n) : 0; }
+
+// Every device allocation a scene makes for tracing up to max_rays rays,
+// made here once on the current device: the scene tables (upload), the
+// take-up order workspace of rbg_trace and the two pipeline slots of
+// rbg_trace_host for hist_cap history points.  (No tracer kernel recurses,
+// so the per-thread stack the driver sizes at each launch from the kernel's
+// static need is enough: no stack limit is set anywhere.)  A
+// smaller reservation than an earlier one keeps the larger workspaces.
+extern "C" int rbg_scene_reserve(rbg_scene* s, int64_t max_rays, int32_t hist_cap) {
+  if (!s || max_rays < 0 || hist_cap < 0) return RBG_ERR_ARG;
+  int rc = ensure_device(s);
+  if (rc) return rc;
+  const size_t need = max_rays >= kOrderMinRays ? ray_order_bytes(max_rays) : 0;
+  if (need > s->order_ws_bytes) {
+    // the old workspace may still be read by work queued on a stream
+    if (s->order_ws && (cudaDeviceSynchronize() != cudaSuccess || cudaFree(s->order_ws) != cudaSuccess))
+      return RBG_ERR_CUDA;
+    s->order_ws = nullptr;
+    s->order_ws_bytes = 0;
+    if (cudaMalloc(&s->order_ws, need) != cudaSuccess) {
+      s->order_ws = nullptr;
+      return RBG_ERR_NOMEM;
+    }
+    s->order_ws_bytes = need;
+  }
+  return host_workspace_reserve(s, max_rays, hist_cap);
 }
 
 extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, const rbg_trace_opts* opts,
@@ -181,9 +209,9 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
   if (in->n < 0 || opts->limit <= 0) return RBG_ERR_ARG;
   if (in->n > 0 && (!in->x || !in->y || !in->z || !in->dx || !in->dy || !in->dz || !in->lambda)) return RBG_ERR_ARG;
   if (out->hist_cap < 0 || (out->hist_cap > 0 && (!out->hist_xyzt || !out->hist_node))) return RBG_ERR_ARG;
+  if (opts->workspace && (reinterpret_cast<uintptr_t>(opts->workspace) & 255)) return RBG_ERR_ARG;
   int rc = ensure_device(s);
   if (rc) return rc;
-  if ((rc = stack_ready())) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   s->last_launches = 0;
   if (in->n == 0) return RBG_OK;
@@ -191,37 +219,28 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
   KernelRays kr{in->x, in->y, in->z, in->t, in->dx, in->dy, in->dz, in->lambda};
   KernelOut ko{out->status, out->npoints, out->last_node, out->x, out->y, out->z, out->t,
                out->dx, out->dy, out->dz, out->hist_cap, out->hist_xyzt, out->hist_node};
-  if (opts->precision == RBG_PREC_MIXED) {
-    int launches = 0;
-    rbg_trace_opts o = *opts;
-    if (o.compaction == 0) o.compaction = s->tuned_compaction;
-    if (want_ray_order(o, in->n)) {
-      const size_t need = ray_order_bytes(in->n);
-      if (s->order_ws_bytes < need) {
-        // the previous workspace may still be read by work queued earlier
-        // on another stream: wait for the device before freeing it
-        if (s->order_ws && (cudaDeviceSynchronize() != cudaSuccess || cudaFree(s->order_ws) != cudaSuccess))
-          return RBG_ERR_CUDA;
-        s->order_ws = nullptr;
-        s->order_ws_bytes = 0;
-        if (cudaMalloc(&s->order_ws, need) != cudaSuccess) {
-          s->order_ws = nullptr;
-          return RBG_ERR_NOMEM;
-        }
-        s->order_ws_bytes = need;
-      }
-      if ((rc = build_ray_order(kr, in->n, s->order_ws, &kr, st))) return rc;
+  int launches = 0;
+  rbg_trace_opts o = *opts;
+  if (o.compaction == 0) o.compaction = s->tuned_compaction;
+  // the take-up order needs a workspace: the caller's, else the one
+  // rbg_scene_reserve sized; a batch beyond both is taken up in input order
+  // (same results, nothing allocated)
+  if (want_ray_order(o, in->n)) {
+    const size_t need = ray_order_bytes(in->n);
+    void* ws = nullptr;
+    if (o.workspace && o.workspace_bytes >= need) ws = o.workspace;
+    else if (s->order_ws && s->order_ws_bytes >= need) ws = s->order_ws;
+    if (ws) {
+      if ((rc = build_ray_order(kr, in->n, ws, &kr, st))) return rc;
       launches += 7;
     }
-    rc = launch_mixed(s->dev->view, kr, ko, in->n, o, st, s->dev->err_flags, s->dev->counter, &launches);
-    if (rc) return rc;
-    s->last_launches = launches;
-  } else {
-    int launches = 0;
-    rc = launch_fp64(s->dev->view, kr, ko, in->n, *opts, st, s->dev->err_flags, &launches);
-    if (rc) return rc;
-    s->last_launches = launches;
   }
+  if (o.precision == RBG_PREC_MIXED)
+    rc = launch_mixed(s->dev->view, kr, ko, in->n, o, st, s->dev->err_flags, s->dev->counter, &launches);
+  else
+    rc = launch_fp64(s->dev->view, kr, ko, in->n, o, st, s->dev->err_flags, &launches);
+  if (rc) return rc;
+  s->last_launches = launches;
   unsigned bits = 0;
   if ((rc = read_errors(s, st, &bits))) return rc;
   if (bits & ERR_BIT_NAN) return RBG_ERR_NAN;
@@ -296,6 +315,10 @@ int launch_trace(rbg_scene* s, const KernelRays& kr, const KernelOut& ko, int64_
 // between calls (freed with the scene), so repeated calls allocate nothing
 int grow_workspace(rbg_scene* s, size_t bytes, char** out) {
   if (s->workspace_bytes < bytes) {
+    // a call that failed part-way may have left copies queued on the
+    // pipeline streams: let them finish before the old block goes
+    for (cudaStream_t st : s->dev->host_streams)
+      if (st && cudaStreamSynchronize(st) != cudaSuccess) return RBG_ERR_CUDA;
     if (s->workspace) cudaFree(s->workspace);
     s->workspace = nullptr;
     s->workspace_bytes = 0;
@@ -330,6 +353,13 @@ size_t slot_bytes(int64_t cap, int hist_cap) {
   return 256 + (size_t)cap * (15 * 8 + 2 * 4 + 8) + (size_t)cap * hist_cap * (4 * 8 + 4) + ray_order_bytes(cap);
 }
 
+// rays per pipeline chunk and number of slots for a batch of n rays
+void host_plan(int64_t n, int64_t* cap, int* nslots) {
+  *cap = ((n < kHostChunk ? n : kHostChunk) + 255) / 256 * 256;
+  const int64_t chunks = *cap > 0 ? (n + *cap - 1) / *cap : 0;
+  *nslots = chunks < kHostStreams ? (int)chunks : kHostStreams;
+}
+
 Slot slot_at(char* base, int64_t cap, int hist_cap) {
   Slot sl;
   sl.err = reinterpret_cast<unsigned*>(base);
@@ -352,6 +382,16 @@ Slot slot_at(char* base, int64_t cap, int hist_cap) {
 }
 
 }  // namespace
+
+int host_workspace_reserve(rbg_scene* s, int64_t max_rays, int32_t hist_cap) {
+  int64_t cap;
+  int nslots;
+  host_plan(max_rays, &cap, &nslots);
+  if (nslots == 0) return RBG_OK;
+  char* ws = nullptr;
+  return grow_workspace(s, slot_bytes(cap, hist_cap) * nslots, &ws);
+}
+
 }  // namespace rbg
 
 // The call a host-side AOpticsManager::TraceNonSequential makes: host
@@ -368,14 +408,14 @@ extern "C" int rbg_trace_host(rbg_scene* s, const rbg_rays* in, rbg_result* out,
   if (out->hist_cap < 0 || (out->hist_cap > 0 && (!out->hist_xyzt || !out->hist_node))) return RBG_ERR_ARG;
   int rc = ensure_device(s);
   if (rc) return rc;
-  if ((rc = stack_ready())) return rc;
   const int64_t n = in->n;
   s->last_launches = 0;
   if (n == 0) return RBG_OK;
   const int hcap = out->hist_cap;
-  const int64_t cap = ((n < kHostChunk ? n : kHostChunk) + 255) / 256 * 256;
+  int64_t cap;
+  int nslots;
+  host_plan(n, &cap, &nslots);
   const int64_t chunks = (n + cap - 1) / cap;
-  const int nslots = chunks < kHostStreams ? (int)chunks : kHostStreams;
   const size_t sb = slot_bytes(cap, hcap);
   char* ws = nullptr;
   if ((rc = grow_workspace(s, sb * nslots, &ws))) return rc;
@@ -443,250 +483,5 @@ extern "C" int rbg_trace_host(rbg_scene* s, const rbg_rays* in, rbg_result* out,
   s->last_launches = launches;
   if (bits & ERR_BIT_NAN) return RBG_ERR_NAN;
   if (bits & ERR_BIT_CAP) return RBG_ERR_CAP;
-  return RBG_OK;
-}
-
-// ---------------------------------------------------------------------
-// focal-plane reductions
-// ---------------------------------------------------------------------
-namespace rbg {
-
-__global__ void focal_moments_kernel(int64_t n, const uint8_t* status, const double* x, const double* y,
-                                     const double* t, const int32_t* group, int32_t n_groups, double* sums) {
-  // per-block shared accumulators for up to 64 groups, then one atomic
-  // pass; larger group counts go straight to global atomics
-  __shared__ double acc[64 * 6];
-  const bool shared = n_groups <= 64;
-  if (shared)
-    for (int k = threadIdx.x; k < n_groups * 6; k += blockDim.x) acc[k] = 0;
-  __syncthreads();
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    if (status[i] != RBG_FOCUS) continue;
-    int g = group ? group[i] : 0;
-    if (g < 0 || g >= n_groups) continue;
-    double v[6] = {1.0, x[i], y[i], x[i] * x[i], y[i] * y[i], t ? t[i] : 0.0};
-    double* dst = shared ? acc + g * 6 : sums + g * 6;
-    for (int k = 0; k < 6; ++k) atomicAdd(dst + k, v[k]);
-  }
-  __syncthreads();
-  if (shared)
-    for (int k = threadIdx.x; k < n_groups * 6; k += blockDim.x)
-      if (acc[k] != 0) atomicAdd(sums + k, acc[k]);
-}
-
-__global__ void focal_hist_kernel(int64_t n, const uint8_t* status, const double* x, const double* y, int32_t nx,
-                                  double xlo, double xhi, int32_t ny, double ylo, double yhi, double* counts) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    if (status[i] != RBG_FOCUS) continue;
-    double fx = (x[i] - xlo) / (xhi - xlo) * nx, fy = (y[i] - ylo) / (yhi - ylo) * ny;
-    if (!(fx >= 0) || !(fy >= 0) || fx >= nx || fy >= ny) continue;
-    atomicAdd(counts + (int64_t)fx * ny + (int64_t)fy, 1.0);
-  }
-}
-
-// SumInRadius (src/AGeoUtil.cxx:18-42) for a batch of probes
-__global__ void sum_in_radius_kernel(const double* counts, int32_t nx, double xlo, double xw, int32_t ny,
-                                     double ylo, double yw, const double* probes, int nprobe, double* sums) {
-  extern __shared__ double part[];
-  for (int p = 0; p < nprobe; ++p) part[p * blockDim.x + threadIdx.x] = 0;
-  int64_t nb = (int64_t)nx * ny;
-  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nb; b += (int64_t)gridDim.x * blockDim.x) {
-    double c = counts[b];
-    if (c <= 0) continue;
-    int ix = (int)(b / ny), iy = (int)(b % ny);
-    double cx = xlo + (ix + 0.5) * xw, cy = ylo + (iy + 0.5) * yw;
-    for (int p = 0; p < nprobe; ++p) {
-      double dx = cx - probes[3 * p], dy = cy - probes[3 * p + 1], r = probes[3 * p + 2];
-      if (dx * dx + dy * dy <= r * r) part[p * blockDim.x + threadIdx.x] += c;
-    }
-  }
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if ((int)threadIdx.x < s)
-      for (int p = 0; p < nprobe; ++p) part[p * blockDim.x + threadIdx.x] += part[p * blockDim.x + threadIdx.x + s];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0)
-    for (int p = 0; p < nprobe; ++p) atomicAdd(sums + p, part[p * blockDim.x]);
-}
-
-}  // namespace rbg
-
-extern "C" int rbg_focal_moments(int64_t n, const uint8_t* status, const double* x, const double* y,
-                                 const double* t, const int32_t* group, int32_t n_groups, double* sums,
-                                 void* stream) {
-  if (n < 0 || n_groups <= 0 || !status || !x || !y || !sums) return RBG_ERR_ARG;
-  if (n == 0) return RBG_OK;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 8);
-  focal_moments_kernel<<<blocks, 256, 0, st>>>(n, status, x, y, t, group, n_groups, sums);
-  return cudaGetLastError() == cudaSuccess ? RBG_OK : RBG_ERR_CUDA;
-}
-
-extern "C" int rbg_focal_histogram(int64_t n, const uint8_t* status, const double* x, const double* y, int32_t nx,
-                                   double xlo, double xhi, int32_t ny, double ylo, double yhi, double* counts,
-                                   void* stream) {
-  if (n < 0 || nx <= 0 || ny <= 0 || !(xhi > xlo) || !(yhi > ylo) || !status || !x || !y || !counts)
-    return RBG_ERR_ARG;
-  if (n == 0) return RBG_OK;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 8);
-  focal_hist_kernel<<<blocks, 256, 0, st>>>(n, status, x, y, nx, xlo, xhi, ny, ylo, yhi, counts);
-  return cudaGetLastError() == cudaSuccess ? RBG_OK : RBG_ERR_CUDA;
-}
-
-namespace {
-struct ProbeBatch {
-  double* dprobe = nullptr;
-  double* dsum = nullptr;
-  ~ProbeBatch() {
-    if (dprobe) cudaFree(dprobe);
-    if (dsum) cudaFree(dsum);
-  }
-};
-}  // namespace
-
-// AGeoUtil::ContainmentRadius with device SumInRadius probes
-extern "C" int rbg_containment_radius(const double* counts, int32_t nx, double xlo, double xhi, int32_t ny,
-                                      double ylo, double yhi, double fraction, double* pr, double* px, double* py,
-                                      void* stream) {
-  if (!counts || nx <= 0 || ny <= 0 || !pr || !px || !py || !(xhi > xlo) || !(yhi > ylo)) return RBG_ERR_ARG;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const double xw = (xhi - xlo) / nx, yw = (yhi - ylo) / ny;
-  ProbeBatch pb;
-  const int kMaxProbe = 8;
-  if (cudaMalloc(&pb.dprobe, 3 * kMaxProbe * sizeof(double)) != cudaSuccess) return RBG_ERR_NOMEM;
-  if (cudaMalloc(&pb.dsum, kMaxProbe * sizeof(double)) != cudaSuccess) return RBG_ERR_NOMEM;
-  const int block = 256;
-  const int blocks = (int)std::min<int64_t>(((int64_t)nx * ny + block - 1) / block, (int64_t)sm_count() * 4);
-  int failed = 0;
-  auto probe = [&](int np, const double* xyr, double* out) {
-    if (failed) {
-      for (int i = 0; i < np; ++i) out[i] = 0;
-      return;
-    }
-    if (cudaMemcpyAsync(pb.dprobe, xyr, 3 * np * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaMemsetAsync(pb.dsum, 0, np * sizeof(double), st) != cudaSuccess) {
-      failed = 1;
-      return;
-    }
-    sum_in_radius_kernel<<<blocks, block, np * block * sizeof(double), st>>>(counts, nx, xlo, xw, ny, ylo, yw,
-                                                                             pb.dprobe, np, pb.dsum);
-    if (cudaMemcpyAsync(out, pb.dsum, np * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess) {
-      failed = 1;
-    }
-  };
-  auto sum_in_radius = [&](double x, double y, double r) {
-    double q[3] = {x, y, r}, o = 0;
-    probe(1, q, &o);
-    return o;
-  };
-  // moments from bin centres: r = 1 probe at "infinite" radius is not enough,
-  // so read the histogram moments with one pass of 5 probes-worth of sums
-  std::vector<double> hc((size_t)nx * ny);
-  if (cudaMemcpyAsync(hc.data(), counts, hc.size() * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess)
-    return RBG_ERR_CUDA;
-  double sw = 0, sx = 0, sy = 0, sxx = 0, syy = 0;
-  for (int ix = 0; ix < nx; ++ix) {
-    double cx = xlo + (ix + 0.5) * xw;
-    for (int iy = 0; iy < ny; ++iy) {
-      double cy = ylo + (iy + 0.5) * yw, c = hc[(size_t)ix * ny + iy];
-      sw += c;
-      sx += c * cx;
-      sy += c * cy;
-      sxx += c * cx * cx;
-      syy += c * cy * cy;
-    }
-  }
-  double x = sw ? sx / sw : 0, y = sw ? sy / sw : 0;
-  double vx = sw ? sxx / sw - x * x : 0, vy = sw ? syy / sw - y * y : 0;
-  double sdx = vx > 0 ? std::sqrt(vx) : 0, sdy = vy > 0 ? std::sqrt(vy) : 0;
-  double r = std::sqrt(sdx * sdx + sdy * sdy) * 1.5;
-  double dr = 0.1 * r;
-  double sum_goal = sw * fraction;
-  int no_shift = 0, no_stable = 0;
-  for (int i = 0; i < 100 && no_shift < 30; i++) {
-    bool stable_r = false, stable_x = true, stable_y = true;
-    double sum0 = sum_in_radius(x, y, r);
-    double next_r = r;
-    if (sum0 < sum_goal) {
-      double sum1 = sum_in_radius(x, y, r + dr);
-      if (sum1 == sum0) {
-        dr *= 2.;
-        continue;
-      }
-      next_r = r + dr * (sum_goal - sum0) / (sum1 - sum0);
-    } else if (sum0 != sum_goal) {
-      double sum1 = sum_in_radius(x, y, r - dr);
-      if (sum1 == sum0) {
-        dr *= 2.;
-        continue;
-      }
-      next_r = r - dr * (sum0 - sum_goal) / (sum0 - sum1);
-    }
-    if (next_r < 0.) next_r = 0.5 * r;
-    if (next_r < 0.5 * r) next_r = 0.5 * r;
-    if (next_r > 2. * r) next_r = 2. * r;
-    stable_r = std::fabs(next_r - r) < 0.0001 * r;
-    r = next_r;
-    {
-      double sum1 = sum_in_radius(x, y, r);
-      dr *= sum0 != sum_goal ? std::fabs((sum1 - sum_goal) / (sum0 - sum_goal)) : 0.5;
-      if (dr > 0.5 * r) dr = 0.5 * r;
-      if (dr < 0.0005 * r) dr = 0.0005 * r;
-      no_shift++;
-      for (double dx = 0.25 * r; dx > 0.1 * dr; dx *= 0.25) {
-        double q[6] = {x + dx, y, r, x - dx, y, r}, o[2];
-        probe(2, q, o);
-        double sx1 = o[0], sx2 = o[1];
-        while (sx1 > sum1) {
-          no_shift = 0;
-          x += dx;
-          sx2 = sum1;
-          sum1 = sx1;
-          sx1 = sum_in_radius(x + dx, y, r);
-          stable_x = false;
-        }
-        while (sx2 > sum1) {
-          no_shift = 0;
-          x -= dx;
-          sx1 = sum1;
-          sum1 = sx2;
-          sx2 = sum_in_radius(x - dx, y, r);
-          stable_x = false;
-        }
-      }
-    }
-    for (double dy = 0.1 * r; dy > 0.1 * dr; dy *= 0.25) {
-      double q[9] = {x, y, r, x, y + dy, r, x, y - dy, r}, o[3];
-      probe(3, q, o);
-      double sum1 = o[0], sy1 = o[1], sy2 = o[2];
-      while (sy1 > sum1) {
-        no_shift = 0;
-        y += dy;
-        sy2 = sum1;
-        sum1 = sy1;
-        sy1 = sum_in_radius(x, y + dy, r);
-        stable_y = false;
-      }
-      while (sy2 > sum1) {
-        no_shift = 0;
-        y -= dy;
-        sy1 = sum1;
-        sum1 = sy2;
-        sy2 = sum_in_radius(x, y - dy, r);
-        stable_y = false;
-      }
-    }
-    if (stable_r && stable_x && stable_y) no_stable++;
-    else no_stable = 0;
-    if (no_stable >= 4) break;
-  }
-  if (failed) return RBG_ERR_CUDA;
-  *pr = r;
-  *px = x;
-  *py = y;
   return RBG_OK;
 }

@@ -9,12 +9,13 @@ struct rbg_device_scene {
   std::vector<void*> allocations;
   unsigned* err_flags;          // device word of error bits
   unsigned long long* counter;  // ray queue head of the persistent kernel
+  unsigned long long* adj_skip; // rays the adjoint skipped
   cudaStream_t host_streams[2] = {nullptr, nullptr};  // rbg_trace_host pipeline
 };
 
 namespace rbg {
 int ensure_device(rbg_scene* s);  // upload on first use (capi.cu)
-int sm_count();
+int sm_count();     // SMs of the current device
 // precalculated thin-film tables of s into `tables` (device), tmm.cu
 int fill_tmm_tables(const rbg_scene* s, const DevScene& S, double* tables, cudaStream_t st);
 }  // namespace rbg

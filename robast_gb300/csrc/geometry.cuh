@@ -136,19 +136,54 @@ RBG_D bool prim_contains(int type, const double* P, const double* T, d3 p) {
 
 // CSG containment.  A primitive, or a composite of two primitives (the
 // common case: every composite of the telescope scenes), is resolved
-// without recursion from the composite's own operand matrices; deeper trees
-// recurse.  Both are compiled once, out of line.
+// from the composite's own operand matrices; deeper trees are walked with
+// an explicit stack (depth <= RBG_MAX_COMPOSITE_DEPTH, checked when the
+// scene is flattened), left operand first, with TGeo's short cuts: an
+// intersection or subtraction whose left operand does not contain the point
+// does not, a union whose left operand does, does.  Both are compiled once,
+// out of line.
 RBG_NOINLINE bool csg_contains_deep(const DevScene& S, int shape, d3 p) {
-  const rbg_shape_desc sh = S.shapes[shape];
-  if (sh.type != RBG_SHAPE_COMPOSITE) return prim_contains(sh.type, SP(S, shape), ST(S, shape), p);
-  const double* P = SP(S, shape);
-  bool a = csg_contains_deep(S, sh.left, to_local(P + RBG_COMP_ML, p));
-  if (sh.op == RBG_OP_INTERSECTION && !a) return false;
-  if (sh.op == RBG_OP_SUBTRACTION && !a) return false;
-  if (sh.op == RBG_OP_UNION && a) return true;
-  bool b = csg_contains_deep(S, sh.right, to_local(P + RBG_COMP_MR, p));
-  if (sh.op == RBG_OP_SUBTRACTION) return !b;
-  return b;
+  constexpr int kFrames = RBG_MAX_COMPOSITE_DEPTH + 1;
+  int fs[kFrames], stage[kFrames];
+  d3 fp[kFrames];
+  int sp = 0;
+  fs[0] = shape;
+  stage[0] = 0;
+  fp[0] = p;
+  bool ret = false;  // the value of the frame popped last
+  while (sp >= 0) {
+    const int id = fs[sp];
+    const rbg_shape_desc sh = S.shapes[id];
+    if (sh.type != RBG_SHAPE_COMPOSITE) {
+      ret = prim_contains(sh.type, SP(S, id), ST(S, id), fp[sp]);
+      --sp;
+      continue;
+    }
+    const double* P = SP(S, id);
+    if (stage[sp] == 2) {  // right operand evaluated
+      if (sh.op == RBG_OP_SUBTRACTION) ret = !ret;
+      --sp;
+      continue;
+    }
+    if (stage[sp] == 1) {  // left operand evaluated
+      if ((sh.op == RBG_OP_INTERSECTION || sh.op == RBG_OP_SUBTRACTION) && !ret) {
+        --sp;
+        continue;
+      }
+      if (sh.op == RBG_OP_UNION && ret) {
+        --sp;
+        continue;
+      }
+    }
+    if (sp + 1 >= kFrames) return false;  // deeper than the flattener allows: never
+    const bool right = stage[sp] == 1;
+    stage[sp] = right ? 2 : 1;
+    fs[sp + 1] = right ? sh.right : sh.left;
+    stage[sp + 1] = 0;
+    fp[sp + 1] = to_local(P + (right ? RBG_COMP_MR : RBG_COMP_ML), fp[sp]);
+    ++sp;
+  }
+  return ret;
 }
 
 RBG_NOINLINE bool csg_contains(const DevScene& S, int shape, d3 p) {
@@ -384,44 +419,69 @@ RBG_D d3 prim_normal(int type, const double* P, const double* T, uint32_t surf, 
   return mk(0, 0, 1);
 }
 
-// Collect crossings of a composite tree deeper than two primitives.  Leaves
-// are numbered in depth-first order; M maps the shape's frame to the query
-// frame.  Recursion depth is bounded by the composite depth checked at build.
+// Leaves of a composite tree in depth-first order (left operand first),
+// each with the matrix from its frame to the query frame (M maps the
+// tree's own frame there).  An explicit stack holds the pending right
+// operands: at most one per level, RBG_MAX_COMPOSITE_DEPTH + 1 entries.
+struct CsgWalk {
+  int shape[RBG_MAX_COMPOSITE_DEPTH + 1];
+  M12 m[RBG_MAX_COMPOSITE_DEPTH + 1];
+  int sp;
+};
+RBG_D void csg_walk_begin(CsgWalk& w, int shape, const double* M) {
+  w.sp = 0;
+  w.shape[0] = shape;
+#pragma unroll
+  for (int i = 0; i < 12; ++i) w.m[0].v[i] = M[i];
+}
+// next leaf (shape id and matrix); false when the walk is done
+RBG_D bool csg_walk_next(const DevScene& S, CsgWalk& w, int& leaf_shape, M12& leafM) {
+  while (w.sp >= 0) {
+    const int id = w.shape[w.sp];
+    const M12 M = w.m[w.sp];
+    const rbg_shape_desc sh = S.shapes[id];
+    if (sh.type != RBG_SHAPE_COMPOSITE) {
+      --w.sp;
+      leaf_shape = id;
+      leafM = M;
+      return true;
+    }
+    const double* P = SP(S, id);
+    if (w.sp + 1 >= RBG_MAX_COMPOSITE_DEPTH + 1) return false;  // deeper than the flattener allows: never
+    // replace the composite by its right operand, then push its left one
+    w.shape[w.sp] = sh.right;
+    w.m[w.sp] = mat_mul(M.v, P + RBG_COMP_MR);
+    ++w.sp;
+    w.shape[w.sp] = sh.left;
+    w.m[w.sp] = mat_mul(M.v, P + RBG_COMP_ML);
+  }
+  return false;
+}
+
+// Collect crossings of a composite tree deeper than two primitives; leaves
+// are numbered in depth-first order.
 RBG_NOINLINE void csg_collect_deep(const DevScene& S, int shape, const double* M, d3 o, d3 d, uint32_t& leaf,
                                    XList& L) {
-  const rbg_shape_desc sh = S.shapes[shape];
-  if (sh.type != RBG_SHAPE_COMPOSITE) {
-    d3 ol = to_local(M, o), dl = dir_to_local(M, d);
-    prim_collect(sh.type, SP(S, shape), ST(S, shape), ol, dl, leaf << 16, L);
+  CsgWalk w;
+  csg_walk_begin(w, shape, M);
+  int ls;
+  M12 LM;
+  while (csg_walk_next(S, w, ls, LM)) {
+    prim_collect(S.shapes[ls].type, SP(S, ls), ST(S, ls), to_local(LM.v, o), dir_to_local(LM.v, d), leaf << 16, L);
     ++leaf;
-    return;
   }
-  const double* P = SP(S, shape);
-  M12 ML = mat_mul(M, P + RBG_COMP_ML);
-  csg_collect_deep(S, sh.left, ML.v, o, d, leaf, L);
-  M12 MR = mat_mul(M, P + RBG_COMP_MR);
-  csg_collect_deep(S, sh.right, MR.v, o, d, leaf, L);
 }
 
 // find leaf #target (depth-first) and its matrix
 RBG_NOINLINE bool csg_find_leaf(const DevScene& S, int shape, const double* M, uint32_t target, uint32_t& leaf,
                                 int& leaf_shape, M12& leafM) {
-  const rbg_shape_desc sh = S.shapes[shape];
-  if (sh.type != RBG_SHAPE_COMPOSITE) {
-    if (leaf == target) {
-      leaf_shape = shape;
-#pragma unroll
-      for (int i = 0; i < 12; ++i) leafM.v[i] = M[i];
-      return true;
-    }
+  CsgWalk w;
+  csg_walk_begin(w, shape, M);
+  while (csg_walk_next(S, w, leaf_shape, leafM)) {
+    if (leaf == target) return true;
     ++leaf;
-    return false;
   }
-  const double* P = SP(S, shape);
-  M12 ML = mat_mul(M, P + RBG_COMP_ML);
-  if (csg_find_leaf(S, sh.left, ML.v, target, leaf, leaf_shape, leafM)) return true;
-  M12 MR = mat_mul(M, P + RBG_COMP_MR);
-  return csg_find_leaf(S, sh.right, MR.v, target, leaf, leaf_shape, leafM);
+  return false;
 }
 
 // Distance to enter (exit = false) or leave (exit = true) a TGeo primitive or
@@ -684,27 +744,29 @@ RBG_D bool asph_contains_fast(const Asph& a, d3 p) {
   return !(p.z < f1 || f2 < p.z);
 }
 
-// ComputeNormal of the mixed path: the same closest-surface choice, but the
-// normal of a face is its exact gradient (-2x F', -2y F', 1) (no atan2 /
-// RotateZ) and the face residuals are FP64 while the comparisons are FP32.
+// ComputeNormal of the mixed path: the same closest-surface choice, made on
+// FP64 safety distances (|dF/dr| = 2 r |F'| with F' the derivative in H2),
+// with the normal of a face taken as its exact gradient (-2x F', -2y F', 1)
+// (no atan2 / RotateZ).  The choice must be FP64: a point within half an
+// FP32 ulp (1.5e-5 cm at r = 270 cm) of a rim reads as ON the rim in FP32,
+// and the wall would win over a face crossed 1e-9 cm ago.
 RBG_D d3 asph_normal_fast(const Asph& a, d3 point, d3 dir) {
   const double H2 = point.x * point.x + point.y * point.y;
-  const float r = sqrtf((float)H2);
-  float saf[4];
-  saf[0] = a.rseg() ? fabsf(r - (float)a.rmin()) : 3e38f;
-  saf[1] = fabsf(r - (float)a.rmax());
+  const double r = sqrt(H2);
+  double saf[4];
+  saf[0] = a.rseg() ? fabs(r - a.rmin()) : kBig;
+  saf[1] = fabs(r - a.rmax());
   double F1, F2, dF1 = 0, dF2 = 0;
   bool ok1 = asph_sag_fast(a, 1, H2, F1, dF1), ok2 = asph_sag_fast(a, 2, H2, F2, dF2);
-  // |dF/dr| = 2 r |F'|
-  saf[2] = ok1 ? (float)fabs(F1 - point.z) / sqrtf(1.f + 4.f * (float)H2 * (float)(dF1 * dF1)) : 3e38f;
-  saf[3] = ok2 ? (float)fabs(F2 - point.z) / sqrtf(1.f + 4.f * (float)H2 * (float)(dF2 * dF2)) : 3e38f;
+  saf[2] = ok1 ? fabs(F1 - point.z) / sqrt(1.0 + 4.0 * H2 * (dF1 * dF1)) : kBig;
+  saf[3] = ok2 ? fabs(F2 - point.z) / sqrt(1.0 + 4.0 * H2 * (dF2 * dF2)) : kBig;
   int i = 0;
   for (int k = 1; k < 4; ++k)
     if (saf[k] < saf[i]) i = k;
   d3 n;
   if (i <= 1) {
     if (H2 > 0) {
-      double inv = 1.0 / sqrt(H2);
+      double inv = 1.0 / r;
       n = mk(point.x * inv, point.y * inv, 0);
     } else {
       n = mk(1, 0, 0);

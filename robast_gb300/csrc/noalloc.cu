@@ -30,11 +30,8 @@
 #include <mutex>
 
 #include "scene_internal.h"
+#include "device_state.cuh"
 #include "tracer.cuh"
-
-namespace rbg {
-int fill_tmm_tables(const rbg_scene* s, const DevScene& S, double* tables, cudaStream_t st);
-}
 
 #define RBG_NOALLOC_SCRATCH_BYTES (4u << 20)
 

@@ -25,7 +25,7 @@ constexpr int kBvhLeaf = 4;
 // traverses with a 32-entry stack)
 constexpr int kBvhSahDepth = 28;
 constexpr int kBvhMinChildren = 9;
-constexpr int kMaxCompositeDepth = 6;
+constexpr int kMaxCompositeDepth = RBG_MAX_COMPOSITE_DEPTH;
 
 struct Box {
   double lo[3], hi[3];
@@ -361,7 +361,7 @@ struct Builder {
         int rc;
         if ((rc = canon_shape(u.left)) != RBG_OK) return rc;
         if ((rc = canon_shape(u.right)) != RBG_OK) return rc;
-        // the device walks composite trees recursively: bound their depth
+        // the device walks composite trees with fixed-size stacks: bound their depth
         int depth = 1 + std::max(composite_depth[u.left], composite_depth[u.right]);
         if (depth > kMaxCompositeDepth) return RBG_ERR_UNSUPPORTED;
         composite_depth[id] = depth;

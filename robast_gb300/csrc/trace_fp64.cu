@@ -13,9 +13,17 @@ namespace rbg {
 __global__ void __launch_bounds__(128) trace_fp64_kernel(DevScene S, KernelRays in, KernelOut out, int64_t n,
                                                          int limit, int disable_fresnel, uint64_t seed,
                                                          uint64_t id_offset, unsigned* err_flags) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    // slot q -> ray: in a take-up order (ray_order.cu) the ray keeps its
+    // own index for its outputs and random draws
+    const int64_t i = in.order ? (int64_t)in.order[q] : q;
+    const int64_t src = in.gathered ? q : i;
+    if ((uint64_t)i >= (uint64_t)n) {
+      atomicOr(err_flags, ERR_BIT_CAP);  // not a permutation: never expected
+      continue;
+    }
     Ray r;
-    if (load_ray(in, out, i, seed, id_offset, r)) trace_ray<false>(S, r, limit, disable_fresnel != 0);
+    if (load_ray(in, out, src, i, seed, id_offset, r)) trace_ray<false>(S, r, limit, disable_fresnel != 0);
     if (r.err) atomicOr(err_flags, r.err);
     store_ray(out, i, r);
   }

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include "scene_internal.h"
+#include "device_state.cuh"
 #include "tracer.cuh"
 
 namespace rbg {
@@ -94,17 +95,20 @@ __global__ void __launch_bounds__(kMixedBlock) trace_mixed_kernel(DevScene S, Ke
 template <unsigned F>
 int launch_mixed_impl(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n,
                       const rbg_trace_opts& o, cudaStream_t st, unsigned* err_flags, unsigned long long* counter) {
-  static int bps = 0;
-  static int sms = 0;
-  if (bps == 0) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return RBG_ERR_CUDA;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return RBG_ERR_CUDA;
+  // resident blocks per SM, queried once per instantiation and device
+  constexpr int kMaxDev = 64;
+  static int bps_of[kMaxDev] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return RBG_ERR_CUDA;
+  if (dev >= kMaxDev) return RBG_ERR_UNSUPPORTED;
+  if (bps_of[dev] == 0) {
     int b = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_mixed_kernel<F>, kMixedBlock, 0) != cudaSuccess)
       return RBG_ERR_CUDA;
-    bps = b < 1 ? 1 : b;
+    bps_of[dev] = b < 1 ? 1 : b;
   }
+  const int bps = bps_of[dev];
+  const int sms = sm_count();
   int64_t want = (n + kMixedBlock - 1) / kMixedBlock;
   int64_t grid = (int64_t)sms * bps;
   if (want < grid) grid = want;

@@ -1268,15 +1268,16 @@ struct KernelOut {
   int32_t* hist_node;
 };
 
-// Read ray i, record its start point, normalise the direction as
-// ARay::SetDirection does.  Returns false (and flags the error) for a ray
-// that cannot be traced: NaN origin or a zero/NaN direction.
-RBG_D bool load_ray(const KernelRays& in, const KernelOut& out, int64_t i, uint64_t seed, uint64_t id_offset,
-                    Ray& r) {
-  r.x = mk(in.x[i], in.y[i], in.z[i]);
-  r.t = in.t ? in.t[i] : 0.0;
-  r.lambda = in.lambda[i];
-  d3 dd = mk(in.dx[i], in.dy[i], in.dz[i]);
+// Read ray i (its inputs at position `src` of `in`), record its start
+// point, normalise the direction as ARay::SetDirection does.  Returns false
+// (and flags the error) for a ray that cannot be traced: NaN origin or a
+// zero/NaN direction.
+RBG_D bool load_ray(const KernelRays& in, const KernelOut& out, int64_t src, int64_t i, uint64_t seed,
+                    uint64_t id_offset, Ray& r) {
+  r.x = mk(in.x[src], in.y[src], in.z[src]);
+  r.t = in.t ? in.t[src] : 0.0;
+  r.lambda = in.lambda[src];
+  d3 dd = mk(in.dx[src], in.dy[src], in.dz[src]);
   r.status = RBG_RUN;
   r.npoints = 0;
   r.last_node = -2;

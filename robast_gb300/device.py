@@ -80,9 +80,33 @@ def _result_struct(res) -> N.Result:
     return r
 
 
-def trace(manager, rays, res=None, precision: Optional[int] = None, stream=None, check: bool = True):
+# per-device take-up order workspace shared by every scene this process
+# traces (allocated by torch, handed to rbg_trace in its options)
+_WORKSPACE = {}
+
+
+def workspace(n: int, device):
+    """A device buffer of at least rbg_trace_workspace_bytes(n) bytes,
+    grown on demand and kept for later traces on `device`."""
+    torch = _torch()
+    need = int(N.lib().rbg_trace_workspace_bytes(int(n)))
+    if need == 0:
+        return None
+    dev = torch.device(device)
+    ws = _WORKSPACE.get(dev)
+    if ws is None or ws.numel() < need:
+        _WORKSPACE.pop(dev, None)
+        ws = torch.empty(need, dtype=torch.uint8, device=dev)
+        _WORKSPACE[dev] = ws
+    return ws
+
+
+def trace(manager, rays, res=None, precision: Optional[int] = None, stream=None, check: bool = True,
+          workspace_buf="auto"):
     """AOpticsManager::TraceNonSequential on device tensors; returns the
-    result dict and the C status."""
+    result dict and the C status.  workspace_buf: "auto" (this module's
+    shared buffer), None (the scene's own, rbg_scene_reserve) or a uint8
+    device tensor for the take-up order."""
     torch = _torch()
     scene = manager._ensure_scene()
     n = rays["x"].numel()
@@ -91,6 +115,10 @@ def trace(manager, rays, res=None, precision: Optional[int] = None, stream=None,
     rs = _rays_struct(rays)
     rr = _result_struct(res)
     opts = manager.trace_options(precision)
+    ws = workspace(n, rays["x"].device) if isinstance(workspace_buf, str) else workspace_buf
+    if ws is not None:
+        opts.workspace = ws.data_ptr()
+        opts.workspace_bytes = ws.numel()
     st_ptr = (stream if stream is not None else torch.cuda.current_stream()).cuda_stream
     status = N.lib().rbg_trace(scene.handle, C.byref(rs), C.byref(rr), C.byref(opts), C.c_void_p(st_ptr))
     if check and status not in (N.RBG_OK, N.RBG_ERR_CAP):
@@ -107,6 +135,10 @@ def autotune(manager, rays, res=None, stream=None) -> int:
     if res is None:
         res = alloc_result(rays["x"].numel(), rays["x"].device)
     opts = manager.trace_options(N.PREC_MIXED)
+    ws = workspace(rays["x"].numel(), rays["x"].device)
+    if ws is not None:
+        opts.workspace = ws.data_ptr()
+        opts.workspace_bytes = ws.numel()
     st_ptr = (stream if stream is not None else torch.cuda.current_stream()).cuda_stream
     chosen = C.c_int32(0)
     status = N.lib().rbg_scene_autotune(scene.handle, C.byref(_rays_struct(rays)), C.byref(_result_struct(res)),
@@ -137,6 +169,28 @@ def focal_histogram(res, nx, xlo, xhi, ny, ylo, yhi, mask=None, stream=None):
     N.check(N.lib().rbg_focal_histogram(res["x"].numel(), _ptr(status), _ptr(res["x"]), _ptr(res["y"]), nx, xlo,
                                         xhi, ny, ylo, yhi, _ptr(counts), C.c_void_p(st)), "rbg_focal_histogram")
     return counts
+
+
+def reserve(manager, max_rays: int, history: int = 0):
+    """rbg_scene_reserve: make every device allocation tracing batches of up
+    to `max_rays` rays needs, so that later traces allocate nothing."""
+    _torch()
+    scene = manager._ensure_scene()
+    N.check(N.lib().rbg_scene_reserve(scene.handle, int(max_rays), int(history)), "rbg_scene_reserve")
+
+
+def containment_radius_async(counts, xlo, xhi, ylo, yhi, fraction=0.8, out=None, stream=None):
+    """AGeoUtil::ContainmentRadius of a device histogram into a device
+    tensor (r, x, y, status), stream-ordered (one launch, no host sync)."""
+    torch = _torch()
+    counts = counts.contiguous()
+    nx, ny = counts.shape
+    if out is None:
+        out = torch.empty(4, dtype=torch.float64, device=counts.device)
+    st = (stream if stream is not None else torch.cuda.current_stream()).cuda_stream
+    N.check(N.lib().rbg_containment_radius_async(_ptr(counts), nx, xlo, xhi, ny, ylo, yhi, fraction, _ptr(out),
+                                                 C.c_void_p(st)), "rbg_containment_radius_async")
+    return out
 
 
 def containment_radius(counts, xlo, xhi, ylo, yhi, fraction=0.8, stream=None):

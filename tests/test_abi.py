@@ -36,7 +36,7 @@ def test_all_declared_symbols_exported():
 
 def test_abi_version_and_status_strings():
     lib = N.lib()
-    assert lib.rbg_abi_version() == 1
+    assert lib.rbg_abi_version() == 2
     for s in range(9):
         assert lib.rbg_status_string(s)
     o = N.TraceOpts()

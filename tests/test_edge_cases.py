@@ -150,10 +150,10 @@ def test_host_pipeline_matches_device_trace(prec):
         rr, got = make_result(n, hist)
         st = N.lib().rbg_trace_host(man._ensure_scene().handle, C.byref(rs), C.byref(rr), C.byref(opts))
         assert st == N.RBG_OK, (call, N.status_string(st))
-        # one trace per chunk; the mixed tracer's first chunk also runs the
-        # seven kernels of its spatial take-up order (the 3001-ray second
-        # chunk is below the 2^14 rays that get one)
-        want = 2 if prec == N.PREC_FP64 else 2 + 7
+        # one trace per chunk; the first chunk also runs the seven kernels
+        # of its spatial take-up order (the 3001-ray second chunk is below
+        # the 2^14 rays that get one)
+        want = 2 + 7
         assert N.lib().rbg_last_launch_count(man.scene.handle) == want
         for k in FIELDS:
             np.testing.assert_array_equal(got[k], ref[k], err_msg=f"call {call}: {k}")

@@ -1,12 +1,14 @@
 """GPU tracer vs CPU FP64 oracle on the same seeded rays (parity gate).
 
 Deterministic optics (no roughness / Fresnel / absorption draws) must give
-identical fates, point counts and last nodes; final positions and
-directions agree to 1e-6 relative (the oracle and the GPU run the same
-FP64 algorithm, differing only by rounding and FMA contraction).  The
-random draws are Philox keyed by (seed, ray id, draw number) in both, so
-stochastic scenes are compared ray by ray too, with a small allowance for
-rays whose draw sequence forks on a last-ulp difference.
+identical fates, point counts and last nodes, ray by ray, in both tracers;
+final positions and directions agree to 1e-6 relative (the oracle and the
+GPU run the same FP64 algorithm, differing only by rounding and FMA
+contraction).  The random draws are Philox keyed by (seed, ray id, draw
+number) in both, so stochastic scenes are compared ray by ray too: exactly
+for the FP64 tracer, and for the mixed tracer with an allowance for rays
+whose draw compares against an FP32 reflectance (Fresnel, thin films) that
+differs from the FP64 one in its last bits.
 """
 import numpy as np
 import pytest
@@ -31,7 +33,7 @@ def _gpu_trace(man, batch, precision=None, history=0):
     return st, {k: v.cpu().numpy() for k, v in res.items()}
 
 
-def compare(gpu, ref, min_agree=0.9999, pos_rtol=POS_RTOL):
+def compare(gpu, ref, min_agree=1.0, pos_rtol=POS_RTOL):
     same = (gpu["status"] == ref["status"]) & (gpu["npoints"] == ref["npoints"]) & \
            (gpu["last_node"] == ref["last_node"])
     assert same.mean() >= min_agree, f"fate agreement {same.mean():.6f}"
@@ -88,15 +90,15 @@ def test_history_parity():
     ("schmidt_cassegrain", dict(n_rays=16000, n_samples=4)),
 ])
 def test_config_parity(name, kw):
-    """Stochastic configs (roughness, Fresnel, absorption, TMM draws): the
-    Philox streams are identical, so rays agree one by one unless a draw
-    comparison flips on a last-ulp difference."""
+    """Stochastic configs (roughness, Fresnel, absorption, TMM draws) with
+    the plain FP64 tracer: the Philox streams and the reflectances the
+    draws are compared with are the oracle's, so every ray agrees."""
     man, batch = configs.CONFIGS[name](**kw)
     st, gpu = _gpu_trace(man, batch)
     assert st == 0
     ost, ref = oracle_ref.trace(man, configs.to_array(batch), threads=8)
     assert ost == 0
-    compare(gpu, ref, min_agree=0.999)
+    compare(gpu, ref)
     # the fate histograms agree closely as well
     g = np.bincount(gpu["status"], minlength=6)
     r = np.bincount(ref["status"], minlength=6)
@@ -112,12 +114,17 @@ MIXED_CASES = [
 ]
 
 
+# deterministic optics: exact agreement; stochastic: FP32 reflectances
+DETERMINISTIC = ("paraboloid", "schwarzschild_couder")
+
+
 @pytest.mark.parametrize("name,kw", MIXED_CASES)
 def test_mixed_precision_parity(name, kw):
     """The mixed-precision persistent tracer against the FP64 oracle: the
-    accepted intersections are polished in FP64, so fates and final points
-    agree like the plain FP64 tracer's; FP32 reflectances (thin-film
-    matrices, Fresnel) can flip a random draw on a handful of rays."""
+    accepted intersections are polished in FP64, so on deterministic optics
+    every ray's fate, point count and last node equal the oracle's; FP32
+    reflectances (thin-film matrices, Fresnel) can flip a random draw on a
+    handful of rays of the stochastic scenes (at most 1 in 1000)."""
     from robast_gb300 import _native as N
 
     man, batch = configs.CONFIGS[name](**kw)
@@ -125,4 +132,4 @@ def test_mixed_precision_parity(name, kw):
     assert st == 0
     ost, ref = oracle_ref.trace(man, configs.to_array(batch), threads=8)
     assert ost == 0
-    compare(gpu, ref, min_agree=0.999)
+    compare(gpu, ref, min_agree=1.0 if name in DETERMINISTIC else 0.999)
