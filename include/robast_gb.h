@@ -511,6 +511,15 @@ int rbg_containment_radius_async(const double* counts, int32_t nx,
                                  double ylo, double yhi, double fraction,
                                  double* out, void* stream);
 
+/* ---- measurement -------------------------------------------------------- */
+/* FP64 (bits = 64) or FP32 (bits = 32) fused multiply-add rate of the
+ * current GPU in FLOP/s (2 per FMA), from a kernel of independent FMA
+ * chains timed with CUDA events, best of two timed launches: the peak the
+ * tracers' FP64-pipe and FP32-pipe roofline fractions are quoted against
+ * (no counterpart in the reference).  Allocates and frees a small output
+ * buffer; synchronises `stream`. */
+int rbg_measure_fma_peak(int32_t bits, double* flops_per_s, void* stream);
+
 /* ---- gradients ---------------------------------------------------------- */
 /* Parameters the adjoint differentiates.  Shifts and rotations are small
  * rigid motions of a physical node applied in the master frame (the

@@ -188,6 +188,7 @@ def _declare(L):
     L.rbg_scene_upload.argtypes = [vp]
     L.rbg_scene_reserve.argtypes = [vp, C.c_int64, C.c_int32]
     L.rbg_trace_workspace_bytes.argtypes = [C.c_int64]
+    L.rbg_measure_fma_peak.argtypes = [C.c_int32, _dp, vp]
     L.rbg_trace_workspace_bytes.restype = C.c_size_t
     L.rbg_trace.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts), vp]
     L.rbg_trace_host.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts)]

@@ -81,7 +81,10 @@ def test_containment_radius_matches_oracle(name, h, rng):
 
 def test_containment_radius_weighted_counts():
     """Non-integer weights: the sums then depend on the order of addition,
-    so the device and the oracle agree to rounding, not bit for bit."""
+    so a comparison of two sums (sum1 == sum0, sum_x1 > sum1) can go the
+    other way on the device and in the oracle, and the two searches part;
+    both still stop at the reference's own tolerance (a radius step below
+    1e-4 r, shifts below 0.1 dr), so they agree to a few parts in 1e4."""
     import torch
 
     from robast_gb300 import device
@@ -92,7 +95,7 @@ def test_containment_radius_weighted_counts():
     h = _hist(x, y, 256, -5, 5, 256, -3, 4) * 0.37
     r_o, x_o, y_o = oracle_ref.containment_radius(h, -5, 5, -3, 4, 0.8)
     r, xx, yy = device.containment_radius(torch.as_tensor(h).cuda(), -5, 5, -3, 4, 0.8)
-    assert abs(r - r_o) <= 1e-6 * r_o and abs(xx - x_o) <= 1e-6 and abs(yy - y_o) <= 1e-6
+    assert abs(r - r_o) <= 2e-3 * r_o and abs(xx - x_o) <= 2e-3 * r_o and abs(yy - y_o) <= 2e-3 * r_o
 
 
 def test_sc_spots_d80_match_oracle():
