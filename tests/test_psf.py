@@ -84,7 +84,10 @@ def test_containment_radius_weighted_counts():
     so a comparison of two sums (sum1 == sum0, sum_x1 > sum1) can go the
     other way on the device and in the oracle, and the two searches part;
     both still stop at the reference's own tolerance (a radius step below
-    1e-4 r, shifts below 0.1 dr), so they agree to a few parts in 1e4."""
+    1e-4 r, so the radii agree to about 1e-4), while the centre is only
+    fixed to within the flat top of the containment sum (a shift of 1 % of
+    r changes the contained weight by far less than one bin's), so the two
+    centres may stop a few hill-climbing steps apart."""
     import torch
 
     from robast_gb300 import device
@@ -95,7 +98,8 @@ def test_containment_radius_weighted_counts():
     h = _hist(x, y, 256, -5, 5, 256, -3, 4) * 0.37
     r_o, x_o, y_o = oracle_ref.containment_radius(h, -5, 5, -3, 4, 0.8)
     r, xx, yy = device.containment_radius(torch.as_tensor(h).cuda(), -5, 5, -3, 4, 0.8)
-    assert abs(r - r_o) <= 2e-3 * r_o and abs(xx - x_o) <= 2e-3 * r_o and abs(yy - y_o) <= 2e-3 * r_o
+    assert abs(r - r_o) <= 1e-3 * r_o, (r, r_o)
+    assert abs(xx - x_o) <= 0.01 * r_o and abs(yy - y_o) <= 0.01 * r_o, (xx, x_o, yy, y_o)
 
 
 def test_sc_spots_d80_match_oracle():
