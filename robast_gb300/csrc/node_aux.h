@@ -16,7 +16,10 @@ enum : int32_t {
 enum : int32_t {
   // aspheric disk whose two faces share curvature, conic constant and
   // polynomial and differ only by their vertex z (a thin mirror shell)
-  RBG_AUX_ASPH_TWIN_FACES = 1
+  RBG_AUX_ASPH_TWIN_FACES = 1,
+  // the node has AGeoAsphericDisk daughters: its boundary search brackets
+  // their crossings in FP32 first (find_next_boundary_and_step_f)
+  RBG_AUX_ASPH_CHILDREN = 2
 };
 
 struct rbg_node_aux {
@@ -36,6 +39,9 @@ static_assert(sizeof(rbg_node_aux) == 32, "rbg_node_aux layout");
 //                with pe = phi1 + (e + 1/2) dphi / nedges
 //   WINSTON    : [0] cos theta, [1] sin theta, [2] tan(pi / n), then per face
 //                k (cos 2 pi k / n, sin 2 pi k / n)
+//   ASPHERIC   : [0] z2 - z1 (the face separation), then the derivative
+//                coefficients (j + 1) K_j of face 1 (npol1) and of face 2
+//                (npol2), so that d sag / d r^2 is a plain FMA Horner sum
 enum : int32_t {
   RBG_TRIG_PHI = 0,
   RBG_TRIG_SPH_COS = 4,
@@ -44,7 +50,9 @@ enum : int32_t {
   RBG_TRIG_WIN_COS = 0,
   RBG_TRIG_WIN_SIN = 1,
   RBG_TRIG_WIN_TANHALF = 2,
-  RBG_TRIG_WIN_FACE = 3
+  RBG_TRIG_WIN_FACE = 3,
+  RBG_TRIG_ASPH_DZ = 0,
+  RBG_TRIG_ASPH_DK = 1
 };
 
 struct rbg_scene;

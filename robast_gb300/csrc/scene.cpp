@@ -742,6 +742,13 @@ void rbg::build_node_aux(rbg_scene* s) {
         }
         break;
       }
+      case RBG_SHAPE_ASPHERIC_DISK: {
+        const int n1 = (int)P[RBG_ASPH_NPOL1], n2 = (int)P[RBG_ASPH_NPOL2];
+        s->trig.push_back(P[RBG_ASPH_Z2] - P[RBG_ASPH_Z1]);
+        for (int j = 0; j < n1; ++j) s->trig.push_back((j + 1) * P[RBG_ASPH_K + j]);
+        for (int j = 0; j < n2; ++j) s->trig.push_back((j + 1) * P[RBG_ASPH_K + n1 + j]);
+        break;
+      }
       default:
         break;
     }
@@ -770,6 +777,9 @@ void rbg::build_node_aux(rbg_scene* s) {
       for (int j = 0; twin && j < n1; ++j) twin = P[RBG_ASPH_K + j] == P[RBG_ASPH_K + n1 + j];
       if (twin) a.flags |= RBG_AUX_ASPH_TWIN_FACES;
     }
+    for (int c = 0; c < n.child_count; ++c)
+      if (s->shapes[s->nodes[s->children[n.child_begin + c]].shape].type == RBG_SHAPE_ASPHERIC_DISK)
+        a.flags |= RBG_AUX_ASPH_CHILDREN;
   }
 }
 
