@@ -2,10 +2,12 @@
 # Builds oracle/_ref/corsika_dump: oracle/corsika_dump.c over the reference's
 # own eventio reader, compiled from its sources where they lie under the
 # reference tree (test infrastructure; nothing is copied into this repo).
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+# The reference root is the argument, else $ROBAST_REFERENCE, else a
+# checkout named "reference" beside this repository.
 set -e
-REF=${1:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${1:-${ROBAST_REFERENCE:-$HERE/../../reference}}
 if [ ! -d "$REF/src/bernlohr" ]; then
   echo "reference tree not present: oracle/_ref not built"
   exit 0

@@ -403,38 +403,14 @@ RBG_D int find_next_boundary_and_step_f(const DevScene& S, Nav& nv, double& step
     enter = false;
     const bool zx = df.x == 0.f, zy = df.y == 0.f, zz = df.z == 0.f;
     const float ix = zx ? 0.f : 1.0f / df.x, iy = zy ? 0.f : 1.0f / df.y, iz = zz ? 0.f : 1.0f / df.z;
-    // `cull`: an FP32 upper bound of the step (rounded up from the FP64
-    // distances found so far, or from a sure bracket): boxes the segment
-    // [0, cull] misses are skipped, and so are daughters whose bracket
-    // starts beyond it
-    float cull = best >= kBig ? 3e38f : __double2float_ru(best);
     auto reach = [&](const float* lo, const float* hi) {
-      return seg_box_f32(pf.x, pf.y, pf.z, ix, iy, iz, zx, zy, zz, cull, lo, hi);
+      return seg_box_f32(pf.x, pf.y, pf.z, ix, iy, iz, zx, zy, zz, best >= kBig ? 3e38f : (float)best, lo, hi);
     };
-    auto bracket = [&](int k, const LRay& Lk, AsphBracket& b) {
-      const int sh = S.nodes[k].shape, off = S.shapes[sh].param_offset;
-      asph_bracket_out_f(S.params + off, S.fparams + off, ST(S, sh), Lk,
-                         S.aux[k].flags & RBG_AUX_ASPH_TWIN_FACES, b);
-    };
-    auto is_asph = [&](int k) { return S.shapes[S.nodes[k].shape].type == RBG_SHAPE_ASPHERIC_DISK; };
     auto visit = [&](int k) {
       const rbg_node_aux& A = S.aux[k];
       if (!reach(A.lo, A.hi)) return;
-      const LRay Lk = local_ray(S, k, nv.p, nv.d, pf, df);
       d3 nrm = mk(0, 0, 1);
-      double s = kBig;
-      bool done = false;
-      if (is_asph(k)) {
-        AsphBracket b;
-        bracket(k, Lk, b);
-        if (b.lo > cull) return;  // no hit, or never nearer than the step's bound
-        if (b.face) {
-          s = asph_face_dist(S.params + S.shapes[S.nodes[k].shape].param_offset, Lk, b);
-          face = b.face;
-          done = s < kBig;
-        }
-      }
-      if (!done) s = shape_dist_f<F>(S, k, Lk, false, nrm, face, err);
+      double s = shape_dist_f<F>(S, k, local_ray(S, k, nv.p, nv.d, pf, df), false, nrm, face, err);
       // ties: leaving the mother first, then the lowest node id (placement order)
       if (s < best || (s == best && enter && k < xnode)) {
         best = s;
@@ -442,79 +418,62 @@ RBG_D int find_next_boundary_and_step_f(const DevScene& S, Nav& nv, double& step
         enter = true;
         nbest = nrm;
         xface = face;
-        cull = fminf(cull, __double2float_ru(s));
       }
     };
-    // the daughters the segment reaches, in placement order (scan) or in
-    // traversal order (BVH), to `fn`
-    auto traverse = [&](auto&& fn) {
-      if (!(F & kFeatBVH) || N.bvh_root < 0) {
-        // cull every daughter first, then pass the survivors in placement
-        // order (fn re-checks the box against the shrinking bound, so the
-        // tested set is the one a single pass would test)
-        for (int base = 0; base < N.child_count; base += 32) {
-          const int m = N.child_count - base < 32 ? N.child_count - base : 32;
-          unsigned mask = 0;
-          for (int i = 0; i < m; ++i) {
-            const rbg_node_aux& A = S.aux[S.children[N.child_begin + base + i]];
-            if (reach(A.lo, A.hi)) mask |= 1u << i;
-          }
-          while (mask) {
-            const int i = __ffs(mask) - 1;
-            mask &= mask - 1;
-            fn(S.children[N.child_begin + base + i]);
-          }
+    if (!(F & kFeatBVH) || N.bvh_root < 0) {
+      // cull every daughter first, then test the survivors in placement
+      // order (visit re-checks the box against the shrinking distance, so
+      // the tested set is the one a single pass would test)
+      for (int base = 0; base < N.child_count; base += 32) {
+        const int m = N.child_count - base < 32 ? N.child_count - base : 32;
+        unsigned mask = 0;
+        for (int i = 0; i < m; ++i) {
+          const rbg_node_aux& A = S.aux[S.children[N.child_begin + base + i]];
+          if (reach(A.lo, A.hi)) mask |= 1u << i;
         }
-      } else {
-        // two phases: the traversal only collects the daughters whose boxes
-        // the segment reaches, then fn runs over the list.  Lanes whose
-        // traversals take different turns thus still call the (FP64, often
-        // composite) distance together, candidate j at once, instead of one
-        // lane at a time from inside the loop.  The lowest-id tie rule makes
-        // the result independent of the order.
-        constexpr int kCand = 8;
-        int cand[kCand];
-        int nc = 0;
-        int stack[32];
-        int sp = 0;
-        stack[sp++] = N.bvh_root;
-        while (sp > 0) {
-          const rbg_bvh_node& bn = S.bvh[stack[--sp]];
-          if (!reach(bn.lo, bn.hi)) continue;
-          if (bn.left < 0) {
-            for (int i = 0; i < bn.right; ++i) {
-              const int k = S.bvh_items[bn.item_begin + i];
-              const rbg_node_aux& A = S.aux[k];
-              if (!reach(A.lo, A.hi)) continue;
-              if (nc == kCand) {
-                for (int j = 0; j < kCand; ++j) fn(cand[j]);
-                nc = 0;
-              }
-              cand[nc++] = k;
+        while (mask) {
+          const int i = __ffs(mask) - 1;
+          mask &= mask - 1;
+          visit(S.children[N.child_begin + base + i]);
+        }
+      }
+    } else {
+      // two phases: the traversal only collects the daughters whose boxes
+      // the segment reaches, then the shape distances run over the list.
+      // Lanes whose traversals take different turns thus still call the
+      // (FP64, often composite) distance together, candidate j at once,
+      // instead of one lane at a time from inside the loop.  visit re-checks
+      // each box against the distance found so far; the lowest-id tie rule
+      // makes the result independent of the order.
+      constexpr int kCand = 8;
+      int cand[kCand];
+      int nc = 0;
+      int stack[32];
+      int sp = 0;
+      stack[sp++] = N.bvh_root;
+      while (sp > 0) {
+        const rbg_bvh_node& b = S.bvh[stack[--sp]];
+        if (!reach(b.lo, b.hi)) continue;
+        if (b.left < 0) {
+          for (int i = 0; i < b.right; ++i) {
+            const int k = S.bvh_items[b.item_begin + i];
+            const rbg_node_aux& A = S.aux[k];
+            if (!reach(A.lo, A.hi)) continue;
+            if (nc == kCand) {
+              for (int j = 0; j < kCand; ++j) visit(cand[j]);
+              nc = 0;
             }
-          } else if (sp + 2 <= 32) {
-            stack[sp++] = bn.right;
-            stack[sp++] = bn.left;
-          } else {
-            err |= ERR_BIT_CAP;
+            cand[nc++] = k;
           }
+        } else if (sp + 2 <= 32) {
+          stack[sp++] = b.right;
+          stack[sp++] = b.left;
+        } else {
+          err |= ERR_BIT_CAP;
         }
-        for (int j = 0; j < nc; ++j) fn(cand[j]);
       }
-    };
-    // Pass 1 (mothers of aspheric disks): FP32 brackets of the aspheric
-    // daughters; a sure bracket's upper end bounds the step, so in pass 2
-    // only the daughters that can be the nearest are polished in FP64
-    if (S.aux[c].flags & RBG_AUX_ASPH_CHILDREN) {
-      traverse([&](int k) {
-        const rbg_node_aux& A = S.aux[k];
-        if (!is_asph(k) || !reach(A.lo, A.hi)) return;
-        AsphBracket b;
-        bracket(k, local_ray(S, k, nv.p, nv.d, pf, df), b);
-        if (b.face) cull = fminf(cull, b.hi);
-      });
+      for (int j = 0; j < nc; ++j) visit(cand[j]);
     }
-    traverse(visit);
     if (lazy && !(enter && best < (double)exit_lo)) {
       d3 en = mk(0, 0, 1);
       const double e = box_dist_fast(S.params + S.shapes[N.shape].param_offset, Lc.p, Lc.d, true, en);

@@ -16,7 +16,10 @@ tests never read the reference at run time:
                   from it: run header, input-card line count, telescope
                   positions, event header, array offsets and every bunch
 
-  python tests/golden/make_fixtures.py /root/reference
+  python tests/golden/make_fixtures.py REFERENCE_ROOT
+
+REFERENCE_ROOT defaults to $ROBAST_REFERENCE, else to a checkout named
+"reference" beside this repository.
 """
 import json
 import os
@@ -104,4 +107,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    default = os.environ.get("ROBAST_REFERENCE") or os.path.join(
+        os.path.dirname(os.path.abspath(__file__)), "..", "..", "..", "reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else os.path.normpath(default))

@@ -54,16 +54,20 @@ def lib():
     return _lib
 
 
-def trace(manager, rays, threads: int = 1, history: int = 0):
+def trace(manager, rays, threads: int = 1, history: int = 0, flat: str = "independent"):
     """Trace a copy of `rays` (ARayArray) with the oracle using the manager's
-    scene and options.  Returns (status, dict of result arrays)."""
+    scene and options.  The oracle reads the scene as flattened
+    independently of the product (flat_ref.py) unless flat == "product".
+    Returns (status, dict of result arrays)."""
+    import flat_ref
     from robast_gb300.manager import make_result
 
     scene = manager._ensure_scene()
+    fs = flat_ref.independent_flat(scene).flat if flat == "independent" else scene.flat
     res, keep = make_result(len(rays), history)
     opts = manager.trace_options()
     rs = rays.rays_struct()
-    st = lib().orc_trace(C.byref(scene.flat), C.byref(rs), C.byref(res), C.byref(opts), threads)
+    st = lib().orc_trace(C.byref(fs), C.byref(rs), C.byref(res), C.byref(opts), threads)
     return st, keep
 
 
