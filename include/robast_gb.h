@@ -579,6 +579,17 @@ enum {
 int rbg_shoot(int32_t kind, const double* params, int64_t n, const double* rot,
               const double* tr, const double* dir, uint64_t seed,
               uint64_t first_id, double lambda, rbg_rays* out);
+/* The same generators writing DEVICE arrays on `stream` (one thread per
+ * ray; params, rot, tr and dir stay host pointers): ray i draws exactly
+ * what rbg_shoot draws for it, and the random-circle, -cone and -rectangle
+ * sources and the grids give bit-identical rays (the sphere sources call
+ * the device's cos / sin / acos, which may differ in the last bit).  out->n
+ * is the capacity on entry and the count written on return; RBG_ERR_ARG if
+ * the source needs more.  Returns after the launch; nothing is allocated. */
+int rbg_shoot_device(int32_t kind, const double* params, int64_t n,
+                     const double* rot, const double* tr, const double* dir,
+                     uint64_t seed, uint64_t first_id, double lambda,
+                     rbg_rays* out, void* stream);
 
 #ifdef __cplusplus
 }

@@ -205,6 +205,8 @@ def _declare(L):
                                                C.c_double, C.c_double, C.c_double, vp, vp]
     L.rbg_shoot.argtypes = [C.c_int32, _dp, C.c_int64, _dp, _dp, _dp, C.c_uint64, C.c_uint64,
                             C.c_double, C.POINTER(Rays)]
+    L.rbg_shoot_device.argtypes = [C.c_int32, _dp, C.c_int64, _dp, _dp, _dp, C.c_uint64, C.c_uint64,
+                                   C.c_double, C.POINTER(Rays), vp]
     fp = C.POINTER(C.c_float)
     ip = C.POINTER(C.c_int32)
     L.rbg_corsika_open.argtypes = [C.c_char_p, C.c_int64, C.POINTER(vp)]

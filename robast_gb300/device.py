@@ -203,3 +203,32 @@ def containment_radius(counts, xlo, xhi, ylo, yhi, fraction=0.8, stream=None):
     N.check(N.lib().rbg_containment_radius(_ptr(counts), nx, xlo, xhi, ny, ylo, yhi, fraction, C.byref(r),
                                            C.byref(x), C.byref(y), C.c_void_p(st)), "rbg_containment_radius")
     return r.value, x.value, y.value
+
+
+def shoot(kind: int, params, n: int, lam: float, rot=None, tr=None, v=None, seed=None, first_id: int = 0,
+          device="cuda:0", stream=None):
+    """An ARayShooter source (rbg_shoot's kinds and parameters) generated on
+    the GPU by rbg_shoot_device: a dict of device tensors x, y, z, t, dx,
+    dy, dz, lam holding the same rays the host generator draws."""
+    torch = _torch()
+    from .manager import ARayShooter
+
+    cap = int(n)
+    if kind == N.RBG_SHOOT_CIRCLE:
+        cap = 1 + int(params[2]) * int(params[1]) * (int(params[1]) + 1) // 2
+    elif kind == N.RBG_SHOOT_RECTANGLE:
+        cap = int(params[2]) * int(params[3])
+    out = {f: torch.empty(cap, dtype=torch.float64, device=device) for f in RAY_FIELDS}
+    rays = _rays_struct(out)
+    dp = C.POINTER(C.c_double)
+    p = (C.c_double * max(1, len(params)))(*params)
+    r9 = (C.c_double * 9)(*rot.R.reshape(-1)) if rot is not None else None
+    t3 = (C.c_double * 3)(*tr.t) if tr is not None else None
+    d3 = (C.c_double * 3)(*[float(a) for a in v]) if v is not None else None
+    s = ARayShooter.seed if seed is None else seed
+    st = (stream if stream is not None else torch.cuda.current_stream()).cuda_stream
+    N.check(N.lib().rbg_shoot_device(kind, C.cast(p, dp), int(n), C.cast(r9, dp) if r9 else None,
+                                     C.cast(t3, dp) if t3 else None, C.cast(d3, dp) if d3 else None, s,
+                                     first_id, lam, C.byref(rays), C.c_void_p(st)), "rbg_shoot_device")
+    m = rays.n
+    return {f: t[:m] for f, t in out.items()}
