@@ -1339,39 +1339,51 @@ RBG_D bool asph_newton_f(const float* Pf, int n, const LRay& L, float& t_out, fl
   const float px = L.pf.x, py = L.pf.y, pz = L.pf.z - Pf[n == 1 ? RBG_ASPH_Z1 : RBG_ASPH_Z2];
   const float dx = L.df.x, dy = L.df.y, dz = L.df.z;
   float H2 = px * px + py * py;
-  float p = -(pz * dz + px * dx + py * dy);
-  float M = p * dz + pz;
-  float M2 = pz * pz + H2 - p * p;
-  float check = 1.f - (M2 * curve - 2.f * M) * curve / dz / dz;
-  if (!(check >= 0.f)) return false;
-  float tf = p + (M2 * curve - 2.f * M) / (dz * (1.f + sqrtf(check)));
+  const float p = -(pz * dz + px * dx + py * dy);
+  const float M = p * dz + pz;
+  // the spherical first guess; a flat vertex (curve 0) takes the plane
+  float tf;
+  if (curve != 0.f) {
+    const float M2 = pz * pz + H2 - p * p;
+    const float idz = __frcp_rn(dz);
+    const float check = 1.f - (M2 * curve - 2.f * M) * curve * idz * idz;
+    if (!(check >= 0.f)) return false;
+    tf = p + __fdividef((M2 * curve - 2.f * M) * idz, 1.f + sqrtf(check));
+  } else {
+    tf = p - __fdividef(M, dz);
+  }
+  const float ick = curve != 0.f ? __frcp_rn(curve * kappa) : 0.f;
   float nx = px + tf * dx, ny = py + tf * dy, nz = pz + tf * dz;
   for (int i = 0; i < 40; i++) {
     H2 = nx * nx + ny * ny;
-    check = 1.f - kappa * H2 * curve * curve;
-    if (check < 0) return false;
-    float l = sqrtf(check);
-    float x = 0.f, v = 0.f;
+    float l = 1.f;
+    if (curve != 0.f) {
+      const float ch = 1.f - kappa * H2 * curve * curve;
+      if (ch < 0) return false;
+      l = sqrtf(ch);
+    }
+    // x = sum K_j H2^(j+1) (+ the conic), v = sum (j+1) K_j H2^j
+    float x = 0.f, v = 0.f, jf = (float)npol;
     for (int j = npol - 1; j >= 0; --j) {
       x = (x + Kf[j]) * H2;
-      v = v * H2 + 2.f * (j + 1) * Kf[j];
+      v = fmaf(v, H2, jf * Kf[j]);
+      jf -= 1.f;
     }
-    if (curve != 0.f) x += (1.f - l) / curve / kappa;
-    v = curve * kappa + l * v;
-    float m = -nx * v, nn = -ny * v;
-    float norm = sqrtf(l * l + m * m + nn * nn);
-    l /= norm;
-    m /= norm;
-    nn /= norm;
-    check = dz * l + dx * m + dy * nn;
+    if (curve != 0.f) x += (1.f - l) * ick;
+    // the surface gradient (l, m, nn) up to a factor; the Newton step along
+    // the ray needs only the ratio of its z component to its projection
+    // on the direction, so it is not normalised
+    const float g = curve * kappa + l * 2.f * v;
+    const float m = -nx * g, nn = -ny * g;
+    const float check = dz * l + dx * m + dy * nn;
     if (check == 0.f) return false;
-    const float scale = l / check;  // dt per unit sag residual
-    float e = scale * (x - nz);
+    const float scale = __fdividef(l, check);  // dt per unit sag residual
+    const float e = scale * (x - nz);
     tf += e;
     nx += e * dx;
     ny += e * dy;
     nz += e * dz;
-    if (fabsf(e) < 4e-6f * (1.f + fabsf(nz) + sqrtf(H2))) {
+    if (fabsf(e) < 4e-6f * (1.f + fabsf(nz) + fabsf(nx) + fabsf(ny))) {
       if (!isfinite(tf)) return false;
       t_out = tf;
       scale_out = scale;
@@ -1471,7 +1483,8 @@ RBG_D bool asph_wall_maybe_f(const float* Pf, bool outer, const LRay& L, float l
   float nsq = dx * dx + dy * dy;
   if (nsq < 1e-20f) return false;
   float rsq = px * px + py * py, rdotn = px * dx + py * dy;
-  float b = rdotn / nsq, delta = b * b - (rsq - R * R) / nsq;
+  const float insq = __frcp_rn(nsq);
+  float b = rdotn * insq, delta = b * b - (rsq - R * R) * insq;
   const float pad = 1e-3f + 1e-5f * (R + fabsf(pz));
   if (delta < -pad) return false;
   float sq = sqrtf(fmaxf(delta, 0.f));
@@ -1530,7 +1543,8 @@ RBG_D double asph_dist_out_f(const double* P, const float* Pf, const LRay& L, bo
   const float dx = L.df.x, dy = L.df.y, dzz = L.df.z;
   float t0 = 0.f, t1 = 3.0e38f;
   if (dzz != 0.f) {
-    float ta = (-Z - oz) / dzz, tb = (Z - oz) / dzz;
+    const float idz = __frcp_rn(dzz);
+    float ta = (-Z - oz) * idz, tb = (Z - oz) * idz;
     t0 = fmaxf(t0, fminf(ta, tb));
     t1 = fminf(t1, fmaxf(ta, tb));
   } else if (fabsf(oz) > Z) {
@@ -1544,7 +1558,8 @@ RBG_D double asph_dist_out_f(const double* P, const float* Pf, const LRay& L, bo
     float disc = B * B - A * C;
     if (disc < 0.f) return kBig;
     float sq = sqrtf(disc);
-    float c0 = (-B - sq) / A, c1 = (-B + sq) / A;
+    const float iA = __frcp_rn(A);
+    float c0 = (-B - sq) * iA, c1 = (-B + sq) * iA;
     const float lo = fmaxf(t0, c0), hi = fminf(t1, c1);
     if (lo > hi + pad + 1e-5f * (fabsf(lo) + fabsf(hi))) return kBig;
   }
@@ -1695,7 +1710,7 @@ RBG_D bool box_exit_bounds_f(const float* Pf, const LRay& L, float& lo, float& h
     }
     const float o = pf[k] - Pf[RBG_BOX_OX + k];
     const float half = Pf[RBG_BOX_DX + k];
-    const float inv = 1.0f / df[k];
+    const float inv = __frcp_rn(df[k]);
     const float t = ((df[k] > 0.f ? half : -half) - o) * inv;
     const float e = 1e-6f * ((fabsf(pf[k]) + fabsf(Pf[RBG_BOX_OX + k]) + half) * fabsf(inv) + fabsf(t)) + 1e-30f;
     lo = fminf(lo, t - e);

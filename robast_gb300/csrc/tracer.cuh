@@ -402,7 +402,7 @@ RBG_D int find_next_boundary_and_step_f(const DevScene& S, Nav& nv, double& step
     xnode = c;
     enter = false;
     const bool zx = df.x == 0.f, zy = df.y == 0.f, zz = df.z == 0.f;
-    const float ix = zx ? 0.f : 1.0f / df.x, iy = zy ? 0.f : 1.0f / df.y, iz = zz ? 0.f : 1.0f / df.z;
+    const float ix = zx ? 0.f : __frcp_rn(df.x), iy = zy ? 0.f : __frcp_rn(df.y), iz = zz ? 0.f : __frcp_rn(df.z);
     auto reach = [&](const float* lo, const float* hi) {
       return seg_box_f32(pf.x, pf.y, pf.z, ix, iy, iz, zx, zy, zz, best >= kBig ? 3e38f : (float)best, lo, hi);
     };
