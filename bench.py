@@ -256,6 +256,57 @@ def cpu_baseline(man, batch, sample):
                       f"{cores} threads, contiguous chunks"}, st
 
 
+def fma_peaks(N, torch):
+    """FP64 and FP32 FMA rates (FLOP/s) of this GPU from the library's
+    microbenchmark (independent FMA chains timed with CUDA events)."""
+    import ctypes as C
+
+    out = {}
+    st = torch.cuda.current_stream().cuda_stream
+    for bits in (64, 32):
+        v = C.c_double()
+        N.check(N.lib().rbg_measure_fma_peak(bits, C.byref(v), C.c_void_p(st)), "rbg_measure_fma_peak")
+        out[bits] = v.value
+    return out
+
+
+def roofline(man, rays, n, seg, kernel_ms, prec, workload, device, N, torch):
+    """The tracer kernel against its three ceilings: HBM (algorithmic ray
+    bytes), the FP64 pipe and the FP32 pipe (algorithmic flops from the
+    counting build's events, rbg_trace_count_events, for scenes it counts);
+    the bound is the largest fraction.  Peaks: HBM from the measured copy
+    bandwidth, FMA rates measured here."""
+    hbm, how = peaks()
+    alg_bytes = n * BYTES_PER_RAY + seg * BYTES_PER_SEGMENT
+    t = kernel_ms / 1e3
+    fr = {"hbm": {"achieved": alg_bytes / t / 1e9, "peak": hbm, "unit": "GB/s", "peak_source": how}}
+    fr["hbm"]["frac"] = fr["hbm"]["achieved"] / hbm
+    counts = None
+    if prec == N.PREC_MIXED:
+        try:
+            counts, f64, f32 = device.count_events(man, rays)
+        except Exception:
+            counts = None
+    if counts is not None:
+        pk = fma_peaks(N, torch)
+        for key, fl, bits in (("fp64", f64, 64), ("fp32", f32, 32)):
+            fr[key] = {"achieved": fl / t / 1e12, "peak": pk[bits] / 1e12, "unit": "TFLOP/s",
+                       "frac": fl / t / pk[bits], "peak_source": "measured here (FMA microbenchmark)",
+                       "flops_per_launch": fl}
+    bound = max(fr, key=lambda k: fr[k]["frac"])
+    out = {"bound": bound, "achieved": fr[bound]["achieved"], "peak": fr[bound]["peak"], "unit": fr[bound]["unit"],
+           "frac": fr[bound]["frac"],
+           "traffic": (DRAM_BYTES_PER_RAY_SC * n if workload == "schwarzschild_couder" and prec == N.PREC_MIXED
+                       else None),
+           "kernel_ms": kernel_ms, "fractions": fr,
+           "note": "achieved = algorithmic work per launch / the tracer kernel's own duration (CUDA events "
+                   "around its launch); bytes = 88 B per ray + 104 B per segment; flops = counted events x "
+                   "flops per event kind (rbg_event_flops)"}
+    if counts is not None:
+        out["event_counts"] = counts
+    return out
+
+
 def spot_r80(device, res, group, g, lims, nbins=500):
     """r80 of group g's focused rays: the device histogram through the
     device ContainmentRadius."""
@@ -623,6 +674,8 @@ def main():
     # timed steps and time each step on its own
     flush = torch.empty(64 << 20, dtype=torch.float32, device=f"cuda:{local}") if n * 56 < 2 * 129e6 else None
 
+    kernel_ms = []
+
     def timed(p, out):
         for _ in range(args.warmup):
             device.trace(man, rays, out, precision=p)
@@ -631,12 +684,16 @@ def main():
         barrier()
         torch.cuda.synchronize()
         ev = lambda: torch.cuda.Event(enable_timing=True)
+        kernel_ms.clear()
         with ClockSampler(local) as ck:
             if flush is None:
                 e0, e1 = ev(), ev()
                 e0.record(stream)
                 for _ in range(args.steps):
                     device.trace(man, rays, out, precision=p)
+                    # the tracer kernel's own duration (events on its
+                    # stream around the launch, read after the call's sync)
+                    kernel_ms.append(N.lib().rbg_last_kernel_ms(man.scene.handle))
                 e1.record(stream)
                 torch.cuda.synchronize()
                 t = e0.elapsed_time(e1) / args.steps
@@ -649,6 +706,7 @@ def main():
                     device.trace(man, rays, out, precision=p)
                     b.record(stream)
                     pairs.append((a, b))
+                    kernel_ms.append(N.lib().rbg_last_kernel_ms(man.scene.handle))
                 torch.cuda.synchronize()
                 t = sum(a.elapsed_time(b) for a, b in pairs) / args.steps
         barrier()
@@ -663,12 +721,14 @@ def main():
     # every device allocation of the trace made up front (scene tables,
     # take-up order workspace, host pipeline slots)
     device.reserve(man, n)
+    N.check(N.lib().rbg_scene_set_timing(man.scene.handle, 1), "rbg_scene_set_timing")
     # autotune the mixed tracer's compaction threshold on this batch (outside
     # the timed region, like the warm-up) unless one was given
     tuned = None
     if prec == N.PREC_MIXED and args.compaction == 0:
         tuned = device.autotune(man, rays, res)
     ms, launches, clocks = timed(prec, res)
+    kms = float(np.mean(kernel_ms)) if kernel_ms and min(kernel_ms) > 0 else None
     seg = int((res["npoints"].to(torch.int64) - 1).sum().item())
     value = n * ws / (ms / 1e3)
     group = rays["group"]
@@ -740,23 +800,15 @@ def main():
 
     if rank != 0:
         return
-    hbm, how = peaks()
-    alg_bytes = n * BYTES_PER_RAY + seg * BYTES_PER_SEGMENT
-    achieved = alg_bytes / (ms / 1e3) / 1e9
+    roof = roofline(man, rays, n, seg, kms if kms else ms, prec, args.workload, device, N, torch)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if prec == N.PREC_FP64 else "f32+f64", "data": "synthetic",
             "config": workload_config(args.workload, n, args.precision), "gpu_launches": launches * args.steps,
             "segments_per_step": seg,
             "compaction": args.compaction or tuned,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm,
-                         "traffic": (DRAM_BYTES_PER_RAY_SC * n if args.workload == "schwarzschild_couder"
-                                     and prec == N.PREC_MIXED else None),
-                         "peak_source": how,
-                         "note": "algorithmic bytes = 88 B per ray + 104 B per segment (wavefront ray state); "
-                                 "the kernel keeps ray state in registers and is bound by the FP64 pipe "
-                                 "(56 % busy, 30 of 32 lanes active under ncu), not by HBM"},
+            "tracer_kernel_ms": kms,
+            "roofline": roof,
             "e2e": e2e, "clocks": clocks, "vs_plain_fp64": compare}
     if not args.no_grad and ws == 1 and args.workload == "schwarzschild_couder":
         line["grad"] = grad_bench(batch, rays, max(1, min(args.steps, 3)), device, N, torch)

@@ -472,6 +472,14 @@ int rbg_trace_host(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
 int rbg_trace_noalloc(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
                       const rbg_trace_opts* opts, void* stream);
 
+/* Kernel timing (no counterpart in the reference): with on != 0, every
+ * later rbg_trace of the scene records CUDA events on its stream around the
+ * tracer kernel itself (not the take-up order's kernels), and
+ * rbg_last_kernel_ms returns the last one's duration in ms (-1 when timing
+ * is off).  For roofline measurements. */
+int rbg_scene_set_timing(rbg_scene* scene, int32_t on);
+double rbg_last_kernel_ms(const rbg_scene* scene);
+
 /* Number of tracer kernel launches the last rbg_trace on this scene issued
  * (1 for either precision: the whole batch is one launch). */
 int rbg_last_launch_count(const rbg_scene* scene);
@@ -519,6 +527,24 @@ int rbg_containment_radius_async(const double* counts, int32_t nx,
  * (no counterpart in the reference).  Allocates and frees a small output
  * buffer; synchronises `stream`. */
 int rbg_measure_fma_peak(int32_t bits, double* flops_per_s, void* stream);
+
+/* Counted work of a mixed-precision trace (no counterpart in the reference):
+ * the same trace as rbg_trace with RBG_PREC_MIXED, through a build of the
+ * tracer that tallies each event of its arithmetic -- a boundary step, an
+ * FP64 polish step of an aspheric root, a Horner term, an FP32 Newton
+ * iteration, an FP32 screen, an FP64 fallback -- into counts[0 ..
+ * rbg_event_kinds() - 1] (n_counts >= that).  rbg_event_flops gives the
+ * FP64 and FP32 flops of one event of a kind, counted from the formulas it
+ * evaluates (an FMA counts 2); the sum over kinds is the trace's algorithmic
+ * flop count, the numerator of its FP64-pipe and FP32-pipe roofline
+ * fractions.  Only scenes of boxes and aspheric disks (two-mirror
+ * telescopes) are counted (RBG_ERR_UNSUPPORTED otherwise).  The take-up
+ * order runs when opts lends a workspace.  Synchronises `stream`. */
+int rbg_event_kinds(void);
+int rbg_event_flops(int32_t kind, double* fp64, double* fp32);
+int rbg_trace_count_events(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
+                           const rbg_trace_opts* opts, void* stream, uint64_t* counts,
+                           int32_t n_counts);
 
 /* ---- gradients ---------------------------------------------------------- */
 /* Parameters the adjoint differentiates.  Shifts and rotations are small

@@ -189,12 +189,18 @@ def _declare(L):
     L.rbg_scene_reserve.argtypes = [vp, C.c_int64, C.c_int32]
     L.rbg_trace_workspace_bytes.argtypes = [C.c_int64]
     L.rbg_measure_fma_peak.argtypes = [C.c_int32, _dp, vp]
+    L.rbg_event_flops.argtypes = [C.c_int32, _dp, _dp]
+    L.rbg_trace_count_events.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts), vp,
+                                         C.POINTER(C.c_uint64), C.c_int32]
     L.rbg_trace_workspace_bytes.restype = C.c_size_t
     L.rbg_trace.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts), vp]
     L.rbg_trace_host.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts)]
     L.rbg_scene_autotune.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts), vp,
                                      C.POINTER(C.c_int32)]
     L.rbg_last_launch_count.argtypes = [vp]
+    L.rbg_scene_set_timing.argtypes = [vp, C.c_int32]
+    L.rbg_last_kernel_ms.argtypes = [vp]
+    L.rbg_last_kernel_ms.restype = C.c_double
     L.rbg_multilayer_rt.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int64, vp, vp, vp, vp, vp, vp]
     L.rbg_focal_moments.argtypes = [C.c_int64, vp, vp, vp, vp, vp, C.c_int32, vp, vp]
     L.rbg_focal_histogram.argtypes = [C.c_int64, vp, vp, vp, C.c_int32, C.c_double, C.c_double,

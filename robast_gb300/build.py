@@ -26,7 +26,7 @@ ORACLE_BUILD = os.path.join(ORACLE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["trace_fp64.cu", "trace_mixed_all.cu", "trace_mixed_facets.cu", "trace_mixed_coated.cu",
               "trace_mixed_cones.cu", "trace_mixed_csg.cu", "capi.cu", "trace_mixed.cu", "adjoint.cu", "noalloc.cu",
-              "corsika_rays.cu", "ray_order.cu", "tmm.cu", "psf.cu", "fma_peak.cu", "shoot.cu"]
+              "corsika_rays.cu", "ray_order.cu", "tmm.cu", "psf.cu", "fma_peak.cu", "shoot.cu", "trace_count.cu"]
 CPP_SOURCES = ["scene.cpp", "shoot.cpp", "corsika.cpp"]
 
 

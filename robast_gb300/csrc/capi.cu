@@ -46,6 +46,11 @@ void release_device(rbg_scene* s) {
   for (void* p : s->dev->allocations) cudaFree(p);
   if (s->workspace) cudaFree(s->workspace);
   if (s->order_ws) cudaFree(s->order_ws);
+  for (void*& e : s->tev) {
+    if (e) cudaEventDestroy(static_cast<cudaEvent_t>(e));
+    e = nullptr;
+  }
+  s->timing = false;
   if (prev >= 0) cudaSetDevice(prev);
   delete s->dev;
   s->dev = nullptr;
@@ -155,6 +160,25 @@ extern "C" int rbg_scene_upload(rbg_scene* s) {
 
 extern "C" int rbg_last_launch_count(const rbg_scene* s) { return s ? s->last_launches : -1; }
 
+// CUDA events around the tracer kernel of every later rbg_trace on the scene
+// (created here, destroyed with the scene's device state)
+extern "C" int rbg_scene_set_timing(rbg_scene* s, int32_t on) {
+  if (!s) return RBG_ERR_ARG;
+  int rc = ensure_device(s);
+  if (rc) return rc;
+  if (on && !s->tev[0]) {
+    for (auto& e : s->tev) {
+      cudaEvent_t ev;
+      if (cudaEventCreate(&ev) != cudaSuccess) return RBG_ERR_CUDA;
+      e = ev;
+    }
+  }
+  s->timing = on != 0;
+  return RBG_OK;
+}
+
+extern "C" double rbg_last_kernel_ms(const rbg_scene* s) { return s && s->timing ? s->last_kernel_ms : -1.0; }
+
 // the two tracer launchers (trace_mixed.cu, trace_fp64.cu)
 namespace rbg {
 int launch_mixed(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o,
@@ -235,14 +259,18 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
       launches += 7;
     }
   }
+  cudaEvent_t* tev = reinterpret_cast<cudaEvent_t*>(s->tev);
+  if (s->timing && cudaEventRecord(tev[0], st) != cudaSuccess) return RBG_ERR_CUDA;
   if (o.precision == RBG_PREC_MIXED)
     rc = launch_mixed(s->dev->view, kr, ko, in->n, o, st, s->dev->err_flags, s->dev->counter, &launches);
   else
     rc = launch_fp64(s->dev->view, kr, ko, in->n, o, st, s->dev->err_flags, &launches);
   if (rc) return rc;
+  if (s->timing && cudaEventRecord(tev[1], st) != cudaSuccess) return RBG_ERR_CUDA;
   s->last_launches = launches;
   unsigned bits = 0;
   if ((rc = read_errors(s, st, &bits))) return rc;
+  if (s->timing && cudaEventElapsedTime(&s->last_kernel_ms, tev[0], tev[1]) != cudaSuccess) return RBG_ERR_CUDA;
   if (bits & ERR_BIT_NAN) return RBG_ERR_NAN;
   if (bits & ERR_BIT_CAP) return RBG_ERR_CAP;
   return RBG_OK;

@@ -8,6 +8,7 @@
 #include "robast_gb.h"
 #include "robast_gb_layout.h"
 #include "node_aux.h"
+#include "events.h"
 
 #define RBG_D __device__ __forceinline__
 

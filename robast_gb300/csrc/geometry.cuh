@@ -1116,6 +1116,7 @@ RBG_D double rcp_refined(double v) {
 // TGeoBBox distances for the mixed path (slabs; the same crossings the
 // exact-solid method finds for a box).
 RBG_D double box_dist_fast(const double* P, d3 p, d3 d, bool exit, d3& nrm) {
+  RBG_EVENT(EV_BOX64);
   const double o[3] = {p.x - P[RBG_BOX_OX], p.y - P[RBG_BOX_OY], p.z - P[RBG_BOX_OZ]};
   const double dd[3] = {d.x, d.y, d.z};
   if (exit) {
@@ -1247,9 +1248,11 @@ RBG_D LRay local_ray(const DevScene& S, int k, d3 p, d3 d, f3 pf, f3 df) {
   if (xf == RBG_XFORM_IDENTITY) return LRay{p, d, pf, df};
   const rbg_node& N = S.nodes[k];
   if (xf == RBG_XFORM_TRANSLATION) {
+    RBG_EVENT(EV_XFORM_T);
     d3 lp = mk(p.x - N.m[9], p.y - N.m[10], p.z - N.m[11]);
     return LRay{lp, d, to_f3(lp), df};
   }
+  RBG_EVENT(EV_XFORM_G);
   d3 lp = to_local(N.m, p), ld = dir_to_local(N.m, d);
   return LRay{lp, ld, to_f3(lp), to_f3(ld)};
 }
@@ -1257,6 +1260,7 @@ RBG_D LRay local_point(const DevScene& S, int k, d3 p, f3 pf) {
   const int xf = S.aux[k].xform;
   if (xf == RBG_XFORM_IDENTITY) return LRay{p, p, pf, pf};
   const rbg_node& N = S.nodes[k];
+  RBG_EVENT(xf == RBG_XFORM_TRANSLATION ? EV_XFORM_T : EV_XFORM_G);
   d3 lp = xf == RBG_XFORM_TRANSLATION ? mk(p.x - N.m[9], p.y - N.m[10], p.z - N.m[11]) : to_local(N.m, p);
   f3 lpf = to_f3(lp);
   return LRay{lp, lp, lpf, lpf};
@@ -1301,15 +1305,19 @@ RBG_D float asph_poly_f(const float* K, int n, float h, float& mag) {
 // the FP64 reference algorithms, out of line: taken only when a screen
 // cannot decide or the FP32 iteration breaks down
 RBG_NOINLINE double asph_dist_surface_exact(const double* P, int n, d3 point, d3 dir) {
+  RBG_EVENT(EV_DIST_EXACT);
   return asph_dist_surface(Asph{P}, n, point, dir);
 }
 RBG_NOINLINE double asph_dist_wall_exact(const double* P, bool outer, d3 point, d3 dir) {
+  RBG_EVENT(EV_WALL_EXACT);
   return asph_dist_wall(Asph{P}, outer, point, dir);
 }
 // Contains in FP64: for faces with c == 0 the sags are z + sum K_j H2^(j+1)
 // by FMA Horner (one sum when both faces share it); conic faces take the
 // full evaluation
 RBG_NOINLINE bool asph_contains_exact(const double* P, d3 p, bool twin) {
+  RBG_EVENT(EV_CONTAINS_EXACT);
+  RBG_EVENT_N(EV_HORNER64, (int)P[RBG_ASPH_NPOL1] + (twin ? 0 : (int)P[RBG_ASPH_NPOL2]));
   const double H2 = p.x * p.x + p.y * p.y;
   const double rmin = P[RBG_ASPH_RMIN], rmax = P[RBG_ASPH_RMAX];
   if (H2 > rmax * rmax || H2 < rmin * rmin) return false;
@@ -1321,6 +1329,8 @@ RBG_NOINLINE bool asph_contains_exact(const double* P, d3 p, bool twin) {
   return !(P[RBG_ASPH_Z2] + p2 < p.z);
 }
 RBG_NOINLINE d3 asph_normal_exact(const double* P, d3 point, d3 dir) {
+  RBG_EVENT(EV_NORMAL_EXACT);
+  RBG_EVENT_N(EV_HORNER64, 4 * ((int)P[RBG_ASPH_NPOL1] + (int)P[RBG_ASPH_NPOL2]) / 2);
   return asph_normal_fast(Asph{P}, point, dir);
 }
 
@@ -1355,6 +1365,8 @@ RBG_D bool asph_newton_f(const float* Pf, int n, const LRay& L, float& t_out, fl
   const float ick = curve != 0.f ? __frcp_rn(curve * kappa) : 0.f;
   float nx = px + tf * dx, ny = py + tf * dy, nz = pz + tf * dz;
   for (int i = 0; i < 40; i++) {
+    RBG_EVENT(EV_NEWTON32);
+    RBG_EVENT_N(EV_HORNER32, npol);
     H2 = nx * nx + ny * ny;
     float l = 1.f;
     if (curve != 0.f) {
@@ -1417,6 +1429,8 @@ RBG_D bool asph_polish(const double* P, int n, const LRay& L, double sc, double&
   const double kap64 = P[s1 ? RBG_ASPH_KAPPA1 : RBG_ASPH_KAPPA2];
   const double pz0 = L.p.z - P[s1 ? RBG_ASPH_Z1 : RBG_ASPH_Z2];
   for (int it = 0; it < 8; ++it) {
+    RBG_EVENT(EV_POLISH);
+    RBG_EVENT_N(EV_HORNER64, npol > 0 ? npol - 1 : 0);
     double qx = fma(t, L.d.x, L.p.x), qy = fma(t, L.d.y, L.p.y), qz = fma(t, L.d.z, pz0);
     double h2 = fma(qx, qx, qy * qy);
     double x = asph_poly(K, npol, h2);
@@ -1438,6 +1452,7 @@ RBG_D bool asph_polish(const double* P, int n, const LRay& L, double sc, double&
 // [rmin, rmax] (compared squared)
 RBG_D double asph_accept(const double* P, const LRay& L, double t) {
   if (t < 0) return kBig;
+  RBG_EVENT(EV_ACCEPT);
   double qx = fma(t, L.d.x, L.p.x), qy = fma(t, L.d.y, L.p.y);
   double h2 = fma(qx, qx, qy * qy);
   const double rmin = P[RBG_ASPH_RMIN], rmax = P[RBG_ASPH_RMAX];
@@ -1477,6 +1492,7 @@ RBG_D void asph_faces_f(const double* P, const float* Pf, const LRay& L, bool tw
 // test asph_wall_maybe makes, without conversions)
 RBG_D bool asph_wall_maybe_f(const float* Pf, bool outer, const LRay& L, float limit) {
   if (!outer && Pf[RBG_ASPH_RSEG] == 0.f) return false;
+  RBG_EVENT(EV_SCREEN32);
   const float R = outer ? Pf[RBG_ASPH_RMAX] : Pf[RBG_ASPH_RMIN];
   const float px = L.pf.x, py = L.pf.y, pz = L.pf.z;
   const float dx = L.df.x, dy = L.df.y, dz = L.df.z;
@@ -1534,6 +1550,7 @@ RBG_D double asph_dist4_f(const double* P, const float* Pf, const LRay& L, bool 
 // DistFromOutside (:383-412): the bounding-tube screen in FP32 (enlarged,
 // never rejecting a ray the exact TGeoTube test accepts), then the faces
 RBG_D double asph_dist_out_f(const double* P, const float* Pf, const LRay& L, bool twin, int& face) {
+  RBG_EVENT(EV_SCREEN32);
   // pad: 1e-4 cm, plus 1e-5 of the tube size and 1e-6 of the coordinates
   // (the float position and origin carry ~6e-8 relative error each)
   const float pad = 1e-4f + 1e-5f * (Pf[RBG_ASPH_RMAX] + Pf[RBG_ASPH_DZ]) +
@@ -1658,6 +1675,7 @@ RBG_D double asph_face_dist(const double* P, const LRay& L, const AsphBracket& b
 // (faces with c == 0; the screen margin is 2e-5 of the sum of the sag's term
 // magnitudes plus the coordinates, >10x the FP32 rounding of the sums)
 RBG_D bool asph_contains_f(const double* P, const float* Pf, const LRay& L, bool twin) {
+  RBG_EVENT(EV_SCREEN32);
   const float h = L.pf.x * L.pf.x + L.pf.y * L.pf.y;
   const float rmax = Pf[RBG_ASPH_RMAX], rmin = Pf[RBG_ASPH_RMIN];
   const float hr = 4e-6f * h + 1e-12f;
@@ -1680,6 +1698,7 @@ RBG_D bool asph_contains_f(const double* P, const float* Pf, const LRay& L, bool
 
 // TGeoBBox::Contains behind an FP32 screen
 RBG_D bool box_contains_f(const double* P, const float* Pf, const LRay& L) {
+  RBG_EVENT(EV_SCREEN32);
   const float ax = fabsf(L.pf.x - Pf[RBG_BOX_OX]), ay = fabsf(L.pf.y - Pf[RBG_BOX_OY]),
               az = fabsf(L.pf.z - Pf[RBG_BOX_OZ]);
   const float ex = 1e-6f * (fabsf(L.pf.x) + fabsf(Pf[RBG_BOX_OX]) + Pf[RBG_BOX_DX]) + 1e-30f;
@@ -1697,6 +1716,7 @@ RBG_D bool box_contains_f(const double* P, const float* Pf, const LRay& L) {
 // false when an axis's direction underflows to zero in float while it is
 // not zero in FP64 (then only the FP64 distance is valid).
 RBG_D bool box_exit_bounds_f(const float* Pf, const LRay& L, float& lo, float& hi) {
+  RBG_EVENT(EV_SCREEN32);
   const float pf[3] = {L.pf.x, L.pf.y, L.pf.z}, df[3] = {L.df.x, L.df.y, L.df.z};
   const double dd[3] = {L.d.x, L.d.y, L.d.z};
   lo = 3e38f;
@@ -1739,6 +1759,8 @@ RBG_D d3 asph_normal_f(const DevScene& S, int node, const double* P, const float
       const double H2 = L.p.x * L.p.x + L.p.y * L.p.y;
       // the derivative coefficients (j + 1) K_j come precomputed
       const double* dK = ST(S, S.nodes[node].shape) + RBG_TRIG_ASPH_DK;
+      RBG_EVENT(EV_NORMAL);
+      RBG_EVENT_N(EV_HORNER64, n1 > 0 ? n1 - 1 : 0);
       double dF = 0.0;
       if (n1 > 0) {
         dF = dK[n1 - 1];

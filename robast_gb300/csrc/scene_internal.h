@@ -44,6 +44,11 @@ struct rbg_scene {
   rbg_device_scene* dev = nullptr;
   int dev_id = -1;
   int last_launches = 0;
+  // kernel timing of rbg_trace (rbg_scene_set_timing): CUDA events around
+  // the tracer kernel, its last duration in ms
+  bool timing = false;
+  void* tev[2] = {nullptr, nullptr};
+  float last_kernel_ms = -1.f;
   int tuned_compaction = 0;  // rbg_scene_autotune's choice, 0: none yet
   void* workspace = nullptr;
   size_t workspace_bytes = 0;

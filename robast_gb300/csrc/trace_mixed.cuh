@@ -44,6 +44,10 @@ __global__ void __launch_bounds__(kMixedBlock) trace_mixed_kernel(DevScene S, Ke
   bool drained = false;  // warp-uniform: the global queue is empty
   unsigned err = 0;
   r.status = RBG_STOP;
+#ifdef RBG_COUNT_EVENTS
+  for (int k = threadIdx.x; k < EV_COUNT; k += blockDim.x) rbg_block_events[k] = 0;
+  __syncthreads();
+#endif
   for (;;) {
     unsigned need = __ballot_sync(FULL, !active);
     // refill once enough lanes are idle (compaction threshold): fewer,
@@ -87,6 +91,10 @@ __global__ void __launch_bounds__(kMixedBlock) trace_mixed_kernel(DevScene S, Ke
     }
   }
   if (err) atomicOr(err_flags, err);
+#ifdef RBG_COUNT_EVENTS
+  __syncthreads();
+  for (int k = threadIdx.x; k < EV_COUNT; k += blockDim.x) atomicAdd(&rbg_event_totals[k], rbg_block_events[k]);
+#endif
 }
 
 // Launch over n rays on stream st: one block per resident slot of every SM

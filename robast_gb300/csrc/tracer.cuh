@@ -35,6 +35,7 @@ RBG_D bool node_contains(const DevScene& S, int k, d3 p) {
 template <typename T>
 RBG_D bool seg_box_f32(float ox, float oy, float oz, float ix, float iy, float iz, bool zx, bool zy, bool zz,
                        float smax, const T* lo, const T* hi) {
+  RBG_EVENT(EV_SCREEN32);
   float t0 = 0.f, t1 = smax;
   const float o3[3] = {ox, oy, oz}, i3[3] = {ix, iy, iz};
   const bool z3[3] = {zx, zy, zz};
@@ -486,6 +487,7 @@ RBG_D int find_next_boundary_and_step_f(const DevScene& S, Nav& nv, double& step
       }
     }
   }
+  RBG_EVENT(EV_SEGMENT);
   nv.p = nv.p + (best + RBG_BOUNDARY_PUSH) * nv.d;
   nv.xnode = xnode;
   nv.xn = nbest;
@@ -1074,6 +1076,7 @@ RBG_D void do_reflection(const DevScene& S, Nav& nv, Ray& r, double n1, double s
   }
   double t = MIXED ? r.t + step * (n1 * (1.0 / RBG_SPEED_OF_LIGHT_CM)) : r.t + step / (RBG_SPEED_OF_LIGHT_CM / n1);
   nv.p = nv.p - RBG_REFLECT_BACKSTEP * d1;
+  RBG_EVENT(EV_REFLECT);
   nv.node = MIXED ? locate_from_top_f<F>(S, nv.p) : locate_from_top<F>(S, nv.p);
   nv.d = d2;
   add_point(r, nv.p, t);
@@ -1322,6 +1325,7 @@ RBG_D bool load_ray_f(const KernelRays& in, const KernelOut& out, int64_t src, i
   r.rng.init(seed, id_offset + (uint64_t)i, 0);
   add_point(r, r.x, r.t);
   const double m2 = dot(dd, dd);
+  RBG_EVENT(EV_RAY);
   const bool bad = !finite_bits(r.x.x) || !finite_bits(r.x.y) || !finite_bits(r.x.z) || !finite_bits(dd.x) ||
                    !finite_bits(dd.y) || !finite_bits(dd.z) || !(m2 > 0) || !finite_bits(m2);
   if (bad) {

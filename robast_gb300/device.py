@@ -232,3 +232,37 @@ def shoot(kind: int, params, n: int, lam: float, rot=None, tr=None, v=None, seed
                                      first_id, lam, C.byref(rays), C.c_void_p(st)), "rbg_shoot_device")
     m = rays.n
     return {f: t[:m] for f, t in out.items()}
+
+
+# event kinds of rbg_trace_count_events, in the order of the counts
+EVENT_KINDS = ("segment", "ray", "xform_t", "xform_g", "polish", "horner64", "accept", "normal", "normal_exact",
+               "contains_exact", "box64", "dist_exact", "wall_exact", "reflect", "newton32", "horner32", "screen32")
+
+
+def count_events(manager, rays, res=None, stream=None):
+    """rbg_trace_count_events: the mixed trace of `rays` through the
+    counting build.  Returns (counts per event kind, FP64 flops, FP32
+    flops) of the whole trace."""
+    torch = _torch()
+    L = N.lib()
+    scene = manager._ensure_scene()
+    n = rays["x"].numel()
+    if res is None:
+        res = alloc_result(n, rays["x"].device)
+    opts = manager.trace_options(N.PREC_MIXED)
+    ws = workspace(n, rays["x"].device)
+    if ws is not None:
+        opts.workspace = ws.data_ptr()
+        opts.workspace_bytes = ws.numel()
+    k = L.rbg_event_kinds()
+    counts = (C.c_uint64 * k)()
+    st = (stream if stream is not None else torch.cuda.current_stream()).cuda_stream
+    N.check(L.rbg_trace_count_events(scene.handle, C.byref(_rays_struct(rays)), C.byref(_result_struct(res)),
+                                     C.byref(opts), C.c_void_p(st), counts, k), "rbg_trace_count_events")
+    f64 = f32 = 0.0
+    for i in range(k):
+        a, b = C.c_double(), C.c_double()
+        N.check(L.rbg_event_flops(i, C.byref(a), C.byref(b)), "rbg_event_flops")
+        f64 += counts[i] * a.value
+        f32 += counts[i] * b.value
+    return [int(c) for c in counts], f64, f32
