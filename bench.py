@@ -198,7 +198,7 @@ def grad_bench(batch, rays, steps, device, N, torch):
 
     def adjoint_eval():
         params = torch.tensor(p0, dtype=torch.float64, requires_grad=True)
-        x, y, f = TF.apply(params, build, rays)
+        x, y, f = TF.apply(params, build, rays)[:3]
         loss_of(x, y, f & stable).backward()
         return params.grad.clone()
 

@@ -569,18 +569,27 @@ typedef struct {
  * which has no gradients: replaces the finite-difference Minuit scans of
  * tutorials/Optimize.C:60-205).  `fwd` is the DEVICE result of a trace of
  * the same rays with a point/node history (hist_cap >= the points of every
- * contributing ray); dL_dx/dy/dz are DEVICE cotangents of each ray's final
- * point (NULL = 0).  Accumulates (+=) into the DEVICE array dL_dparams:
+ * contributing ray); lambda (DEVICE, the rays' wavelengths) is needed when
+ * the scene has lenses; dL_dx/dy/dz are DEVICE cotangents of each ray's
+ * final point and g_points (DEVICE, n * hist_cap * 3, x y z per recorded
+ * point) cotangents of its recorded reflection / refraction points (either
+ * may be NULL = 0; a loss on a rim margin at a mirror uses the latter).
+ * Accumulates (+=) into the DEVICE array dL_dparams:
  *   dL/dp_k = sum_i dL/dx_i . dx_i/dp_k
- * Segments are recomputed from the recorded hit points; reflections and
- * surface intersections are differentiated (implicit-function rule at each
- * hit, mirror-normal curvature included).  Rays whose path refracts are
- * skipped and counted in *n_skipped (host, may be NULL). */
+ * Segments are recomputed from the recorded hit points; surface
+ * intersections (implicit-function rule at each hit), reflections (mirror
+ * normal curvature included) and refractions (Snell's transmitted
+ * direction, src/AOpticsManager.cxx:146-155, with the indices of the media
+ * located along the path) are differentiated, with each ray's branches
+ * (transmit, Fresnel or total internal reflection) held fixed.  Rays whose
+ * path has more than 22 such events or an unsupported surface are skipped
+ * and counted in *n_skipped (host, may be NULL). */
 int rbg_trace_adjoint(rbg_scene* scene, int64_t n, const rbg_result* fwd,
-                      const double* dL_dx, const double* dL_dy,
-                      const double* dL_dz, int32_t n_params,
-                      const rbg_adjoint_param* params, double* dL_dparams,
-                      int64_t* n_skipped, void* stream);
+                      const double* lambda, const double* dL_dx,
+                      const double* dL_dy, const double* dL_dz,
+                      const double* g_points, int32_t n_params,
+                      const rbg_adjoint_param* params,
+                      double* dL_dparams, int64_t* n_skipped, void* stream);
 
 /* ---- ray sources -------------------------------------------------------- */
 /* ARayShooter generators (include/ARayShooter.h:25-51,

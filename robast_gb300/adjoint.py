@@ -37,8 +37,8 @@ def _declare():
     L = N.lib()
     if not getattr(L, "_adj_declared", False):
         L.rbg_trace_adjoint.argtypes = [C.c_void_p, C.c_int64, C.POINTER(N.Result), C.c_void_p, C.c_void_p,
-                                        C.c_void_p, C.c_int32, C.POINTER(AdjointParam), C.c_void_p,
-                                        C.POINTER(C.c_int64), C.c_void_p]
+                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(AdjointParam),
+                                        C.c_void_p, C.POINTER(C.c_int64), C.c_void_p]
         L._adj_declared = True
     return L
 
@@ -64,8 +64,10 @@ def trace_with_history(manager, rays, precision=N.PREC_MIXED, history=8, stream=
     return res, st
 
 
-def vjp(manager, res, specs: List[ParamSpec], gx, gy, gz=None, stream=None):
-    """dL/dp for cotangents (gx, gy, gz) of the final points (device tensors)."""
+def vjp(manager, res, specs: List[ParamSpec], gx, gy, gz=None, stream=None, lam=None, gpts=None):
+    """dL/dp for cotangents (gx, gy, gz) of the final points and gpts
+    (n, hist_cap, 3) of the recorded points (device tensors, None = 0);
+    lam: the rays' wavelengths (needed by scenes with lenses)."""
     import torch
 
     L = _declare()
@@ -75,9 +77,10 @@ def vjp(manager, res, specs: List[ParamSpec], gx, gy, gz=None, stream=None):
     out = torch.zeros(len(specs), dtype=torch.float64, device=res["x"].device)
     skipped = C.c_int64(0)
     st = (stream if stream is not None else torch.cuda.current_stream()).cuda_stream
-    N.check(L.rbg_trace_adjoint(manager.scene.handle, n, C.byref(rr), device._ptr(gx), device._ptr(gy),
-                                device._ptr(gz), len(specs), arr, device._ptr(out), C.byref(skipped),
-                                C.c_void_p(st)), "rbg_trace_adjoint")
+    gp = gpts.contiguous() if gpts is not None else None
+    N.check(L.rbg_trace_adjoint(manager.scene.handle, n, C.byref(rr), device._ptr(lam), device._ptr(gx),
+                                device._ptr(gy), device._ptr(gz), device._ptr(gp), len(specs), arr,
+                                device._ptr(out), C.byref(skipped), C.c_void_p(st)), "rbg_trace_adjoint")
     return out, skipped.value
 
 
@@ -85,28 +88,34 @@ def make_trace_function():
     import torch
 
     class TraceFunction(torch.autograd.Function):
-        """forward(params, build, rays, precision) -> (x, y, focused).
+        """forward(params, build, rays, precision, history) ->
+        (x, y, focused, points, nodes).
 
         ``build(params_numpy) -> (manager, [ParamSpec])`` constructs the
-        scene at the given parameter values."""
+        scene at the given parameter values.  points (n, history, 3) are
+        the recorded hit points (differentiable at reflections,
+        refractions and the end point), nodes (n, history) their nodes."""
 
         @staticmethod
-        def forward(ctx, params, build: Callable, rays, precision=N.PREC_MIXED):
+        def forward(ctx, params, build: Callable, rays, precision=N.PREC_MIXED, history=8):
             man, specs = build(params.detach().cpu().numpy())
-            res, st = trace_with_history(man, rays, precision)
+            res, st = trace_with_history(man, rays, precision, history)
             if st not in (N.RBG_OK,):
                 N.check(st, "rbg_trace")
             focused = res["status"] == N.RBG_FOCUS
-            ctx.man, ctx.specs, ctx.res = man, specs, res
+            ctx.man, ctx.specs, ctx.res, ctx.lam = man, specs, res, rays["lam"]
             ctx.param_device, ctx.param_dtype = params.device, params.dtype
-            ctx.mark_non_differentiable(focused)
-            return res["x"].clone(), res["y"].clone(), focused
+            nodes = res["hist_node"].clone()
+            ctx.mark_non_differentiable(focused, nodes)
+            return res["x"].clone(), res["y"].clone(), focused, res["hist_xyzt"][..., :3].clone(), nodes
 
         @staticmethod
-        def backward(ctx, gx, gy, _gf):
-            g, skipped = vjp(ctx.man, ctx.res, ctx.specs, gx.contiguous(), gy.contiguous())
+        def backward(ctx, gx, gy, _gf, gp, _gn):
+            gx = gx.contiguous() if gx is not None else None
+            gy = gy.contiguous() if gy is not None else None
+            g, skipped = vjp(ctx.man, ctx.res, ctx.specs, gx, gy, lam=ctx.lam, gpts=gp)
             ctx.skipped = skipped
-            return g.to(device=ctx.param_device, dtype=ctx.param_dtype), None, None, None
+            return g.to(device=ctx.param_device, dtype=ctx.param_dtype), None, None, None, None
 
     return TraceFunction
 
@@ -184,3 +193,38 @@ def fd_steps(params):
     h[16:19] = 1e-4
     h[19:22] = 1e-6
     return h
+
+
+# ---------------------------------------------------------------------------
+# Schmidt-Cassegrain batch (configuration 5): per misalignment sample, the
+# secondary's shift in x and y and rotation about x and y (through its
+# displaced vertex), as increments on top of the drawn misalignment
+# ---------------------------------------------------------------------------
+def sct_builder(n_samples: int, seed: int = 5):
+    """build(params) for configs.schmidt_cassegrain with 4 parameters per
+    sample (shift x, shift y, rotation x, rotation y of its secondary)."""
+    from .configs import schmidt_cassegrain
+
+    def build(p):
+        inc = np.asarray(p, dtype=float).reshape(n_samples, 4)
+        man, _ = schmidt_cassegrain(n_rays=n_samples, n_samples=n_samples, seed=seed, increments=inc)
+        names = man.scene.node_names()
+        flat = man.scene.flat
+        specs = []
+        for v in range(n_samples):
+            k = names.index(f"secondary{v}")
+            # the rotation pivot: the node's vertex (local (0, 0, zs)) in the world
+            sdisk = man.scene.builder.volume_objs[flat.nodes[k].volume].shape
+            zs = max(sdisk.z1, sdisk.z2)
+            m = np.array(flat.nodes[k].m[:])
+            pivot = tuple(m[:9].reshape(3, 3) @ np.array([0.0, 0.0, zs]) + m[9:])
+            specs += [ParamSpec(ADJ_NODE_SHIFT, k, a) for a in range(2)]
+            specs += [ParamSpec(ADJ_NODE_ROTATE, k, a, pivot=pivot) for a in range(2)]
+        return man, specs
+
+    return build
+
+
+def sct_fd_steps(n_samples: int):
+    """Central-difference steps: 1e-4 cm shifts, 1e-6 rad rotations."""
+    return np.tile([1e-4, 1e-4, 1e-6, 1e-6], n_samples)

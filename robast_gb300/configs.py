@@ -332,7 +332,16 @@ def _quarter_wave_stack(air, substrate, n_pairs=10, lam0=450 * nm, nh=2.4, nl=1.
     return ml
 
 
-def _sct_unit(world, tag, origin, corrector_index, coating, decenter=(0.0, 0.0), tilt=(0.0, 0.0)):
+def _rot_of(tilt):
+    """The secondary's drawn tilt as a matrix: RotateX then RotateY."""
+    r = TGeoRotation("", 0, 0, 0)
+    r.RotateX(math.degrees(tilt[0]))
+    r.RotateY(math.degrees(tilt[1]))
+    return r.R
+
+
+def _sct_unit(world, tag, origin, corrector_index, coating, decenter=(0.0, 0.0), tilt=(0.0, 0.0),
+              inc=(0.0, 0.0, 0.0, 0.0)):
     s = 100 * cm / (12.183 * INCH)  # 2-m primary
     off = 10 * cm
     ox, oy, oz = origin
@@ -370,6 +379,18 @@ def _sct_unit(world, tag, origin, corrector_index, coating, decenter=(0.0, 0.0),
     rot.RotateY(math.degrees(tilt[1]))
     c = np.array([0.0, 0.0, zs])
     t = c - rot.R @ c + np.array([decenter[0], decenter[1], 0.0]) + np.array([ox, oy, oz])
+    if any(inc):
+        # a further shift (inc[0], inc[1]) and rotation Rx(inc[2]) Ry(inc[3])
+        # about the displaced vertex, axes of the world: the parameters the
+        # adjoint differentiates (node shift / rotation at zero increment)
+        ax, ay = inc[2], inc[3]
+        rx = np.array([[1, 0, 0], [0, math.cos(ax), -math.sin(ax)], [0, math.sin(ax), math.cos(ax)]])
+        ry = np.array([[math.cos(ay), 0, math.sin(ay)], [0, 1, 0], [-math.sin(ay), 0, math.cos(ay)]])
+        ri = rx @ ry
+        pivot = np.array([ox + decenter[0], oy + decenter[1], oz + zs])
+        t = ri @ (t - pivot) + pivot + np.array([inc[0], inc[1], 0.0])
+        rot = TGeoRotation("", 0, 0, 0)
+        rot.SetMatrix(ri @ _rot_of(tilt))
     world.AddNode(secondary, 1, TGeoCombiTrans(t[0], t[1], t[2], rot))
     # focal screen behind the primary
     zf = ((0.65 + 40. + 32. - 30.86635 + 50.6706488) * INCH + off) * s
@@ -382,10 +403,13 @@ def _sct_unit(world, tag, origin, corrector_index, coating, decenter=(0.0, 0.0),
 
 
 def schmidt_cassegrain(n_rays: int = 100_000_000, n_samples: int = 256, seed: int = 5,
-                       decenter_sigma: float = 0.02 * cm, tilt_sigma: float = 0.1e-3, coating_table=None):
+                       decenter_sigma: float = 0.02 * cm, tilt_sigma: float = 0.1e-3, coating_table=None,
+                       increments=None):
     """coating_table: None (per-ray CoherentTMMMixed of the stack), or the
     (lam_nbins, lam_min, lam_max, th_nbins, th_min, th_max) arguments of
-    AMultilayer::PreCalculateCoherentTMM for the stack."""
+    AMultilayer::PreCalculateCoherentTMM for the stack.  increments: None,
+    or per sample (shift x, shift y, rotation x, rotation y) of its
+    secondary on top of the drawn misalignment (_sct_unit)."""
     man = AOpticsManager("manager", "Schmidt-Cassegrain")
     man.DisableFresnelReflection(True)
     side = int(math.ceil(math.sqrt(n_samples)))
@@ -404,7 +428,8 @@ def schmidt_cassegrain(n_rays: int = 100_000_000, n_samples: int = 256, seed: in
         origin = (spacing * (v % side - (side - 1) / 2), spacing * (v // side - (side - 1) / 2), 0.0)
         dec = tuple(decenter_sigma * rng.standard_normal(2))
         tilt = tuple(tilt_sigma * rng.standard_normal(2))
-        rap, zc = _sct_unit(world, v, origin, silica, coating, dec, tilt)
+        inc = tuple(increments[v]) if increments is not None else (0.0, 0.0, 0.0, 0.0)
+        rap, zc = _sct_unit(world, v, origin, silica, coating, dec, tilt, inc)
         units.append((origin, rap, zc))
     man.CloseGeometry()
     batches = []

@@ -12,8 +12,15 @@
 //     src/AOpticsManager.cxx:226-230), including the curvature term
 //     dn = (I - n n^T) H dP / |g| and the parameter term of g;
 //   * the 1e-6 + 1e-6 cm step back after a reflection (o' = P - eps d).
-// Straight-through crossings (entering an AOpticalComponent, ...) do not
-// change the path and are collapsed.  Rays that refract are skipped.
+//   * refraction d' = eta d + (c2 - eta c1) n at a lens face (DoFresnel's
+//     transmitted direction, src/AOpticsManager.cxx:146-155; c1 = d.n with n
+//     oriented along d, c2 = sqrt(1 - eta^2 (1 - c1^2)), eta = n1 / n2 at
+//     the ray's wavelength), with the boundary push o' = P + 1e-9 cm d;
+//     which branch a ray took (transmit, Fresnel reflection, total internal
+//     reflection) is read from its recorded path and held fixed, as the
+//     random draws are.
+// Straight-through crossings (entering an AOpticalComponent, or a medium of
+// the same index) do not change the path and are collapsed.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -25,7 +32,7 @@
 namespace rbg {
 
 constexpr int kAdjMaxParams = 64;
-constexpr int kAdjMaxEvents = 64;
+constexpr int kAdjMaxEvents = 24;
 
 struct Surf {
   d3 g;         // gradient of f in the master frame
@@ -276,10 +283,25 @@ struct AdjParams {
   rbg_adjoint_param p[kAdjMaxParams];
 };
 
+// true if `anc` is an ancestor of node k (or k itself)
+RBG_D bool is_within(const DevScene& S, int anc, int k) { return anc >= 0 && moves_with(S, anc, k); }
+
+// refractive index of the medium of node k at lam (1 outside lenses)
+RBG_D double medium_n(const DevScene& S, int k, double lam) {
+  if (k < 0 || S.nodes[k].kind != RBG_KIND_LENS) return 1.0;
+  return index_n(S, S.volumes[S.nodes[k].volume].index, lam);
+}
+
+// Event kinds of a recorded path: a point where the direction changes by a
+// reflection (mirror, Fresnel or total internal reflection) or by a
+// refraction; straight crossings between media of equal index are collapsed
+enum { kEvStart = 0, kEvReflect = 1, kEvRefract = 2, kEvFinal = 3 };
+
 __global__ void adjoint_kernel(DevScene S, int64_t n, const uint8_t* status, const int32_t* npoints,
                                int32_t hist_cap, const double* hist_xyzt, const int32_t* hist_node,
-                               const double* gx, const double* gy, const double* gz, int n_params,
-                               const AdjParams params_v, double* out, unsigned long long* skipped) {
+                               const double* lambda, const double* gx, const double* gy, const double* gz,
+                               const double* gpts, int n_params, const AdjParams params_v, double* out,
+                               unsigned long long* skipped) {
   __shared__ rbg_adjoint_param params[kAdjMaxParams];
   for (int k = threadIdx.x; k < n_params; k += blockDim.x) params[k] = params_v.p[k];
   __syncthreads();
@@ -288,42 +310,86 @@ __global__ void adjoint_kernel(DevScene S, int64_t n, const uint8_t* status, con
   unsigned long long nskip = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     d3 Pbar = mk(gx ? gx[i] : 0.0, gy ? gy[i] : 0.0, gz ? gz[i] : 0.0);
-    if (Pbar.x == 0 && Pbar.y == 0 && Pbar.z == 0) continue;
     const int np = npoints[i];
+    // cotangents of the recorded points (hit records), when given
+    const double* gp = gpts ? gpts + (size_t)i * hist_cap * 3 : nullptr;
+    auto gpt = [&](int j) { return gp ? mk(gp[3 * j], gp[3 * j + 1], gp[3 * j + 2]) : mk(0, 0, 0); };
+    bool any = !(Pbar.x == 0 && Pbar.y == 0 && Pbar.z == 0);
+    for (int j = 0; gp && !any && j < np && j < hist_cap; ++j) {
+      const d3 q = gpt(j);
+      any = q.x != 0 || q.y != 0 || q.z != 0;
+    }
+    if (!any) continue;
     if (np < 2 || np > hist_cap) {
       ++nskip;
       continue;
     }
     const double* h = hist_xyzt + (size_t)i * hist_cap * 4;
     const int32_t* hn = hist_node + (size_t)i * hist_cap;
-    // events: start, reflections, final point
-    int ev[kAdjMaxEvents];
+    auto pt = [&](int j) { return mk(h[4 * j], h[4 * j + 1], h[4 * j + 2]); };
+    const double lam = lambda ? lambda[i] : 0.0;
+    const bool lenses = S.features & kFeatLens;
+    // events: the start, every reflection and refraction, the final point.
+    // Media (for refractions) are located at the midpoints of the recorded
+    // segments; a point between two media of equal index is straight.
+    int ev[kAdjMaxEvents], evk[kAdjMaxEvents], evs[kAdjMaxEvents];
+    double eta[kAdjMaxEvents];
     int ne = 0;
     bool ok = true;
-    ev[ne++] = 0;
-    for (int j = 1; j < np - 1; ++j) {
-      int k = hn[j];
-      int kind = k >= 0 ? S.nodes[k].kind : kNull;
+    ev[ne] = 0;
+    evk[ne] = kEvStart;
+    evs[ne] = -1;
+    eta[ne] = 1.0;
+    ++ne;
+    int m_prev = lenses ? locate_from_top(S, 0.5 * (pt(0) + pt(1))) : -1;
+    for (int j = 1; j < np - 1 && ok; ++j) {
+      const int k = hn[j];
+      const int kind = k >= 0 ? S.nodes[k].kind : kNull;
+      int m_next = -1;
+      if (lenses) m_next = locate_from_top(S, 0.5 * (pt(j) + pt(j + 1)));
+      int ekind = -1, snode = -1;
+      double e_eta = 1.0;
       if (kind == RBG_KIND_MIRROR) {
-        if (ne >= kAdjMaxEvents - 1) {
+        ekind = kEvReflect;
+        snode = k;
+      } else if (lenses) {
+        const double n_in = medium_n(S, m_prev, lam), n_out = medium_n(S, m_next, lam);
+        const d3 din = normalized(pt(j) - pt(j - 1)), dout = normalized(pt(j + 1) - pt(j));
+        if (m_prev == m_next && dot(din - dout, din - dout) > 1e-18) {
+          // Fresnel or total internal reflection at a lens face
+          ekind = kEvReflect;
+          snode = (m_prev >= 0 && S.nodes[m_prev].kind == RBG_KIND_LENS) ? m_prev : k;
+        } else if (n_in != n_out) {
+          ekind = kEvRefract;
+          e_eta = n_in / n_out;
+          // the crossed surface belongs to the node entered, or to the one left
+          snode = is_within(S, m_prev, m_next) && m_next != m_prev ? m_next : m_prev;
+        }
+      }
+      if (ekind >= 0) {
+        if (ne >= kAdjMaxEvents - 1 || snode < 0) {
           ok = false;
           break;
         }
-        ev[ne++] = j;
-      } else if (kind == RBG_KIND_LENS) {
-        ok = false;  // refraction is not differentiated
-        break;
+        ev[ne] = j;
+        evk[ne] = ekind;
+        evs[ne] = snode;
+        eta[ne] = e_eta;
+        ++ne;
       }
+      m_prev = m_next;
     }
     if (!ok) {
       ++nskip;
       continue;
     }
-    ev[ne++] = np - 1;
-    auto pt = [&](int j) { return mk(h[4 * j], h[4 * j + 1], h[4 * j + 2]); };
+    ev[ne] = np - 1;
+    evk[ne] = kEvFinal;
+    ++ne;
     // final point: intersection with the surface of the entered node (or
     // the top volume when the ray left it)
     int m = ne - 1;
+    Pbar = Pbar + gpt(ev[m]);
     d3 Pm = pt(ev[m]);
     d3 Pprev = pt(ev[m - 1]);
     d3 dseg = normalized(Pm - Pprev);
@@ -349,34 +415,58 @@ __global__ void adjoint_kernel(DevScene S, int64_t n, const uint8_t* status, con
     d3 obar = Pbar - (pd / gd) * sf.g;
     d3 dbar = tseg * obar;
     for (int e = m - 1; e >= 1; --e) {
-      // reflection at event e: recorded point = hit - eps * d_in
-      d3 Prec = pt(ev[e]);
-      d3 Pin = pt(ev[e - 1]);
-      d3 din = normalized(Prec - Pin);
-      d3 Phit = Prec + RBG_REFLECT_BACKSTEP * din;
-      double t_in = sqrt(dot(Phit - Pin, Phit - Pin));
-      int node = hn[ev[e]];
+      const d3 Prec = pt(ev[e]);
+      const d3 Pin = pt(ev[e - 1]);
+      const d3 din = normalized(Prec - Pin);
+      const bool refl = evk[e] == kEvReflect;
+      // recorded point: reflection = hit - eps d_in (the step back),
+      // refraction = hit + push d_in (the boundary push)
+      const double off = refl ? -RBG_REFLECT_BACKSTEP : RBG_BOUNDARY_PUSH;
+      const d3 Phit = Prec - off * din;
+      const double t_in = sqrt(dot(Phit - Pin, Phit - Pin));
+      const int node = evs[e];
       if (!surface_at(S, node, Phit, sf)) {
         ok = false;
         break;
       }
-      double gn = sqrt(dot(sf.g, sf.g));
-      d3 nrm = (1.0 / gn) * sf.g;
-      // o_next = Phit - eps din
-      d3 Phbar = obar;
-      d3 dinbar = (-RBG_REFLECT_BACKSTEP) * obar;
-      // d_out = din - 2 (din.n) n
-      double dn = dot(din, nrm), ndb = dot(nrm, dbar);
-      dinbar = dinbar + dbar - (2 * ndb) * nrm;
-      d3 nbar = (-2.0) * (dn * dbar + ndb * din);
-      d3 gbar = (1.0 / gn) * (nbar - dot(nrm, nbar) * nrm);
+      const double gn = sqrt(dot(sf.g, sf.g));
+      // o_next = the recorded point = Phit + off d_in, with its own cotangent
+      const d3 Precbar = obar + gpt(ev[e]);
+      d3 Phbar = Precbar;
+      d3 dinbar = off * Precbar;
+      d3 gbar;
+      if (refl) {
+        const d3 nrm = (1.0 / gn) * sf.g;
+        // d_out = din - 2 (din.n) n
+        const double dn = dot(din, nrm), ndb = dot(nrm, dbar);
+        dinbar = dinbar + dbar - (2 * ndb) * nrm;
+        const d3 nbar = (-2.0) * (dn * dbar + ndb * din);
+        gbar = (1.0 / gn) * (nbar - dot(nrm, nbar) * nrm);
+      } else {
+        // d_out = eta din + (c2 - eta c1) nh, nh = s g / |g| oriented along
+        // din, c1 = din.nh, c2 = sqrt(1 - eta^2 (1 - c1^2))
+        const double sgn = dot(sf.g, din) < 0 ? -1.0 : 1.0;
+        const d3 nh = (sgn / gn) * sf.g;
+        const double et = eta[e];
+        const double c1 = dot(din, nh);
+        const double s2 = 1 - et * et * (1 - c1 * c1);
+        if (!(s2 > 0)) {
+          ok = false;
+          break;
+        }
+        const double c2 = sqrt(s2);
+        const double kk = et * et * c1 / c2 - et, sd = dot(nh, dbar);
+        dinbar = dinbar + et * dbar + (kk * sd) * nh;
+        const d3 nhbar = (c2 - et * c1) * dbar + (kk * sd) * din;
+        gbar = (sgn / gn) * (nhbar - dot(nh, nhbar) * nh);
+      }
       Phbar = Phbar + sym_vec(sf.H, gbar);
-      double gdi = dot(sf.g, din);
+      const double gdi = dot(sf.g, din);
       if (gdi == 0) {
         ok = false;
         break;
       }
-      double phd = dot(Phbar, din);
+      const double phd = dot(Phbar, din);
       for (int k = 0; k < n_params; ++k) {
         double df;
         d3 dg;
@@ -402,12 +492,15 @@ __global__ void adjoint_kernel(DevScene S, int64_t n, const uint8_t* status, con
 
 using namespace rbg;
 
-extern "C" int rbg_trace_adjoint(rbg_scene* s, int64_t n, const rbg_result* fwd, const double* gx, const double* gy,
-                                 const double* gz, int32_t n_params, const rbg_adjoint_param* params,
-                                 double* dL_dparams, int64_t* n_skipped, void* stream) {
+extern "C" int rbg_trace_adjoint(rbg_scene* s, int64_t n, const rbg_result* fwd, const double* lambda,
+                                 const double* gx, const double* gy, const double* gz, const double* g_points,
+                                 int32_t n_params,
+                                 const rbg_adjoint_param* params, double* dL_dparams, int64_t* n_skipped,
+                                 void* stream) {
   if (!s || !fwd || n < 0 || n_params < 0 || n_params > kAdjMaxParams || (n_params > 0 && (!params || !dL_dparams)))
     return RBG_ERR_ARG;
   if (!fwd->npoints || fwd->hist_cap <= 0 || !fwd->hist_xyzt || !fwd->hist_node) return RBG_ERR_ARG;
+  if ((s->features & kFeatLens) && n > 0 && !lambda) return RBG_ERR_ARG;  // refractive indices need it
   int rc = ensure_device(s);
   if (rc) return rc;
   for (int k = 0; k < n_params; ++k) {
@@ -431,8 +524,8 @@ extern "C" int rbg_trace_adjoint(rbg_scene* s, int64_t n, const rbg_result* fwd,
   int block = 128;
   int blocks = (int)std::min<int64_t>((n + block - 1) / block, (int64_t)sm_count() * 8);
   adjoint_kernel<<<blocks, block, 0, st>>>(s->dev->view, n, fwd->status, fwd->npoints, fwd->hist_cap,
-                                            fwd->hist_xyzt, fwd->hist_node, gx, gy, gz, n_params, pv, dL_dparams,
-                                            dskip);
+                                            fwd->hist_xyzt, fwd->hist_node, lambda, gx, gy, gz, g_points,
+                                            n_params, pv, dL_dparams, dskip);
   if (cudaGetLastError() != cudaSuccess) return RBG_ERR_CUDA;
   unsigned long long sk = 0;
   if (cudaMemcpyAsync(&sk, dskip, sizeof(sk), cudaMemcpyDeviceToHost, st) != cudaSuccess ||

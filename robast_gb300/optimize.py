@@ -56,7 +56,7 @@ class DesignOptimizer:
 
         with torch.no_grad():
             p = self._p0 + self._scale * self.u
-            x, y, f = self.TF.apply(p, self.build, self.rays)
+            x, y, f = self.TF.apply(p, self.build, self.rays)[:3]
             self.traces += 1
             return float(self.loss_fn(x, y, f))
 
@@ -65,7 +65,7 @@ class DesignOptimizer:
         optimiser update.  Returns the loss before the update."""
         self.opt.zero_grad()
         p = self._p0 + self._scale * self.u
-        x, y, f = self.TF.apply(p, self.build, self.rays)
+        x, y, f = self.TF.apply(p, self.build, self.rays)[:3]
         loss = self.loss_fn(x, y, f)
         loss.backward()
         self.traces += 2

@@ -58,7 +58,7 @@ def test_sc_gradient_vs_finite_differences(kind):
     rays = device.to_device(batch)
     params = torch.tensor(p0, dtype=torch.float64, requires_grad=True)
     TF = A.make_trace_function()
-    x, y, focused = TF.apply(params, build, rays)
+    x, y, focused = TF.apply(params, build, rays)[:3]
     m = torch.as_tensor(mask, device=x.device)
     assert bool((focused == m).all())
     loss = A.rms_spot(x, y, m) if kind == "rms" else A.r80_smooth(x, y, m)

@@ -36,7 +36,7 @@ def test_secondary_alignment_recovered_by_gradient_steps():
     best = min(opt.history)
     torch.cuda.synchronize()
     # the spot at the true alignment, for scale
-    x0, y0, f0 = opt.TF.apply(torch.zeros(6, dtype=torch.float64), build, rays)
+    x0, y0, f0 = opt.TF.apply(torch.zeros(6, dtype=torch.float64), build, rays)[:3]
     nominal = float(A.rms_spot(x0, y0, f0))
     # most of the excess spot size over the aligned design is removed (a
     # lateral shift and a tilt partly compensate each other, so the
