@@ -246,20 +246,21 @@ RBG_D bool moves_with(const DevScene& S, int anc, int k) {
 
 // d f / d theta and d g / d theta of parameter `p` at a hit on `node`
 RBG_D bool param_terms(const DevScene& S, const rbg_adjoint_param& p, int node, d3 P, const Surf& sf, double& df,
-                       d3& dg) {
+                       d3& dg, int moves = -1) {
   if (p.kind == RBG_ADJ_ASPH_COEF) {
     if (p.node != node || sf.face == 0 || !(p.faces & (1 << (sf.face - 1)))) return false;
     Asph a{SP(S, S.nodes[node].shape)};
     int j = p.index;
     if (j < 0 || j >= a.npol(sf.face)) return false;
-    double hj = 1;
-    for (int i = 0; i < j; ++i) hj *= sf.H2;  // H2^j
+    double hj = 1, b = sf.H2;  // H2^j by squaring
+    for (int e = j; e; e >>= 1, b *= b)
+      if (e & 1) hj *= b;
     df = -hj * sf.H2;                           // -H2^(j+1)
     d3 gl = mk(-2 * sf.x * (j + 1) * hj, -2 * sf.y * (j + 1) * hj, 0);
     dg = dir_to_master(sf.R, gl);
     return true;
   }
-  if (!moves_with(S, p.node, node)) return false;
+  if (!(moves >= 0 ? moves != 0 : moves_with(S, p.node, node))) return false;
   const int a = p.index;
   d3 e = mk(a == 0, a == 1, a == 2);
   if (p.kind == RBG_ADJ_NODE_SHIFT) {
@@ -297,16 +298,43 @@ RBG_D double medium_n(const DevScene& S, int k, double lam) {
 // refraction; straight crossings between media of equal index are collapsed
 enum { kEvStart = 0, kEvReflect = 1, kEvRefract = 2, kEvFinal = 3 };
 
-__global__ void adjoint_kernel(DevScene S, int64_t n, const uint8_t* status, const int32_t* npoints,
+// acc[k] += gbar . dg_k + c df_k over the parameters (unrolled to MAXP so
+// that the accumulators stay in registers); moves_with is evaluated once
+// per distinct parameter node
+template <int MAXP>
+RBG_D void add_terms(const DevScene& S, const rbg_adjoint_param* params, int n_params, int node, d3 P, const Surf& sf,
+                     d3 gbar, double c, double* acc) {
+  int last_node = -1, last_moves = 0;
+#pragma unroll
+  for (int k = 0; k < MAXP; ++k) {
+    if (k >= n_params) break;
+    const rbg_adjoint_param& p = params[k];
+    int mv = -1;
+    if (p.kind != RBG_ADJ_ASPH_COEF) {
+      if (p.node != last_node) {
+        last_node = p.node;
+        last_moves = moves_with(S, p.node, node);
+      }
+      mv = last_moves;
+    }
+    double df;
+    d3 dg;
+    if (param_terms(S, p, node, P, sf, df, dg, mv)) acc[k] += dot(gbar, dg) + c * df;
+  }
+}
+
+template <int MAXP>
+__global__ void __launch_bounds__(128) adjoint_kernel(DevScene S, int64_t n, const uint8_t* status, const int32_t* npoints,
                                int32_t hist_cap, const double* hist_xyzt, const int32_t* hist_node,
                                const double* lambda, const double* gx, const double* gy, const double* gz,
-                               const double* gpts, int n_params, const AdjParams params_v, double* out,
+                               const double* gpts, int n_params, const __grid_constant__ AdjParams params_v, double* out,
                                unsigned long long* skipped) {
   __shared__ rbg_adjoint_param params[kAdjMaxParams];
   for (int k = threadIdx.x; k < n_params; k += blockDim.x) params[k] = params_v.p[k];
   __syncthreads();
-  double acc[kAdjMaxParams];
-  for (int k = 0; k < n_params; ++k) acc[k] = 0;
+  double acc[MAXP];
+#pragma unroll
+  for (int k = 0; k < MAXP; ++k) acc[k] = 0;
   unsigned long long nskip = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     d3 Pbar = mk(gx ? gx[i] : 0.0, gy ? gy[i] : 0.0, gz ? gz[i] : 0.0);
@@ -407,11 +435,7 @@ __global__ void adjoint_kernel(DevScene S, int64_t n, const uint8_t* status, con
       continue;
     }
     double pd = dot(Pbar, dseg);
-    for (int k = 0; k < n_params; ++k) {
-      double df;
-      d3 dg;
-      if (param_terms(S, params[k], fnode, Pm, sf, df, dg)) acc[k] += -pd / gd * df;
-    }
+    add_terms<MAXP>(S, params, n_params, fnode, Pm, sf, mk(0, 0, 0), -pd / gd, acc);
     d3 obar = Pbar - (pd / gd) * sf.g;
     d3 dbar = tseg * obar;
     for (int e = m - 1; e >= 1; --e) {
@@ -467,18 +491,16 @@ __global__ void adjoint_kernel(DevScene S, int64_t n, const uint8_t* status, con
         break;
       }
       const double phd = dot(Phbar, din);
-      for (int k = 0; k < n_params; ++k) {
-        double df;
-        d3 dg;
-        if (param_terms(S, params[k], node, Phit, sf, df, dg)) acc[k] += dot(gbar, dg) - phd / gdi * df;
-      }
+      add_terms<MAXP>(S, params, n_params, node, Phit, sf, gbar, -phd / gdi, acc);
       obar = Phbar - (phd / gdi) * sf.g;
       dbar = dinbar + t_in * obar;
     }
     if (!ok) ++nskip;
   }
   // warp reduction, one atomic per warp and parameter
-  for (int k = 0; k < n_params; ++k) {
+#pragma unroll
+  for (int k = 0; k < MAXP; ++k) {
+    if (k >= n_params) break;
     double v = acc[k];
     for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
     if ((threadIdx.x & 31) == 0 && v != 0) atomicAdd(out + k, v);
@@ -523,9 +545,15 @@ extern "C" int rbg_trace_adjoint(rbg_scene* s, int64_t n, const rbg_result* fwd,
   if (cudaMemsetAsync(dskip, 0, sizeof(unsigned long long), st) != cudaSuccess) return RBG_ERR_CUDA;
   int block = 128;
   int blocks = (int)std::min<int64_t>((n + block - 1) / block, (int64_t)sm_count() * 8);
-  adjoint_kernel<<<blocks, block, 0, st>>>(s->dev->view, n, fwd->status, fwd->npoints, fwd->hist_cap,
-                                            fwd->hist_xyzt, fwd->hist_node, lambda, gx, gy, gz, g_points,
-                                            n_params, pv, dL_dparams, dskip);
+  // a small parameter list keeps its accumulators in registers
+  if (n_params <= 24)
+    adjoint_kernel<24><<<blocks, block, 0, st>>>(s->dev->view, n, fwd->status, fwd->npoints, fwd->hist_cap,
+                                                 fwd->hist_xyzt, fwd->hist_node, lambda, gx, gy, gz, g_points,
+                                                 n_params, pv, dL_dparams, dskip);
+  else
+    adjoint_kernel<kAdjMaxParams><<<blocks, block, 0, st>>>(s->dev->view, n, fwd->status, fwd->npoints,
+                                                            fwd->hist_cap, fwd->hist_xyzt, fwd->hist_node, lambda,
+                                                            gx, gy, gz, g_points, n_params, pv, dL_dparams, dskip);
   if (cudaGetLastError() != cudaSuccess) return RBG_ERR_CUDA;
   unsigned long long sk = 0;
   if (cudaMemcpyAsync(&sk, dskip, sizeof(sk), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
