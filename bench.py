@@ -618,6 +618,42 @@ def run_thinfilm(args):
                                  "by the FP64 pipe (complex transfer matrices), not by HBM"})
 
 
+def run_kernels(args):
+    """One small pass over every kernel of the library, for profilers (the
+    command of the ncu captures under profiles/): the Schwarzschild-Couder
+    batch traced by both tracers (with the take-up order's kernels), the
+    adjoint of its RMS spot, the focal-plane moments, histogram and
+    ContainmentRadius, and a device ray source.  Prints a one-line
+    summary; no timing."""
+    import torch
+
+    from robast_gb300 import _native as N
+    from robast_gb300 import adjoint as A
+    from robast_gb300 import build, configs, device
+
+    build.build_library()
+    n = args.rays or 3_000_000
+    _, batch = configs.schwarzschild_couder(n_rays=n)
+    rays = device.to_device(batch)
+    man, specs = A.sc_builder()(A.sc_parameters())
+    for _ in range(max(1, args.warmup)):
+        device.trace(man, rays, precision=N.PREC_MIXED)
+    device.trace(man, rays, precision=N.PREC_FP64)
+    res, st = A.trace_with_history(man, rays)
+    f = res["status"] == N.RBG_FOCUS
+    gx = torch.where(f, 2 * res["x"], torch.zeros_like(res["x"]))
+    gy = torch.where(f, 2 * res["y"], torch.zeros_like(res["y"]))
+    g, skipped = A.vjp(man, res, specs, gx, gy)
+    group = rays["group"]
+    mom = device.focal_moments(res, group, 5)
+    h = device.focal_histogram(res, 500, -2.0, 2.0, 500, -2.0, 2.0, mask=group == 0)
+    r80 = device.containment_radius(h, -2.0, 2.0, -2.0, 2.0, 0.8)[0]
+    shot = device.shoot(N.RBG_SHOOT_RANDOM_CIRCLE, [500.0], n, 400e-7, None, None, (0.0, 0.0, -1.0))
+    torch.cuda.synchronize()
+    print(json.dumps({"kernels": "ok", "rays": n, "focused": int(f.sum().item()), "adjoint_skipped": skipped,
+                      "r80_cm": r80, "shot": int(shot["x"].numel()), "moments_rays": float(mom[:, 0].sum())}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -633,7 +669,11 @@ def main():
     ap.add_argument("--compaction", type=int, default=0, help="mixed tracer refill threshold (0: tuned)")
     ap.add_argument("--no-parity", dest="parity", action="store_false",
                     help="skip the whole-batch oracle trace (the CPU baseline then times a sample)")
+    ap.add_argument("--kernels", action="store_true",
+                    help="one small pass over every kernel (for profilers), no timing")
     args = ap.parse_args()
+    if args.kernels:
+        return run_kernels(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "corsika":

@@ -9,9 +9,10 @@ points, so ``loss.backward()`` gives d loss / d parameters in one forward +
 one backward pass -- the gradient step that replaces the Minuit scans of
 tutorials/Optimize.C:60-205.
 
-The reference has no gradients; effective area (a count of focused rays)
-is piecewise constant in the parameters, so its pathwise gradient is zero
-and it is reported, not differentiated.
+The reference has no gradients.  Effective area (a count of focused rays)
+is piecewise constant in the parameters, so its pathwise gradient is zero;
+``sc_effective_area`` is a smooth surrogate whose gradient counts the rays
+the moving rims sweep across.
 """
 from __future__ import annotations
 
@@ -107,12 +108,18 @@ def make_trace_function():
             ctx.param_device, ctx.param_dtype = params.device, params.dtype
             nodes = res["hist_node"].clone()
             ctx.mark_non_differentiable(focused, nodes)
+            # outputs the loss does not use get no (zero-filled) cotangent
+            ctx.set_materialize_grads(False)
             return res["x"].clone(), res["y"].clone(), focused, res["hist_xyzt"][..., :3].clone(), nodes
 
         @staticmethod
         def backward(ctx, gx, gy, _gf, gp, _gn):
             gx = gx.contiguous() if gx is not None else None
             gy = gy.contiguous() if gy is not None else None
+            if gx is None and gy is None and gp is None:
+                ctx.skipped = 0
+                z = torch.zeros(len(ctx.specs), dtype=ctx.param_dtype, device=ctx.param_device)
+                return z, None, None, None, None
             g, skipped = vjp(ctx.man, ctx.res, ctx.specs, gx, gy, lam=ctx.lam, gpts=gp)
             ctx.skipped = skipped
             return g.to(device=ctx.param_device, dtype=ctx.param_dtype), None, None, None, None
@@ -228,3 +235,78 @@ def sct_builder(n_samples: int, seed: int = 5):
 def sct_fd_steps(n_samples: int):
     """Central-difference steps: 1e-4 cm shifts, 1e-6 rad rotations."""
     return np.tile([1e-4, 1e-4, 1e-6, 1e-6], n_samples)
+
+
+# ---------------------------------------------------------------------------
+# Effective area: a smooth surrogate with a pathwise gradient
+# ---------------------------------------------------------------------------
+def _rot_zyx(t):
+    """Rz(t[2]) Ry(t[1]) Rx(t[0]) (TGeoRotation's RotateX, then RotateY,
+    then RotateZ; radians) as a torch matrix."""
+    import torch
+
+    cx, sx = torch.cos(t[0]), torch.sin(t[0])
+    cy, sy = torch.cos(t[1]), torch.sin(t[1])
+    cz, sz = torch.cos(t[2]), torch.sin(t[2])
+    one, zero = torch.ones_like(cx), torch.zeros_like(cx)
+    rx = torch.stack([torch.stack([one, zero, zero]), torch.stack([zero, cx, -sx]), torch.stack([zero, sx, cx])])
+    ry = torch.stack([torch.stack([cy, zero, sy]), torch.stack([zero, one, zero]), torch.stack([-sy, zero, cy])])
+    rz = torch.stack([torch.stack([cz, -sz, zero]), torch.stack([sz, cz, zero]), torch.stack([zero, zero, one])])
+    return rz @ ry @ rx
+
+
+def sc_effective_area(params, pts, nodes, o, d, keep, area_per_ray, node_ids, width=1.0):
+    """Effective area of the Schwarzschild-Couder telescope (the focused
+    count times the area per ray, tutorials/SchwarzschildCouder.C:139) as a
+    smooth function of the parameters.  A focused ray passed five rims: it
+    missed the secondary on its way down (outside its 270 cm rim), hit the
+    primary between its 220 and 485 cm rims, hit the secondary inside its
+    rim and the focal surface inside its 100 cm rim.  Its weight is the
+    product of tanh(margin / width) over those margins, so
+    Aeff_s = area_per_ray * sum_i w_i over the rays of `keep` (focused).
+    The margins at the hit points carry the hit points' gradient (the
+    adjoint, through `pts`); the secondary's rim also moves with its shift
+    and tilt (params[16:22]) explicitly.  As width -> 0 the gradient counts
+    the rays a moving rim sweeps across (tanh' integrates to 1 over m > 0),
+    the derivative of the focused count the pathwise gradient cannot see.
+
+    pts, nodes: the recorded points and nodes (TraceFunction outputs); o, d:
+    the rays' start points and directions (n, 3); node_ids: physical node
+    ids of "primary", "secondary" and "focal"."""
+    import torch
+
+    from .configs import SC_ZS
+
+    R = _rot_zyx(params[19:22])
+    c = torch.tensor([0.0, 0.0, SC_ZS], dtype=params.dtype, device=params.device)
+    t = c - R @ c + params[16:19]
+    o_k, d_k = o[keep], d[keep]
+    P, Nn = pts[keep], nodes[keep]
+
+    def local_sec(v, direction=False):
+        return (v if direction else v - t) @ R  # R^T (v - t) for row vectors
+
+    # the secondary's rim height (its upper face at r = 270 cm)
+    ks = params[8:16]
+    r2 = 270.0 ** 2
+    z_rim = SC_ZS + 1e-4 + sum(ks[j] * r2 ** (j + 1) for j in range(8))
+    ol, dl = local_sec(o_k), local_sec(d_k, True)
+    s = (z_rim - ol[:, 2]) / dl[:, 2]
+    q = ol + s[:, None] * dl
+    m_shadow = torch.sqrt(q[:, 0] ** 2 + q[:, 1] ** 2) - 270.0
+
+    def at(node):
+        sel = (Nn == node).to(P.dtype)
+        return (P * sel[..., None]).sum(dim=1)  # the (one) recorded point on that node
+
+    pp = at(node_ids["primary"])
+    rp = torch.sqrt(pp[:, 0] ** 2 + pp[:, 1] ** 2)
+    ps = local_sec(at(node_ids["secondary"]))
+    rs = torch.sqrt(ps[:, 0] ** 2 + ps[:, 1] ** 2)
+    pf = at(node_ids["focal"])
+    rf = torch.sqrt(pf[:, 0] ** 2 + pf[:, 1] ** 2)
+    margins = [m_shadow, 485.0 - rp, rp - 220.0, 270.0 - rs, 100.0 - rf]
+    w = torch.ones_like(rp)
+    for m in margins:
+        w = w * torch.tanh(torch.clamp(m, min=0.0) / width)
+    return area_per_ray * w.sum()

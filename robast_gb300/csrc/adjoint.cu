@@ -36,110 +36,112 @@ constexpr int kAdjMaxEvents = 24;
 
 struct Surf {
   d3 g;         // gradient of f in the master frame
-  double H[9];  // Hessian of f in the master frame
-  // for aspheric faces: local point, face and derivative ingredients
+  // Hessian of f = Q Hl Q^T: Q (row-major, local -> master) the frame the
+  // surface is written in, Hl its symmetric local Hessian (h00 h01 h02 h11
+  // h12 h22)
+  double Q[9];
+  double h[6];
+  // for aspheric faces: local point, face and polynomial length
   int face;     // 1 lower, 2 upper, 0 not an aspheric face
+  int npol;
   double H2, x, y;
-  const double* R;  // node rotation (local -> master)
 };
 
-RBG_D d3 mat_vec(const double* R, d3 v) {
-  return mk(R[0] * v.x + R[1] * v.y + R[2] * v.z, R[3] * v.x + R[4] * v.y + R[5] * v.z,
-            R[6] * v.x + R[7] * v.y + R[8] * v.z);
-}
-RBG_D d3 sym_vec(const double* H, d3 v) {
-  return mk(H[0] * v.x + H[1] * v.y + H[2] * v.z, H[3] * v.x + H[4] * v.y + H[5] * v.z,
-            H[6] * v.x + H[7] * v.y + H[8] * v.z);
-}
 RBG_D d3 cross(d3 a, d3 b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+RBG_D double comp(d3 v, int a) { return a == 0 ? v.x : a == 1 ? v.y : v.z; }
 
-// H_w = R Hl R^T
-RBG_D void rotate_hessian(const double* R, const double* Hl, double* Hw) {
-  double T[9];
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) T[i * 3 + j] = R[i * 3] * Hl[j] + R[i * 3 + 1] * Hl[3 + j] + R[i * 3 + 2] * Hl[6 + j];
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) Hw[i * 3 + j] = T[i * 3] * R[j * 3] + T[i * 3 + 1] * R[j * 3 + 1] + T[i * 3 + 2] * R[j * 3 + 2];
-}
-
-// Sag of an aspheric face and its first two derivatives in H2 = x^2 + y^2:
-// F = z0 + c H2 / (1 + s) + sum K_j H2^(j+1), s = sqrt(1 - kappa c^2 H2);
-// the conic part equals (1 - s) / (kappa c), so dF = c / (2 s) + ..., and
-// d2F = kappa c^3 / (4 s^3) + ...
-RBG_D bool asph_sag2(const Asph& a, int face, double H2, double& F, double& dF, double& d2F) {
-  double c = a.c(face), k = a.kap(face);
-  double chk = 1 - k * c * c * H2;
-  if (chk <= 0) return false;
-  double s = sqrt(chk);
-  int n = a.npol(face);
-  const double* K = a.K(face);
-  double p = 0, dp = 0, d2p = 0;
-  for (int j = n - 1; j >= 0; --j) {
-    p = (p + K[j]) * H2;
-    dp = dp * H2 + (j + 1) * K[j];
-    d2p = j >= 1 ? d2p * H2 + (j + 1) * j * K[j] : d2p;
-  }
-  // d2p above accumulates sum (j+1) j K_j H2^(j-1) by Horner over j >= 1
-  F = a.z(face) + H2 * c / (1 + s) + p;
-  dF = c / (2 * s) + dp;
-  d2F = k * c * c * c / (4 * s * s * s) + d2p;
-  return true;
+// H v = Q (Hl (Q^T v)); also returns Q^T v (the local components of v)
+RBG_D d3 hess_vec(const Surf& sf, d3 v, d3& vl) {
+  vl = dir_to_local(sf.Q, v);
+  const double* h = sf.h;
+  const d3 hl = mk(h[0] * vl.x + h[1] * vl.y + h[2] * vl.z, h[1] * vl.x + h[3] * vl.y + h[4] * vl.z,
+                   h[2] * vl.x + h[4] * vl.y + h[5] * vl.z);
+  return dir_to_master(sf.Q, hl);
 }
 
 // Implicit function of the surface of node `node` nearest to the master
 // point P: value is ignored, only g and H are needed.  Returns false for
 // shapes whose surfaces the adjoint does not differentiate.
+//
+// Aspheric face f = z - F(H2), H2 = x^2 + y^2,
+// F = z0 + c H2 / (1 + s) + sum K_j H2^(j+1), s = sqrt(1 - kappa c^2 H2);
+// the conic part equals (1 - s) / (kappa c), so dF/dH2 = c / (2 s) + ...
+// and d2F/dH2^2 = kappa c^3 / (4 s^3) + ...  The face nearest to P is the
+// one of least |z - F| / sqrt(1 + 4 H2 F'^2), compared without roots.
 RBG_D bool surface_at(const DevScene& S, int node, d3 P, Surf& out) {
   const rbg_node& N = S.nodes[node];
   const rbg_shape_desc sh = S.shapes[N.shape];
-  d3 p = to_local(N.m, P);
-  out.R = N.m;
+  const d3 p = to_local(N.m, P);
   out.face = 0;
-  double Hl[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  out.npol = 0;
+  out.H2 = out.x = out.y = 0;
+  for (int i = 0; i < 6; ++i) out.h[i] = 0;
   d3 gl;
   if (sh.type == RBG_SHAPE_ASPHERIC_DISK) {
+    for (int i = 0; i < 9; ++i) out.Q[i] = N.m[i];
     Asph a{SP(S, N.shape)};
-    double H2 = p.x * p.x + p.y * p.y;
-    double best = kBig;
+    const double H2 = p.x * p.x + p.y * p.y;
+    // nearest face: dist^2 = dz^2 / q, compared as dz_a^2 q_b < dz_b^2 q_a
+    double best_dz2 = kBig * kBig, best_q = 1.0, best_dF = 0, best_rs = 0;
     int face = 0;
-    double dF = 0, d2F = 0;
     for (int f = 1; f <= 2; ++f) {
-      double Ff, dFf, d2Ff;
-      if (!asph_sag2(a, f, H2, Ff, dFf, d2Ff)) continue;
-      double dist = fabs(p.z - Ff) / sqrt(1 + 4 * H2 * dFf * dFf);
-      if (dist < best) {
-        best = dist;
+      const double c = a.c(f), k = a.kap(f);
+      const double chk = 1 - k * c * c * H2;
+      if (chk <= 0) continue;
+      const double s = sqrt(chk), rs = 1.0 / s;
+      const int n = a.npol(f);
+      const double* K = a.K(f);
+      double pp = 0, dp = 0;
+      for (int j = n - 1; j >= 0; --j) {
+        pp = (pp + K[j]) * H2;
+        dp = dp * H2 + (j + 1) * K[j];
+      }
+      const double F = a.z(f) + H2 * c / (1 + s) + pp;
+      const double dF = 0.5 * c * rs + dp;
+      const double dz = p.z - F, q = 1 + 4 * H2 * dF * dF;
+      if (dz * dz * best_q < best_dz2 * q) {
+        best_dz2 = dz * dz;
+        best_q = q;
+        best_dF = dF;
+        best_rs = rs;
         face = f;
-        dF = dFf;
-        d2F = d2Ff;
       }
     }
-    double r = sqrt(H2);
+    const double r = sqrt(H2);
     double wall = fabs(r - a.rmax());
     if (a.rseg()) wall = fmin(wall, fabs(r - a.rmin()));
-    if (face == 0 || wall < best) {
+    if (face == 0 || wall * wall * best_q < best_dz2) {
       // side wall: f = x^2 + y^2 - R^2
       gl = mk(2 * p.x, 2 * p.y, 0);
-      Hl[0] = 2;
-      Hl[4] = 2;
+      out.h[0] = 2;
+      out.h[3] = 2;
     } else {
       // f = z - F(x^2 + y^2)
+      const double c = a.c(face), k = a.kap(face);
+      const int n = a.npol(face);
+      const double* K = a.K(face);
+      double d2p = 0;  // sum (j+1) j K_j H2^(j-1)
+      for (int j = n - 1; j >= 1; --j) d2p = d2p * H2 + (j + 1) * j * K[j];
+      const double dF = best_dF, rs3 = best_rs * best_rs * best_rs;
+      const double d2F = 0.25 * k * c * c * c * rs3 + d2p;
       gl = mk(-2 * p.x * dF, -2 * p.y * dF, 1);
-      Hl[0] = -2 * dF - 4 * p.x * p.x * d2F;
-      Hl[1] = Hl[3] = -4 * p.x * p.y * d2F;
-      Hl[4] = -2 * dF - 4 * p.y * p.y * d2F;
+      out.h[0] = -2 * dF - 4 * p.x * p.x * d2F;
+      out.h[1] = -4 * p.x * p.y * d2F;
+      out.h[3] = -2 * dF - 4 * p.y * p.y * d2F;
       out.face = face;
+      out.npol = n;
       out.H2 = H2;
       out.x = p.x;
       out.y = p.y;
     }
   } else if (sh.type == RBG_SHAPE_COMPOSITE || sh.type == RBG_SHAPE_SPHERE || sh.type == RBG_SHAPE_BOX ||
              sh.type == RBG_SHAPE_TUBE || sh.type == RBG_SHAPE_PARABOLOID || sh.type == RBG_SHAPE_PGON) {
-    // nearest surface among the leaves (spheres, paraboloids, cylinders, planes)
+    // nearest surface among the leaves (spheres, paraboloids, cylinders,
+    // planes); each leaf's Hessian is diagonal in its own frame
     double best = kBig;
     M12 bestM = mat_identity();
     d3 bg = mk(0, 0, 1);
-    double bH[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double bh0 = 0, bh4 = 0, bh8 = 0;
     int stack_shape[8];
     M12 stack_m[8];
     int sp = 0;
@@ -168,10 +170,9 @@ RBG_D bool surface_at(const DevScene& S, int node, d3 P, Surf& out) {
           best = dist;
           bestM = M;
           bg = g;
-          for (int i = 0; i < 9; ++i) bH[i] = 0;
-          bH[0] = h0;
-          bH[4] = h4;
-          bH[8] = h8;
+          bh0 = h0;
+          bh4 = h4;
+          bh8 = h8;
         }
       };
       switch (ss.type) {
@@ -224,14 +225,18 @@ RBG_D bool surface_at(const DevScene& S, int node, d3 P, Surf& out) {
           break;
       }
     }
-    // leaf frame -> node frame
-    gl = dir_to_master(bestM.v, bg);
-    rotate_hessian(bestM.v, bH, Hl);
+    // the leaf's frame in the master frame: Q = R_node R_leaf
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        out.Q[i * 3 + j] = N.m[i * 3] * bestM.v[j] + N.m[i * 3 + 1] * bestM.v[3 + j] + N.m[i * 3 + 2] * bestM.v[6 + j];
+    out.h[0] = bh0;
+    out.h[3] = bh4;
+    out.h[5] = bh8;
+    gl = bg;
   } else {
     return false;
   }
-  out.g = dir_to_master(N.m, gl);
-  rotate_hessian(N.m, Hl, out.H);
+  out.g = dir_to_master(out.Q, gl);
   return true;
 }
 
@@ -240,41 +245,6 @@ RBG_D bool moves_with(const DevScene& S, int anc, int k) {
   for (int d = 0; k >= 0 && d < 64; ++d) {
     if (k == anc) return true;
     k = S.nodes[k].parent;
-  }
-  return false;
-}
-
-// d f / d theta and d g / d theta of parameter `p` at a hit on `node`
-RBG_D bool param_terms(const DevScene& S, const rbg_adjoint_param& p, int node, d3 P, const Surf& sf, double& df,
-                       d3& dg, int moves = -1) {
-  if (p.kind == RBG_ADJ_ASPH_COEF) {
-    if (p.node != node || sf.face == 0 || !(p.faces & (1 << (sf.face - 1)))) return false;
-    Asph a{SP(S, S.nodes[node].shape)};
-    int j = p.index;
-    if (j < 0 || j >= a.npol(sf.face)) return false;
-    double hj = 1, b = sf.H2;  // H2^j by squaring
-    for (int e = j; e; e >>= 1, b *= b)
-      if (e & 1) hj *= b;
-    df = -hj * sf.H2;                           // -H2^(j+1)
-    d3 gl = mk(-2 * sf.x * (j + 1) * hj, -2 * sf.y * (j + 1) * hj, 0);
-    dg = dir_to_master(sf.R, gl);
-    return true;
-  }
-  if (!(moves >= 0 ? moves != 0 : moves_with(S, p.node, node))) return false;
-  const int a = p.index;
-  d3 e = mk(a == 0, a == 1, a == 2);
-  if (p.kind == RBG_ADJ_NODE_SHIFT) {
-    const double* H = sf.H;
-    df = -(a == 0 ? sf.g.x : a == 1 ? sf.g.y : sf.g.z);
-    dg = mk(-H[a], -H[3 + a], -H[6 + a]);
-    return true;
-  }
-  if (p.kind == RBG_ADJ_NODE_ROTATE) {
-    d3 r = P - mk(p.pivot[0], p.pivot[1], p.pivot[2]);
-    d3 gxr = cross(sf.g, r);
-    df = a == 0 ? gxr.x : a == 1 ? gxr.y : gxr.z;
-    dg = cross(e, sf.g) + sym_vec(sf.H, cross(r, e));
-    return true;
   }
   return false;
 }
@@ -298,28 +268,45 @@ RBG_D double medium_n(const DevScene& S, int k, double lam) {
 // refraction; straight crossings between media of equal index are collapsed
 enum { kEvStart = 0, kEvReflect = 1, kEvRefract = 2, kEvFinal = 3 };
 
-// acc[k] += gbar . dg_k + c df_k over the parameters (unrolled to MAXP so
-// that the accumulators stay in registers); moves_with is evaluated once
-// per distinct parameter node
+// acc[k] += gbar . dg_k + c df_k over the parameters, with dg_k, df_k the
+// derivatives of the implicit function's gradient and value (unrolled to
+// MAXP so that the accumulators stay in registers):
+//   * coefficient K_j of the hit face:  df = -H2^(j+1), dg = Q (-2 (j+1)
+//     H2^j (x, y, 0)), so the term is H2^j (-2 (j+1) u - c H2) with
+//     u = (Q^T gbar) . (x, y, 0);
+//   * shift of a node the surface moves with, along axis a:  df = -g_a,
+//     dg = -H e_a, so the term is -w_a with w = H gbar + c g;
+//   * rotation about axis a through pivot o:  df = (g x r)_a, dg = e_a x g +
+//     H (r x e_a), r = P - o, so the term is (g x gbar)_a + (w x r)_a.
+// moves_with is evaluated once per distinct parameter node.
 template <int MAXP>
 RBG_D void add_terms(const DevScene& S, const rbg_adjoint_param* params, int n_params, int node, d3 P, const Surf& sf,
-                     d3 gbar, double c, double* acc) {
+                     double u, d3 w, d3 gxgbar, double c, double* acc) {
   int last_node = -1, last_moves = 0;
 #pragma unroll
   for (int k = 0; k < MAXP; ++k) {
     if (k >= n_params) break;
     const rbg_adjoint_param& p = params[k];
-    int mv = -1;
-    if (p.kind != RBG_ADJ_ASPH_COEF) {
-      if (p.node != last_node) {
-        last_node = p.node;
-        last_moves = moves_with(S, p.node, node);
-      }
-      mv = last_moves;
+    const int a = p.index;
+    if (p.kind == RBG_ADJ_ASPH_COEF) {
+      if (p.node != node || sf.face == 0 || !(p.faces & (1 << (sf.face - 1))) || a < 0 || a >= sf.npol) continue;
+      double hj = 1, b = sf.H2;  // H2^j by squaring
+      for (int e = a; e; e >>= 1, b *= b)
+        if (e & 1) hj *= b;
+      acc[k] += hj * (-2.0 * (a + 1) * u - c * sf.H2);
+      continue;
     }
-    double df;
-    d3 dg;
-    if (param_terms(S, p, node, P, sf, df, dg, mv)) acc[k] += dot(gbar, dg) + c * df;
+    if (p.node != last_node) {
+      last_node = p.node;
+      last_moves = moves_with(S, p.node, node);
+    }
+    if (!last_moves) continue;
+    if (p.kind == RBG_ADJ_NODE_SHIFT) {
+      acc[k] -= comp(w, a);
+    } else if (p.kind == RBG_ADJ_NODE_ROTATE) {
+      const d3 r = P - mk(p.pivot[0], p.pivot[1], p.pivot[2]);
+      acc[k] += comp(gxgbar, a) + comp(cross(w, r), a);
+    }
   }
 }
 
@@ -434,43 +421,50 @@ __global__ void __launch_bounds__(128) adjoint_kernel(DevScene S, int64_t n, con
       ++nskip;
       continue;
     }
-    double pd = dot(Pbar, dseg);
-    add_terms<MAXP>(S, params, n_params, fnode, Pm, sf, mk(0, 0, 0), -pd / gd, acc);
-    d3 obar = Pbar - (pd / gd) * sf.g;
+    const double cf = -dot(Pbar, dseg) / gd;
+    // at the final point gbar = 0: only the value terms c df remain
+    add_terms<MAXP>(S, params, n_params, fnode, Pm, sf, 0.0, cf * sf.g, mk(0, 0, 0), cf, acc);
+    d3 obar = Pbar + cf * sf.g;
     d3 dbar = tseg * obar;
     for (int e = m - 1; e >= 1; --e) {
       const d3 Prec = pt(ev[e]);
       const d3 Pin = pt(ev[e - 1]);
-      const d3 din = normalized(Prec - Pin);
+      const d3 seg = Prec - Pin;
+      const double L = sqrt(dot(seg, seg));
+      if (!(L > 0)) {
+        ok = false;
+        break;
+      }
+      const d3 din = (1.0 / L) * seg;
       const bool refl = evk[e] == kEvReflect;
       // recorded point: reflection = hit - eps d_in (the step back),
       // refraction = hit + push d_in (the boundary push)
       const double off = refl ? -RBG_REFLECT_BACKSTEP : RBG_BOUNDARY_PUSH;
       const d3 Phit = Prec - off * din;
-      const double t_in = sqrt(dot(Phit - Pin, Phit - Pin));
+      const double t_in = L - off;
       const int node = evs[e];
       if (!surface_at(S, node, Phit, sf)) {
         ok = false;
         break;
       }
-      const double gn = sqrt(dot(sf.g, sf.g));
+      const double rgn = rsqrt(dot(sf.g, sf.g));  // 1 / |g|
       // o_next = the recorded point = Phit + off d_in, with its own cotangent
       const d3 Precbar = obar + gpt(ev[e]);
       d3 Phbar = Precbar;
       d3 dinbar = off * Precbar;
       d3 gbar;
       if (refl) {
-        const d3 nrm = (1.0 / gn) * sf.g;
+        const d3 nrm = rgn * sf.g;
         // d_out = din - 2 (din.n) n
         const double dn = dot(din, nrm), ndb = dot(nrm, dbar);
         dinbar = dinbar + dbar - (2 * ndb) * nrm;
         const d3 nbar = (-2.0) * (dn * dbar + ndb * din);
-        gbar = (1.0 / gn) * (nbar - dot(nrm, nbar) * nrm);
+        gbar = rgn * (nbar - dot(nrm, nbar) * nrm);
       } else {
         // d_out = eta din + (c2 - eta c1) nh, nh = s g / |g| oriented along
         // din, c1 = din.nh, c2 = sqrt(1 - eta^2 (1 - c1^2))
         const double sgn = dot(sf.g, din) < 0 ? -1.0 : 1.0;
-        const d3 nh = (sgn / gn) * sf.g;
+        const d3 nh = (sgn * rgn) * sf.g;
         const double et = eta[e];
         const double c1 = dot(din, nh);
         const double s2 = 1 - et * et * (1 - c1 * c1);
@@ -482,17 +476,20 @@ __global__ void __launch_bounds__(128) adjoint_kernel(DevScene S, int64_t n, con
         const double kk = et * et * c1 / c2 - et, sd = dot(nh, dbar);
         dinbar = dinbar + et * dbar + (kk * sd) * nh;
         const d3 nhbar = (c2 - et * c1) * dbar + (kk * sd) * din;
-        gbar = (sgn / gn) * (nhbar - dot(nh, nhbar) * nh);
+        gbar = (sgn * rgn) * (nhbar - dot(nh, nhbar) * nh);
       }
-      Phbar = Phbar + sym_vec(sf.H, gbar);
+      d3 gbl;  // gbar in the surface's frame
+      const d3 Hgbar = hess_vec(sf, gbar, gbl);
+      Phbar = Phbar + Hgbar;
       const double gdi = dot(sf.g, din);
       if (gdi == 0) {
         ok = false;
         break;
       }
-      const double phd = dot(Phbar, din);
-      add_terms<MAXP>(S, params, n_params, node, Phit, sf, gbar, -phd / gdi, acc);
-      obar = Phbar - (phd / gdi) * sf.g;
+      const double c = -dot(Phbar, din) / gdi;
+      add_terms<MAXP>(S, params, n_params, node, Phit, sf, gbl.x * sf.x + gbl.y * sf.y, Hgbar + c * sf.g,
+                      cross(sf.g, gbar), c, acc);
+      obar = Phbar + c * sf.g;
       dbar = dinbar + t_in * obar;
     }
     if (!ok) ++nskip;

@@ -35,6 +35,15 @@ namespace {
 // key bits: about 4 cells per ray, at most 2^24 cells; a quarter of the
 // bits (at most 6) number the direction cell
 constexpr int kMinKeyBits = 12, kMaxKeyBits = 24, kMaxDirBits = 6;
+// Index chunks: the rays [c 2^s, (c + 1) 2^s) are ordered among themselves
+// and chunk c's rays are taken up before chunk c + 1's (the chunk is the
+// key's top field).  The rays in flight then write their results into one
+// or two chunks' stretch of the output arrays, which stays in L2 until its
+// sectors are complete, instead of into partial sectors all over the batch.
+// s = kChunkShift, raised until there are at most kMaxChunks chunks; 0
+// orders the batch as one chunk.
+constexpr int kChunkShift = 20, kMaxChunks = 32;
+constexpr int64_t kMaxBuckets = int64_t(1) << 25;
 constexpr int kScanTile = 1024;
 constexpr int kThreads = 256;
 
@@ -112,14 +121,17 @@ struct Plan {
   uint32_t qmax[6];
   int32_t bits[6];
   int8_t pos[6][kMaxKeyBits];
+  int32_t chunk_shift, cell_bits;  // key = (i >> chunk_shift) << cell_bits | cell
 };
 
 // Key bits go one at a time, most significant first, to the axis whose
 // cells are then longest (ties to the lower axis): dir_bits among the
 // direction axes, then pos_bits among the start-point axes.
-__global__ void plan_kernel(const uint32_t* box, int dir_bits, int pos_bits, Plan* plan) {
+__global__ void plan_kernel(const uint32_t* box, int dir_bits, int pos_bits, int chunk_shift, Plan* plan) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   Plan P;
+  P.chunk_shift = chunk_shift;
+  P.cell_bits = dir_bits + pos_bits;
   double size[6];
   for (int a = 0; a < 6; ++a) {
     const bool ok = box[a] <= box[6 + a];
@@ -159,7 +171,7 @@ __global__ void __launch_bounds__(kThreads) key_kernel(KernelRays in, int64_t n,
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double* v[6] = {in.x, in.y, in.z, in.dx, in.dy, in.dz};
-  uint32_t key = 0;
+  uint32_t key = plan->chunk_shift > 0 ? (uint32_t)(i >> plan->chunk_shift) << plan->cell_bits : 0u;
 #pragma unroll
   for (int a = 0; a < 6; ++a) {
     const float f = ((float)v[a][i] - plan->lo[a]) * plan->scale[a];
@@ -240,18 +252,26 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(const uint32_t* keys,
 }
 
 struct Layout {
-  int dir_bits, pos_bits;
+  int dir_bits, pos_bits, chunk_shift;
   int64_t buckets, tiles;
   size_t box, plan, keys, counts, tile_sum, order, sorted, total;
 };
 
 Layout layout(int64_t n) {
   Layout L;
+  int cs = kChunkShift;
+  if (cs > 0)
+    while (((n - 1) >> cs) + 1 > kMaxChunks) ++cs;
+  if (cs > 0 && (n - 1) >> cs == 0) cs = 0;  // one chunk
+  const int64_t chunks = cs > 0 ? ((n - 1) >> cs) + 1 : 1;
+  const int64_t per = cs > 0 ? (int64_t(1) << cs) : n;
   int kb = kMinKeyBits;
-  while (kb < kMaxKeyBits && (int64_t(1) << kb) < 4 * n) ++kb;
+  while (kb < kMaxKeyBits && (int64_t(1) << kb) < 4 * per) ++kb;
+  while (kb > kMinKeyBits && (chunks << kb) > kMaxBuckets) --kb;
+  L.chunk_shift = cs;
   L.dir_bits = kb / 4 < kMaxDirBits ? kb / 4 : kMaxDirBits;
   L.pos_bits = kb - L.dir_bits;
-  L.buckets = int64_t(1) << kb;
+  L.buckets = chunks << kb;
   L.tiles = (L.buckets + kScanTile - 1) / kScanTile;
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
   L.box = 0;
@@ -292,7 +312,7 @@ int build_ray_order(const KernelRays& in, int64_t n, void* ws, KernelRays* sorte
   const int64_t blocks = (n + kThreads - 1) / kThreads;
   const int box_blocks = (int)(blocks < 1216 ? blocks : 1216);
   bbox_kernel<<<box_blocks, kThreads, 0, st>>>(in, n, box);
-  plan_kernel<<<1, 32, 0, st>>>(box, L.dir_bits, L.pos_bits, plan);
+  plan_kernel<<<1, 32, 0, st>>>(box, L.dir_bits, L.pos_bits, L.chunk_shift, plan);
   key_kernel<<<(unsigned)blocks, kThreads, 0, st>>>(in, n, plan, keys, counts);
   tile_scan_counts<<<(unsigned)L.tiles, kScanTile, 0, st>>>(counts, L.buckets, tile_sum);
   scan_tile_sums<<<1, kScanTile, 0, st>>>(tile_sum, L.tiles);
