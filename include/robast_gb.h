@@ -267,7 +267,8 @@ typedef struct {
  * last_node = physical node id of the last ARay::AddNode (-1: a null node,
  * i.e. outside the top volume; -2: no node was ever added).
  * Optional history: hist_cap points per ray, hist_xyzt[(i*hist_cap+j)*4+k],
- * hist_node[i*hist_cap+j]; points past hist_cap are dropped. */
+ * hist_node[i*hist_cap+j]; points past hist_cap are dropped, and the
+ * slots past a ray's npoints hold node -3 and point (0, 0, 0, 0). */
 typedef struct {
   uint8_t* status;
   int32_t* npoints;
@@ -293,7 +294,13 @@ typedef struct {
                              (seed, ray id, draw number) */
   uint64_t ray_id_offset; /* ray id of element 0 (for sharded/batched calls) */
   int32_t precision;      /* RBG_PREC_* */
-  int32_t block_size;     /* 0: library default */
+  int32_t block_size;     /* threads per block.  FP64 tracer: up to 128
+                             (0: 128).  Mixed tracer: 128 or 256 for the
+                             lean instance (two-mirror telescopes; 0: the
+                             scene's tuned value, rbg_scene_autotune, else
+                             256); the other instances run at their own
+                             measured size (256 for segmented reflectors,
+                             128 otherwise).  Results do not depend on it. */
   /* mixed tracer: a warp refills its idle lanes with consecutive rays once
    * at least this many (1..32) are idle; 1 keeps every lane busy, 32 keeps
    * a warp's rays together (coherent paths).  0: the scene's tuned value
@@ -438,12 +445,18 @@ int rbg_multilayer_rt(rbg_scene* scene, int32_t multilayer, int32_t mode, int32_
 
 /* Autotuner of the mixed tracer (no counterpart in the reference, whose
  * thread split is fixed by the caller, src/AOpticsManager.cxx:529-567):
- * traces the DEVICE rays `in` with each candidate compaction threshold,
- * keeps the fastest in the scene for later calls that leave
- * opts->compaction at 0, and returns it in *chosen.  `out` receives the
- * trace results (identical for every threshold).  Synchronises `stream`. */
+ * traces the DEVICE rays `in` with each candidate block size (256 and 128
+ * where the scene runs the lean instance) and compaction threshold (1, 8,
+ * 16, 32), keeps the fastest pair in the scene for later calls that leave
+ * opts->block_size / opts->compaction at 0, and returns the threshold in
+ * *chosen (rbg_scene_tuning reads both).  `out` receives the trace
+ * results (identical for every candidate).  Synchronises `stream`. */
 int rbg_scene_autotune(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
                        const rbg_trace_opts* opts, void* stream, int32_t* chosen);
+/* The mixed tracer's block size and compaction threshold for the scene:
+ * rbg_scene_autotune's choice, else the defaults (block: 256 for scenes of
+ * the lean instance, else the instance's own size; threshold 32). */
+int rbg_scene_tuning(const rbg_scene* scene, int32_t* block_size, int32_t* compaction);
 
 /* Same, with HOST buffers: copies the rays in, traces, copies the results
  * out and synchronises (the call a ROOT-side AOpticsManager binding makes,

@@ -1906,6 +1906,11 @@ static void* run_job(void* arg) {
     if (o->dx) o->dx[i] = r.d[0];
     if (o->dy) o->dy[i] = r.d[1];
     if (o->dz) o->dz[i] = r.d[2];
+    /* history slots the ray did not reach: node -3, point 0 */
+    for (int k = r.npoints; k < r.hist_cap; ++k) {
+      r.hist_node[k] = -3;
+      for (int c = 0; c < 4; ++c) r.hist_xyzt[4 * k + c] = 0.0;
+    }
   }
   return NULL;
 }

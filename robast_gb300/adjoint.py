@@ -97,6 +97,8 @@ def make_trace_function():
         the recorded hit points (differentiable at reflections,
         refractions and the end point), nodes (n, history) their nodes."""
 
+        last_skipped = 0  # rays the last backward pass could not differentiate
+
         @staticmethod
         def forward(ctx, params, build: Callable, rays, precision=N.PREC_MIXED, history=8):
             man, specs = build(params.detach().cpu().numpy())
@@ -121,7 +123,7 @@ def make_trace_function():
                 z = torch.zeros(len(ctx.specs), dtype=ctx.param_dtype, device=ctx.param_device)
                 return z, None, None, None, None
             g, skipped = vjp(ctx.man, ctx.res, ctx.specs, gx, gy, lam=ctx.lam, gpts=gp)
-            ctx.skipped = skipped
+            ctx.skipped = TraceFunction.last_skipped = skipped
             return g.to(device=ctx.param_device, dtype=ctx.param_dtype), None, None, None, None
 
     return TraceFunction

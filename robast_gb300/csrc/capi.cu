@@ -181,6 +181,7 @@ extern "C" double rbg_last_kernel_ms(const rbg_scene* s) { return s && s->timing
 
 // the two tracer launchers (trace_mixed.cu, trace_fp64.cu)
 namespace rbg {
+int mixed_block_size(unsigned features);
 int launch_mixed(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o,
                  cudaStream_t st, unsigned* err_flags, unsigned long long* counter, int* launches);
 size_t ray_order_bytes(int64_t n);
@@ -246,6 +247,7 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
   int launches = 0;
   rbg_trace_opts o = *opts;
   if (o.compaction == 0) o.compaction = s->tuned_compaction;
+  if (o.block_size == 0 && o.precision == RBG_PREC_MIXED) o.block_size = s->tuned_block;
   // the take-up order needs a workspace: the caller's, else the one
   // rbg_scene_reserve sized; a batch beyond both is taken up in input order
   // (same results, nothing allocated)
@@ -276,12 +278,21 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
   return RBG_OK;
 }
 
-// The autotuner of the mixed tracer's compaction threshold: trace the
-// caller's rays once to warm up, then once per candidate threshold, timed
-// with events on the stream, and keep the fastest in the scene (used by
-// every later call whose options leave the threshold at 0).  The results
-// in `out` are those of any single trace: they do not depend on the
-// threshold.
+// The autotuner of the mixed tracer: trace the caller's rays once to warm
+// up, then once per candidate (block size, compaction threshold) -- block
+// sizes 256 and 128 for scenes the lean instance traces, the instance's
+// fixed 128 otherwise; thresholds 1, 8, 16, 32 -- timed with events on the
+// stream, and keep the fastest in the scene (used by every later call
+// whose options leave them at 0).  The results in `out` are those of any
+// single trace: they depend on neither.
+extern "C" int rbg_scene_tuning(const rbg_scene* s, int32_t* block_size, int32_t* compaction) {
+  if (!s) return RBG_ERR_ARG;
+  const int fixed = mixed_block_size(s->features);
+  if (block_size) *block_size = fixed ? fixed : (s->tuned_block ? s->tuned_block : 256);
+  if (compaction) *compaction = s->tuned_compaction ? s->tuned_compaction : 32;
+  return RBG_OK;
+}
+
 extern "C" int rbg_scene_autotune(rbg_scene* s, const rbg_rays* in, rbg_result* out, const rbg_trace_opts* opts,
                                   void* stream, int32_t* chosen) {
   if (!s || !in || !out || !opts) return RBG_ERR_ARG;
@@ -298,31 +309,41 @@ extern "C" int rbg_scene_autotune(rbg_scene* s, const rbg_rays* in, rbg_result* 
     cudaEventDestroy(e0);
     return RBG_ERR_CUDA;
   }
+  const bool lean = mixed_block_size(s->features) == 0;
+  static const int32_t kLeanBlocks[] = {256, 128};
+  const int n_blocks = lean ? 2 : 1;
   float best_ms = 0.f;
-  int32_t best = 32;
-  for (int32_t c : kCandidates) {
-    o.compaction = c;
-    float ms = 0.f;
-    if (cudaEventRecord(e0, st) != cudaSuccess) {
-      rc = RBG_ERR_CUDA;
-      break;
-    }
-    rc = rbg_trace(s, in, out, &o, stream);
-    if (rc != RBG_OK && rc != RBG_ERR_NAN && rc != RBG_ERR_CAP) break;
-    if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
-        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
-      rc = RBG_ERR_CUDA;
-      break;
-    }
-    if (c == kCandidates[0] || ms < best_ms) {
-      best_ms = ms;
-      best = c;
+  int32_t best = 32, best_block = lean ? 256 : 0;
+  bool first = true;
+  for (int b = 0; b < n_blocks && (rc == RBG_OK || rc == RBG_ERR_NAN || rc == RBG_ERR_CAP); ++b) {
+    o.block_size = lean ? kLeanBlocks[b] : 0;
+    for (int32_t c : kCandidates) {
+      o.compaction = c;
+      float ms = 0.f;
+      if (cudaEventRecord(e0, st) != cudaSuccess) {
+        rc = RBG_ERR_CUDA;
+        break;
+      }
+      rc = rbg_trace(s, in, out, &o, stream);
+      if (rc != RBG_OK && rc != RBG_ERR_NAN && rc != RBG_ERR_CAP) break;
+      if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+        rc = RBG_ERR_CUDA;
+        break;
+      }
+      if (first || ms < best_ms) {
+        best_ms = ms;
+        best = c;
+        best_block = o.block_size;
+        first = false;
+      }
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc != RBG_OK && rc != RBG_ERR_NAN && rc != RBG_ERR_CAP) return rc;
   s->tuned_compaction = best;
+  s->tuned_block = best_block;
   if (chosen) *chosen = best;
   return rc;
 }
@@ -473,6 +494,7 @@ extern "C" int rbg_trace_host(rbg_scene* s, const rbg_rays* in, rbg_result* out,
     rbg_trace_opts o = *opts;
     o.ray_id_offset = opts->ray_id_offset + (uint64_t)off;
     if (o.compaction == 0) o.compaction = s->tuned_compaction;
+    if (o.block_size == 0 && o.precision == RBG_PREC_MIXED) o.block_size = s->tuned_block;
     int nl = 0;
     if (want_ray_order(o, m)) {
       if ((rc = build_ray_order(kr, m, sl.order_ws, &kr, st))) return rc;

@@ -19,22 +19,38 @@ RBG_MIXED_LAUNCHER(launch_mixed_all)
 #undef RBG_MIXED_LAUNCHER
 
 namespace {
+// the lean instance at 256 threads per block unless the options ask for 128
+int launch_mixed_lean(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n,
+                      const rbg_trace_opts& o, cudaStream_t st, unsigned* err_flags, unsigned long long* counter) {
+  if (o.block_size == 128) return launch_mixed_impl<0u, 128>(S, in, out, n, o, st, err_flags, counter);
+  return launch_mixed_impl<0u, 256>(S, in, out, n, o, st, err_flags, counter);
+}
+
 typedef int (*MixedLauncher)(const DevScene&, const KernelRays&, const KernelOut&, int64_t, const rbg_trace_opts&,
                              cudaStream_t, unsigned*, unsigned long long*);
 struct Instance {
   unsigned features;
   MixedLauncher launch;
+  int block;  // threads per block (0: 256, or 128 when the options ask for it)
 };
 // in order of growing feature sets; the last covers every scene
 const Instance kInstances[] = {
-    {0u, launch_mixed_impl<0u>},
-    {kFeatCSG, launch_mixed_csg},
-    {kFeatCSG | kFeatRough | kFeatBVH, launch_mixed_facets},
-    {kFeatWinston | kFeatLens | kFeatBVH, launch_mixed_cones},
-    {kFeatCSG | kFeatLens | kFeatMultilayer | kFeatBVH, launch_mixed_coated},
-    {kFeatAll, launch_mixed_all},
+    {0u, launch_mixed_lean, 0},
+    {kFeatCSG, launch_mixed_csg, 128},
+    {kFeatCSG | kFeatRough | kFeatBVH, launch_mixed_facets, 256},
+    {kFeatWinston | kFeatLens | kFeatBVH, launch_mixed_cones, 128},
+    {kFeatCSG | kFeatLens | kFeatMultilayer | kFeatBVH, launch_mixed_coated, 128},
+    {kFeatAll, launch_mixed_all, 128},
 };
 }  // namespace
+
+// the block size the mixed tracer runs a scene of these features with;
+// 0 when only the lean instance's two sizes (256, 128) are open to tuning
+int mixed_block_size(unsigned features) {
+  for (const Instance& inst : kInstances)
+    if (!(features & ~inst.features)) return inst.block;
+  return 128;
+}
 
 int launch_mixed(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o,
                  cudaStream_t st, unsigned* err_flags, unsigned long long* counter, int* launches) {

@@ -20,6 +20,11 @@
 
 namespace rbg {
 
+// threads per block, by default; the lean instance comes at 128 and 256
+// (rbg_trace_opts.block_size, tuned by rbg_scene_autotune) and the
+// segmented-reflector instance at 256: there the compiler's budget of 128
+// registers per thread gives 16 resident warps per SM against 12 at 128
+// threads and 168 registers
 constexpr int kMixedBlock = 128;
 // compaction threshold when neither the options nor the scene's tuning
 // give one
@@ -28,8 +33,8 @@ constexpr int kDefaultCompaction = 32;
 // Instances: F = kFeatAll runs any scene; F = 0 (boxes and aspheric disks,
 // mirrors, obscurations and focal surfaces only, e.g. two-mirror
 // telescopes) compiles every other code path out, which frees registers.
-template <unsigned F>
-__global__ void __launch_bounds__(kMixedBlock) trace_mixed_kernel(DevScene S, KernelRays in, KernelOut out,
+template <unsigned F, int B>
+__global__ void __launch_bounds__(B) trace_mixed_kernel(DevScene S, KernelRays in, KernelOut out,
                                                                   int64_t n, int limit, int disable_fresnel,
                                                                   uint64_t seed, uint64_t id_offset,
                                                                   int refill_min, unsigned* err_flags,
@@ -100,7 +105,7 @@ __global__ void __launch_bounds__(kMixedBlock) trace_mixed_kernel(DevScene S, Ke
 // Launch over n rays on stream st: one block per resident slot of every SM
 // (occupancy queried once per instantiation), never more blocks than rays
 // need; the queue head is reset on the stream first.
-template <unsigned F>
+template <unsigned F, int B = kMixedBlock>
 int launch_mixed_impl(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n,
                       const rbg_trace_opts& o, cudaStream_t st, unsigned* err_flags, unsigned long long* counter) {
   // resident blocks per SM, queried once per instantiation and device
@@ -111,18 +116,18 @@ int launch_mixed_impl(const DevScene& S, const KernelRays& in, const KernelOut& 
   if (dev >= kMaxDev) return RBG_ERR_UNSUPPORTED;
   if (bps_of[dev] == 0) {
     int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_mixed_kernel<F>, kMixedBlock, 0) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_mixed_kernel<F, B>, B, 0) != cudaSuccess)
       return RBG_ERR_CUDA;
     bps_of[dev] = b < 1 ? 1 : b;
   }
   const int bps = bps_of[dev];
   const int sms = sm_count();
-  int64_t want = (n + kMixedBlock - 1) / kMixedBlock;
+  int64_t want = (n + B - 1) / B;
   int64_t grid = (int64_t)sms * bps;
   if (want < grid) grid = want;
   if (cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st) != cudaSuccess) return RBG_ERR_CUDA;
   const int refill = o.compaction < 1 ? kDefaultCompaction : (o.compaction > 32 ? 32 : o.compaction);
-  trace_mixed_kernel<F><<<(int)grid, kMixedBlock, 0, st>>>(S, in, out, n, o.limit, o.disable_fresnel, o.seed,
+  trace_mixed_kernel<F, B><<<(int)grid, B, 0, st>>>(S, in, out, n, o.limit, o.disable_fresnel, o.seed,
                                                           o.ray_id_offset, refill, err_flags, counter);
   if (cudaGetLastError() != cudaSuccess) return RBG_ERR_CUDA;
   return RBG_OK;

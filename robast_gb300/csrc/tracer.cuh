@@ -1353,6 +1353,13 @@ RBG_D void store_ray(const KernelOut& out, int64_t i, const Ray& r) {
   if (out.dx) out.dx[i] = r.d.x;
   if (out.dy) out.dy[i] = r.d.y;
   if (out.dz) out.dz[i] = r.d.z;
+  // history slots the ray did not reach: node -3 and point 0, as the host
+  // buffers start, so that no stale device memory reads as a point
+  for (int j = r.npoints; j < r.hist_cap; ++j) {
+    r.hist_node[j] = -3;
+    double* h = r.hist_xyzt + 4 * (size_t)j;
+    h[0] = h[1] = h[2] = h[3] = 0.0;
+  }
 }
 
 }  // namespace rbg

@@ -127,9 +127,10 @@ def trace(manager, rays, res=None, precision: Optional[int] = None, stream=None,
 
 
 def autotune(manager, rays, res=None, stream=None) -> int:
-    """Pick the mixed tracer's compaction threshold for this scene from a
-    timed trace of `rays` per candidate (rbg_scene_autotune); later traces
-    of the scene use it.  Returns the chosen threshold."""
+    """Pick the mixed tracer's block size and compaction threshold for this
+    scene from a timed trace of `rays` per candidate (rbg_scene_autotune);
+    later traces of the scene use them.  Returns the chosen threshold
+    (tuning() gives both)."""
     torch = _torch()
     scene = manager._ensure_scene()
     if res is None:
@@ -146,6 +147,15 @@ def autotune(manager, rays, res=None, stream=None) -> int:
     if status not in (N.RBG_OK, N.RBG_ERR_CAP, N.RBG_ERR_NAN):
         N.check(status, "rbg_scene_autotune")
     return int(chosen.value)
+
+
+def tuning(manager):
+    """(block size, compaction threshold) of the mixed tracer for the scene
+    (rbg_scene_tuning: the autotuner's choice, else the defaults)."""
+    scene = manager._ensure_scene()
+    b, c = C.c_int32(0), C.c_int32(0)
+    N.check(N.lib().rbg_scene_tuning(scene.handle, C.byref(b), C.byref(c)), "rbg_scene_tuning")
+    return int(b.value), int(c.value)
 
 
 def focal_moments(res, group=None, n_groups: int = 1, stream=None):

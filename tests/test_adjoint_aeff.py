@@ -86,6 +86,7 @@ def test_effective_area_gradient():
     pdev = params.to(x.device) if params.device != x.device else params
     aeff = A.sc_effective_area(pdev, pts, nodes, o, d, keep, area, ids, WIDTH)
     aeff.backward()
+    assert TF.last_skipped == 0
     g = params.grad.numpy()
     scale = np.abs(fd * h).max()
     rel = np.abs((g - fd) * h) / np.maximum(np.abs(fd * h), 1e-3 * scale)

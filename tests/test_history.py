@@ -101,6 +101,39 @@ def test_history_api_gpu_matches_oracle():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_device_history_tail_is_defined(precision):
+    """Slots past a ray's npoints read node -3 and point 0 whatever the
+    device memory held before (recycled allocations), in both tracers, and
+    the whole history equals the oracle's."""
+    import torch
+
+    from robast_gb300 import _native as N
+    from robast_gb300 import device
+
+    man, batch = configs.schwarzschild_couder(n_rays=20000, angles=(0.0, 4.0), seed=9)
+    n, cap = len(batch["x"]), 6
+    res = device.alloc_result(n, "cuda:0", cap)
+    res["hist_node"].fill_(2)  # stale ids that name a real node
+    res["hist_xyzt"].fill_(float("nan"))
+    res, st = device.trace(man, device.to_device(batch), res,
+                           precision=N.PREC_FP64 if precision == "fp64" else N.PREC_MIXED)
+    torch.cuda.synchronize()
+    assert st == 0
+    npts = res["npoints"].cpu().numpy()
+    hn = res["hist_node"].cpu().numpy()
+    hx = res["hist_xyzt"].cpu().numpy()
+    tail = np.arange(cap)[None, :] >= npts[:, None]
+    assert tail.any()
+    assert (hn[tail] == -3).all()
+    assert (hx[tail] == 0).all()
+    ost, ref = oracle_ref.trace(man, configs.to_array(batch), threads=8, history=cap)
+    assert ost == 0
+    np.testing.assert_array_equal(hn, ref["hist_node"].reshape(n, cap))
+    np.testing.assert_allclose(hx, ref["hist_xyzt"].reshape(n, cap, 4), rtol=1e-9, atol=1e-9)
+
+
+@pytest.mark.gpu
 def test_single_ray_keeps_full_history():
     man, _ = configs.paraboloid(n_rays=4, angles=(0.0,))
     # outside the 30 cm obscuration disk in front of the focal plane
