@@ -81,10 +81,14 @@ RBG_D bool surface_at(const DevScene& S, int node, d3 P, Surf& out) {
     for (int i = 0; i < 9; ++i) out.Q[i] = N.m[i];
     Asph a{SP(S, N.shape)};
     const double H2 = p.x * p.x + p.y * p.y;
-    // nearest face: dist^2 = dz^2 / q, compared as dz_a^2 q_b < dz_b^2 q_a
+    // nearest face: dist^2 = dz^2 / q, compared as dz_a^2 q_b < dz_b^2 q_a.
+    // Twin faces (the same curvature, conic and polynomial, the vertices
+    // z2 - z1 apart: a thin mirror shell) share F - z0, F' and q, so one
+    // evaluation decides between them.
     double best_dz2 = kBig * kBig, best_q = 1.0, best_dF = 0, best_rs = 0;
     int face = 0;
-    for (int f = 1; f <= 2; ++f) {
+    const bool twin = (S.aux[node].flags & RBG_AUX_ASPH_TWIN_FACES) != 0;
+    for (int f = 1; f <= (twin ? 1 : 2); ++f) {
       const double c = a.c(f), k = a.kap(f);
       const double chk = 1 - k * c * c * H2;
       if (chk <= 0) continue;
@@ -105,6 +109,13 @@ RBG_D bool surface_at(const DevScene& S, int node, d3 P, Surf& out) {
         best_dF = dF;
         best_rs = rs;
         face = f;
+      }
+      if (twin) {
+        const double dz2 = dz - (a.z(2) - a.z(1));  // p.z - F2
+        if (dz2 * dz2 < best_dz2) {
+          best_dz2 = dz2 * dz2;
+          face = 2;
+        }
       }
     }
     const double r = sqrt(H2);

@@ -35,14 +35,17 @@ namespace {
 // key bits: about 4 cells per ray, at most 2^24 cells; a quarter of the
 // bits (at most 6) number the direction cell
 constexpr int kMinKeyBits = 12, kMaxKeyBits = 24, kMaxDirBits = 6;
-// Index chunks: the rays [c 2^s, (c + 1) 2^s) are ordered among themselves
-// and chunk c's rays are taken up before chunk c + 1's (the chunk is the
-// key's top field).  The rays in flight then write their results into one
-// or two chunks' stretch of the output arrays, which stays in L2 until its
-// sectors are complete, instead of into partial sectors all over the batch.
-// s = kChunkShift, raised until there are at most kMaxChunks chunks; 0
-// orders the batch as one chunk.
-constexpr int kChunkShift = 20, kMaxChunks = 32;
+// Index chunks (off): with kChunkShift = s > 0 the rays [c 2^s, (c + 1) 2^s)
+// are ordered among themselves and chunk c's rays are taken up before chunk
+// c + 1's (the chunk is the key's top field), so the rays in flight write
+// their results into one or two chunks' stretch of the output arrays and L2
+// completes more of their 32-byte sectors before writing them back.  On
+// 1e7 Schwarzschild-Couder rays, s = 20 cut the trace kernel's DRAM traffic
+// from 600 to 390 B per ray but made it 5-7 % slower (sparser cells, less
+// coherent warps), and throughput is what the trace is bound by, so the
+// batch is ordered as one chunk.  s is raised until there are at most
+// kMaxChunks chunks.
+constexpr int kChunkShift = 0, kMaxChunks = 32;
 constexpr int64_t kMaxBuckets = int64_t(1) << 25;
 constexpr int kScanTile = 1024;
 constexpr int kThreads = 256;
