@@ -130,9 +130,17 @@ def make_trace_function():
 
 
 def rms_spot(x, y, mask):
-    """RMS spot radius of the focused rays: sqrt(<|p - <p>|^2>)."""
-    xs, ys = x[mask], y[mask]
-    return ((xs - xs.mean()) ** 2 + (ys - ys.mean()) ** 2).mean().sqrt()
+    """RMS spot radius of the rays of `mask`: sqrt(<|p - <p>|^2>).  Masked
+    arithmetic rather than boolean indexing: no host synchronisation, and
+    the backward pass is elementwise."""
+    import torch
+
+    w = mask.to(x.dtype)
+    n = w.sum()
+    xm = torch.where(mask, x, torch.zeros_like(x))
+    ym = torch.where(mask, y, torch.zeros_like(y))
+    mx, my = xm.sum() / n, ym.sum() / n
+    return ((w * ((xm - mx) ** 2 + (ym - my) ** 2)).sum() / n).sqrt()
 
 
 def r80_smooth(x, y, mask, width_frac=0.05, fraction=0.8):
