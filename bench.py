@@ -196,9 +196,12 @@ def grad_bench(batch, rays, steps, device, N, torch):
     for f in outs[1:]:
         stable &= f
 
+    # hit records: a Schwarzschild-Couder ray has at most 4 points (start,
+    # primary, secondary, focal surface); a longer path would be skipped
+    # and counted in adjoint_skipped
     def adjoint_eval():
         params = torch.tensor(p0, dtype=torch.float64, requires_grad=True)
-        x, y, f = TF.apply(params, build, rays)[:3]
+        x, y, f = TF.apply(params, build, rays, N.PREC_MIXED, 4)[:3]
         loss_of(x, y, f & stable).backward()
         return params.grad.clone()
 
@@ -226,7 +229,8 @@ def grad_bench(batch, rays, steps, device, N, torch):
     nonzero = np.abs(fd64 * h) > 1e-9 * scale
     rel_plain = np.where(nonzero, np.abs(ga - fd64) / np.where(nonzero, np.abs(fd64), 1.0), np.nan)
     return {"unit": "grad-evals/s", "params": len(p0), "rays": int(rays["x"].numel()),
-            "rays_in_loss": int(stable.sum().item()),
+            "rays_in_loss": int(stable.sum().item()), "adjoint_skipped": int(TF.last_skipped),
+            "hit_records_per_ray": 4,
             "adjoint": 1.0 / t_adj, "finite_differences_fp64": 1.0 / t_fd64,
             "finite_differences_mixed": 1.0 / t_fdmx,
             "speedup_vs_fd_fp64": t_fd64 / t_adj, "speedup_vs_fd_mixed": t_fdmx / t_adj,

@@ -33,6 +33,8 @@ namespace rbg {
 
 constexpr int kAdjMaxParams = 64;
 constexpr int kAdjMaxEvents = 24;
+constexpr int kAdjThreads = 128;            // threads per block
+constexpr int kAdjTile = 16 * kAdjThreads;  // rays per tile
 
 struct Surf {
   d3 g;         // gradient of f in the master frame
@@ -57,6 +59,113 @@ RBG_D d3 hess_vec(const Surf& sf, d3 v, d3& vl) {
   const d3 hl = mk(h[0] * vl.x + h[1] * vl.y + h[2] * vl.z, h[1] * vl.x + h[3] * vl.y + h[4] * vl.z,
                    h[2] * vl.x + h[4] * vl.y + h[5] * vl.z);
   return dir_to_master(sf.Q, hl);
+}
+
+// The nearest surface among the leaves of a TGeo primitive or composite
+// (spheres, paraboloids, cylinders, planes; each leaf's Hessian is diagonal
+// in its own frame): fills out.Q and out.h and returns the gradient in the
+// leaf's frame.  Kept out of line: its traversal stack stays out of the
+// aspheric path's registers and frame.
+__device__ __noinline__ d3 leaf_surface(const DevScene& S, const rbg_node& N, d3 p, Surf& out) {
+  d3 gl;
+  // nearest surface among the leaves (spheres, paraboloids, cylinders,
+  // planes); each leaf's Hessian is diagonal in its own frame
+  double best = kBig;
+  M12 bestM = mat_identity();
+  d3 bg = mk(0, 0, 1);
+  double bh0 = 0, bh4 = 0, bh8 = 0;
+  int stack_shape[8];
+  M12 stack_m[8];
+  int sp = 0;
+  stack_shape[sp] = N.shape;
+  stack_m[sp] = mat_identity();
+  ++sp;
+  while (sp > 0) {
+    --sp;
+    int sid = stack_shape[sp];
+    M12 M = stack_m[sp];
+    const rbg_shape_desc ss = S.shapes[sid];
+    const double* Pp = SP(S, sid);
+    if (ss.type == RBG_SHAPE_COMPOSITE) {
+      if (sp + 2 > 8) continue;
+      stack_shape[sp] = ss.left;
+      stack_m[sp] = mat_mul(M.v, Pp + RBG_COMP_ML);
+      ++sp;
+      stack_shape[sp] = ss.right;
+      stack_m[sp] = mat_mul(M.v, Pp + RBG_COMP_MR);
+      ++sp;
+      continue;
+    }
+    d3 q = to_local(M.v, p);
+    auto consider = [&](double dist, d3 g, double h0, double h4, double h8) {
+      if (dist < best) {
+        best = dist;
+        bestM = M;
+        bg = g;
+        bh0 = h0;
+        bh4 = h4;
+        bh8 = h8;
+      }
+    };
+    switch (ss.type) {
+      case RBG_SHAPE_SPHERE: {
+        double rq = sqrt(dot(q, q));
+        consider(fabs(rq - Pp[RBG_SPH_RMAX]), 2.0 * q, 2, 2, 2);
+        if (Pp[RBG_SPH_RMIN] > 0) consider(fabs(rq - Pp[RBG_SPH_RMIN]), 2.0 * q, 2, 2, 2);
+        break;
+      }
+      case RBG_SHAPE_PARABOLOID: {
+        double A = Pp[RBG_PARA_A];
+        d3 g = mk(2 * A * q.x, 2 * A * q.y, -1);
+        consider(fabs(A * (q.x * q.x + q.y * q.y) + Pp[RBG_PARA_B] - q.z) / sqrt(dot(g, g)), g, 2 * A, 2 * A, 0);
+        consider(fabs(fabs(q.z) - Pp[RBG_PARA_DZ]), mk(0, 0, 1), 0, 0, 0);
+        break;
+      }
+      case RBG_SHAPE_BOX: {
+        consider(fabs(fabs(q.x - Pp[RBG_BOX_OX]) - Pp[RBG_BOX_DX]), mk(1, 0, 0), 0, 0, 0);
+        consider(fabs(fabs(q.y - Pp[RBG_BOX_OY]) - Pp[RBG_BOX_DY]), mk(0, 1, 0), 0, 0, 0);
+        consider(fabs(fabs(q.z - Pp[RBG_BOX_OZ]) - Pp[RBG_BOX_DZ]), mk(0, 0, 1), 0, 0, 0);
+        break;
+      }
+      case RBG_SHAPE_TUBE: {
+        double rq = sqrt(q.x * q.x + q.y * q.y);
+        consider(fabs(rq - Pp[RBG_TUBE_RMAX]), mk(2 * q.x, 2 * q.y, 0), 2, 2, 0);
+        if (Pp[RBG_TUBE_RMIN] > 0) consider(fabs(rq - Pp[RBG_TUBE_RMIN]), mk(2 * q.x, 2 * q.y, 0), 2, 2, 0);
+        consider(fabs(fabs(q.z) - Pp[RBG_TUBE_DZ]), mk(0, 0, 1), 0, 0, 0);
+        break;
+      }
+      case RBG_SHAPE_PGON: {
+        // flat faces only (the prism sides and the section planes)
+        const int ned = (int)Pp[2], nz = (int)Pp[3];
+        const double* Z = Pp + 4;
+        for (int k = 0; k < nz; ++k) consider(fabs(q.z - Z[k]), mk(0, 0, 1), 0, 0, 0);
+        const double* RMAX = Z + 2 * nz;
+        for (int k = 0; k + 1 < nz; ++k) {
+          double h = Z[k + 1] - Z[k];
+          if (h <= 0) continue;
+          double s = (RMAX[k + 1] - RMAX[k]) / h;
+          for (int e = 0; e < ned; ++e) {
+            double pe = (Pp[0] + (e + 0.5) * (Pp[1] / ned)) * kD2R;
+            d3 nn = mk(cos(pe), sin(pe), -s);
+            double v = dot(nn, q) - (RMAX[k] - s * Z[k]);
+            consider(fabs(v) / sqrt(dot(nn, nn)), nn, 0, 0, 0);
+          }
+        }
+        break;
+      }
+      default:
+        break;
+    }
+  }
+  // the leaf's frame in the master frame: Q = R_node R_leaf
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      out.Q[i * 3 + j] = N.m[i * 3] * bestM.v[j] + N.m[i * 3 + 1] * bestM.v[3 + j] + N.m[i * 3 + 2] * bestM.v[6 + j];
+  out.h[0] = bh0;
+  out.h[3] = bh4;
+  out.h[5] = bh8;
+  gl = bg;
+  return gl;
 }
 
 // Implicit function of the surface of node `node` nearest to the master
@@ -92,7 +201,9 @@ RBG_D bool surface_at(const DevScene& S, int node, d3 P, Surf& out) {
       const double c = a.c(f), k = a.kap(f);
       const double chk = 1 - k * c * c * H2;
       if (chk <= 0) continue;
-      const double s = sqrt(chk), rs = 1.0 / s;
+      const double s = sqrt(chk);
+      const double inv = 1.0 / (s * (1 + s));  // 1/s = (1 + s) inv, 1/(1 + s) = s inv
+      const double rs = (1 + s) * inv;
       const int n = a.npol(f);
       const double* K = a.K(f);
       double pp = 0, dp = 0;
@@ -100,7 +211,7 @@ RBG_D bool surface_at(const DevScene& S, int node, d3 P, Surf& out) {
         pp = (pp + K[j]) * H2;
         dp = dp * H2 + (j + 1) * K[j];
       }
-      const double F = a.z(f) + H2 * c / (1 + s) + pp;
+      const double F = a.z(f) + H2 * c * (s * inv) + pp;
       const double dF = 0.5 * c * rs + dp;
       const double dz = p.z - F, q = 1 + 4 * H2 * dF * dF;
       if (dz * dz * best_q < best_dz2 * q) {
@@ -147,103 +258,7 @@ RBG_D bool surface_at(const DevScene& S, int node, d3 P, Surf& out) {
     }
   } else if (sh.type == RBG_SHAPE_COMPOSITE || sh.type == RBG_SHAPE_SPHERE || sh.type == RBG_SHAPE_BOX ||
              sh.type == RBG_SHAPE_TUBE || sh.type == RBG_SHAPE_PARABOLOID || sh.type == RBG_SHAPE_PGON) {
-    // nearest surface among the leaves (spheres, paraboloids, cylinders,
-    // planes); each leaf's Hessian is diagonal in its own frame
-    double best = kBig;
-    M12 bestM = mat_identity();
-    d3 bg = mk(0, 0, 1);
-    double bh0 = 0, bh4 = 0, bh8 = 0;
-    int stack_shape[8];
-    M12 stack_m[8];
-    int sp = 0;
-    stack_shape[sp] = N.shape;
-    stack_m[sp] = mat_identity();
-    ++sp;
-    while (sp > 0) {
-      --sp;
-      int sid = stack_shape[sp];
-      M12 M = stack_m[sp];
-      const rbg_shape_desc ss = S.shapes[sid];
-      const double* Pp = SP(S, sid);
-      if (ss.type == RBG_SHAPE_COMPOSITE) {
-        if (sp + 2 > 8) continue;
-        stack_shape[sp] = ss.left;
-        stack_m[sp] = mat_mul(M.v, Pp + RBG_COMP_ML);
-        ++sp;
-        stack_shape[sp] = ss.right;
-        stack_m[sp] = mat_mul(M.v, Pp + RBG_COMP_MR);
-        ++sp;
-        continue;
-      }
-      d3 q = to_local(M.v, p);
-      auto consider = [&](double dist, d3 g, double h0, double h4, double h8) {
-        if (dist < best) {
-          best = dist;
-          bestM = M;
-          bg = g;
-          bh0 = h0;
-          bh4 = h4;
-          bh8 = h8;
-        }
-      };
-      switch (ss.type) {
-        case RBG_SHAPE_SPHERE: {
-          double rq = sqrt(dot(q, q));
-          consider(fabs(rq - Pp[RBG_SPH_RMAX]), 2.0 * q, 2, 2, 2);
-          if (Pp[RBG_SPH_RMIN] > 0) consider(fabs(rq - Pp[RBG_SPH_RMIN]), 2.0 * q, 2, 2, 2);
-          break;
-        }
-        case RBG_SHAPE_PARABOLOID: {
-          double A = Pp[RBG_PARA_A];
-          d3 g = mk(2 * A * q.x, 2 * A * q.y, -1);
-          consider(fabs(A * (q.x * q.x + q.y * q.y) + Pp[RBG_PARA_B] - q.z) / sqrt(dot(g, g)), g, 2 * A, 2 * A, 0);
-          consider(fabs(fabs(q.z) - Pp[RBG_PARA_DZ]), mk(0, 0, 1), 0, 0, 0);
-          break;
-        }
-        case RBG_SHAPE_BOX: {
-          consider(fabs(fabs(q.x - Pp[RBG_BOX_OX]) - Pp[RBG_BOX_DX]), mk(1, 0, 0), 0, 0, 0);
-          consider(fabs(fabs(q.y - Pp[RBG_BOX_OY]) - Pp[RBG_BOX_DY]), mk(0, 1, 0), 0, 0, 0);
-          consider(fabs(fabs(q.z - Pp[RBG_BOX_OZ]) - Pp[RBG_BOX_DZ]), mk(0, 0, 1), 0, 0, 0);
-          break;
-        }
-        case RBG_SHAPE_TUBE: {
-          double rq = sqrt(q.x * q.x + q.y * q.y);
-          consider(fabs(rq - Pp[RBG_TUBE_RMAX]), mk(2 * q.x, 2 * q.y, 0), 2, 2, 0);
-          if (Pp[RBG_TUBE_RMIN] > 0) consider(fabs(rq - Pp[RBG_TUBE_RMIN]), mk(2 * q.x, 2 * q.y, 0), 2, 2, 0);
-          consider(fabs(fabs(q.z) - Pp[RBG_TUBE_DZ]), mk(0, 0, 1), 0, 0, 0);
-          break;
-        }
-        case RBG_SHAPE_PGON: {
-          // flat faces only (the prism sides and the section planes)
-          const int ned = (int)Pp[2], nz = (int)Pp[3];
-          const double* Z = Pp + 4;
-          for (int k = 0; k < nz; ++k) consider(fabs(q.z - Z[k]), mk(0, 0, 1), 0, 0, 0);
-          const double* RMAX = Z + 2 * nz;
-          for (int k = 0; k + 1 < nz; ++k) {
-            double h = Z[k + 1] - Z[k];
-            if (h <= 0) continue;
-            double s = (RMAX[k + 1] - RMAX[k]) / h;
-            for (int e = 0; e < ned; ++e) {
-              double pe = (Pp[0] + (e + 0.5) * (Pp[1] / ned)) * kD2R;
-              d3 nn = mk(cos(pe), sin(pe), -s);
-              double v = dot(nn, q) - (RMAX[k] - s * Z[k]);
-              consider(fabs(v) / sqrt(dot(nn, nn)), nn, 0, 0, 0);
-            }
-          }
-          break;
-        }
-        default:
-          break;
-      }
-    }
-    // the leaf's frame in the master frame: Q = R_node R_leaf
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j)
-        out.Q[i * 3 + j] = N.m[i * 3] * bestM.v[j] + N.m[i * 3 + 1] * bestM.v[3 + j] + N.m[i * 3 + 2] * bestM.v[6 + j];
-    out.h[0] = bh0;
-    out.h[3] = bh4;
-    out.h[5] = bh8;
-    gl = bg;
+    gl = leaf_surface(S, N, p, out);
   } else {
     return false;
   }
@@ -290,10 +305,27 @@ enum { kEvStart = 0, kEvReflect = 1, kEvRefract = 2, kEvFinal = 3 };
 //   * rotation about axis a through pivot o:  df = (g x r)_a, dg = e_a x g +
 //     H (r x e_a), r = P - o, so the term is (g x gbar)_a + (w x r)_a.
 // moves_with is evaluated once per distinct parameter node.
+// coefficient terms H2^j (-2 (j + 1) u - c H2) tabulated for j < kCoefTab
+// once per event, when a parameter needs one
+constexpr int kCoefTab = 8;
+
 template <int MAXP>
 RBG_D void add_terms(const DevScene& S, const rbg_adjoint_param* params, int n_params, int node, d3 P, const Surf& sf,
                      double u, d3 w, d3 gxgbar, double c, double* acc) {
   int last_node = -1, last_moves = 0;
+  bool coef = false;
+  if (sf.face != 0)
+    for (int k = 0; k < n_params; ++k) coef |= params[k].kind == RBG_ADJ_ASPH_COEF && params[k].node == node;
+  double tab[kCoefTab];
+  if (coef) {
+    const double cH2 = c * sf.H2;
+    double pw = 1.0;
+#pragma unroll
+    for (int j = 0; j < kCoefTab; ++j) {
+      tab[j] = pw * (-2.0 * (j + 1) * u - cH2);
+      pw *= sf.H2;
+    }
+  }
 #pragma unroll
   for (int k = 0; k < MAXP; ++k) {
     if (k >= n_params) break;
@@ -301,10 +333,17 @@ RBG_D void add_terms(const DevScene& S, const rbg_adjoint_param* params, int n_p
     const int a = p.index;
     if (p.kind == RBG_ADJ_ASPH_COEF) {
       if (p.node != node || sf.face == 0 || !(p.faces & (1 << (sf.face - 1))) || a < 0 || a >= sf.npol) continue;
-      double hj = 1, b = sf.H2;  // H2^j by squaring
-      for (int e = a; e; e >>= 1, b *= b)
-        if (e & 1) hj *= b;
-      acc[k] += hj * (-2.0 * (a + 1) * u - c * sf.H2);
+      double term = tab[0];
+      if (a < kCoefTab) {
+#pragma unroll
+        for (int j = 1; j < kCoefTab; ++j) term = a == j ? tab[j] : term;
+      } else {
+        double hj = 1, b = sf.H2;  // H2^j by squaring
+        for (int e = a; e; e >>= 1, b *= b)
+          if (e & 1) hj *= b;
+        term = hj * (-2.0 * (a + 1) * u - c * sf.H2);
+      }
+      acc[k] += term;
       continue;
     }
     if (p.node != last_node) {
@@ -322,7 +361,7 @@ RBG_D void add_terms(const DevScene& S, const rbg_adjoint_param* params, int n_p
 }
 
 template <int MAXP>
-__global__ void __launch_bounds__(128) adjoint_kernel(DevScene S, int64_t n, const uint8_t* status, const int32_t* npoints,
+__global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(DevScene S, int64_t n, const uint8_t* status, const int32_t* npoints,
                                int32_t hist_cap, const double* hist_xyzt, const int32_t* hist_node,
                                const double* lambda, const double* gx, const double* gy, const double* gz,
                                const double* gpts, int n_params, const __grid_constant__ AdjParams params_v, double* out,
@@ -334,176 +373,202 @@ __global__ void __launch_bounds__(128) adjoint_kernel(DevScene S, int64_t n, con
 #pragma unroll
   for (int k = 0; k < MAXP; ++k) acc[k] = 0;
   unsigned long long nskip = 0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    d3 Pbar = mk(gx ? gx[i] : 0.0, gy ? gy[i] : 0.0, gz ? gz[i] : 0.0);
-    const int np = npoints[i];
-    // cotangents of the recorded points (hit records), when given
-    const double* gp = gpts ? gpts + (size_t)i * hist_cap * 3 : nullptr;
-    auto gpt = [&](int j) { return gp ? mk(gp[3 * j], gp[3 * j + 1], gp[3 * j + 2]) : mk(0, 0, 0); };
-    bool any = !(Pbar.x == 0 && Pbar.y == 0 && Pbar.z == 0);
-    for (int j = 0; gp && !any && j < np && j < hist_cap; ++j) {
-      const d3 q = gpt(j);
-      any = q.x != 0 || q.y != 0 || q.z != 0;
+  // Rays are taken in tiles of kAdjTile: the rays of a tile with a
+  // non-zero cotangent are listed in shared memory first (a warp ballot and
+  // one shared atomic per warp), then the block's threads walk that list,
+  // so no lane idles on a ray that contributes nothing (rays that missed
+  // the focal surface, rays outside the loss)
+  __shared__ int32_t tile[kAdjTile];
+  __shared__ int tile_n;
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * kAdjTile; base < n; base += (int64_t)gridDim.x * kAdjTile) {
+    if (threadIdx.x == 0) tile_n = 0;
+    __syncthreads();
+    for (int k = threadIdx.x; k < kAdjTile; k += blockDim.x) {
+      const int64_t i = base + k;
+      bool act = false;
+      if (i < n) {
+        bool any = (gx && gx[i] != 0) || (gy && gy[i] != 0) || (gz && gz[i] != 0);
+        const int np = npoints[i];
+        // cotangents of the recorded points (hit records), when given
+        const double* gp = gpts ? gpts + (size_t)i * hist_cap * 3 : nullptr;
+        for (int j = 0; gp && !any && j < np && j < hist_cap; ++j)
+          any = gp[3 * j] != 0 || gp[3 * j + 1] != 0 || gp[3 * j + 2] != 0;
+        if (any) {
+          if (np < 2 || np > hist_cap) ++nskip;
+          else act = true;
+        }
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, act);
+      int slot = 0;
+      if (lane == 0 && m) slot = atomicAdd(&tile_n, __popc(m));
+      slot = __shfl_sync(0xffffffffu, slot, 0);
+      if (act) tile[slot + __popc(m & ((1u << lane) - 1u))] = k;
     }
-    if (!any) continue;
-    if (np < 2 || np > hist_cap) {
-      ++nskip;
-      continue;
-    }
-    const double* h = hist_xyzt + (size_t)i * hist_cap * 4;
-    const int32_t* hn = hist_node + (size_t)i * hist_cap;
-    auto pt = [&](int j) { return mk(h[4 * j], h[4 * j + 1], h[4 * j + 2]); };
-    const double lam = lambda ? lambda[i] : 0.0;
-    const bool lenses = S.features & kFeatLens;
-    // events: the start, every reflection and refraction, the final point.
-    // Media (for refractions) are located at the midpoints of the recorded
-    // segments; a point between two media of equal index is straight.
-    int ev[kAdjMaxEvents], evk[kAdjMaxEvents], evs[kAdjMaxEvents];
-    double eta[kAdjMaxEvents];
-    int ne = 0;
-    bool ok = true;
-    ev[ne] = 0;
-    evk[ne] = kEvStart;
-    evs[ne] = -1;
-    eta[ne] = 1.0;
-    ++ne;
-    int m_prev = lenses ? locate_from_top(S, 0.5 * (pt(0) + pt(1))) : -1;
-    for (int j = 1; j < np - 1 && ok; ++j) {
-      const int k = hn[j];
-      const int kind = k >= 0 ? S.nodes[k].kind : kNull;
-      int m_next = -1;
-      if (lenses) m_next = locate_from_top(S, 0.5 * (pt(j) + pt(j + 1)));
-      int ekind = -1, snode = -1;
-      double e_eta = 1.0;
-      if (kind == RBG_KIND_MIRROR) {
-        ekind = kEvReflect;
-        snode = k;
-      } else if (lenses) {
-        const double n_in = medium_n(S, m_prev, lam), n_out = medium_n(S, m_next, lam);
-        const d3 din = normalized(pt(j) - pt(j - 1)), dout = normalized(pt(j + 1) - pt(j));
-        if (m_prev == m_next && dot(din - dout, din - dout) > 1e-18) {
-          // Fresnel or total internal reflection at a lens face
+    __syncthreads();
+    const int count = tile_n;
+    for (int t = threadIdx.x; t < count; t += blockDim.x) {
+      const int64_t i = base + tile[t];
+      d3 Pbar = mk(gx ? gx[i] : 0.0, gy ? gy[i] : 0.0, gz ? gz[i] : 0.0);
+      const int np = npoints[i];
+      const double* gp = gpts ? gpts + (size_t)i * hist_cap * 3 : nullptr;
+      auto gpt = [&](int j) { return gp ? mk(gp[3 * j], gp[3 * j + 1], gp[3 * j + 2]) : mk(0, 0, 0); };
+      const double* h = hist_xyzt + (size_t)i * hist_cap * 4;
+      const int32_t* hn = hist_node + (size_t)i * hist_cap;
+      auto pt = [&](int j) { return mk(h[4 * j], h[4 * j + 1], h[4 * j + 2]); };
+      const double lam = lambda ? lambda[i] : 0.0;
+      const bool lenses = S.features & kFeatLens;
+      // events: the start, every reflection and refraction, the final point.
+      // Media (for refractions) are located at the midpoints of the recorded
+      // segments; a point between two media of equal index is straight.
+      int ev[kAdjMaxEvents], evk[kAdjMaxEvents], evs[kAdjMaxEvents];
+      double eta[kAdjMaxEvents];
+      int ne = 0;
+      bool ok = true;
+      ev[ne] = 0;
+      evk[ne] = kEvStart;
+      evs[ne] = -1;
+      eta[ne] = 1.0;
+      ++ne;
+      int m_prev = lenses ? locate_from_top(S, 0.5 * (pt(0) + pt(1))) : -1;
+      for (int j = 1; j < np - 1 && ok; ++j) {
+        const int k = hn[j];
+        const int kind = k >= 0 ? S.nodes[k].kind : kNull;
+        int m_next = -1;
+        if (lenses) m_next = locate_from_top(S, 0.5 * (pt(j) + pt(j + 1)));
+        int ekind = -1, snode = -1;
+        double e_eta = 1.0;
+        if (kind == RBG_KIND_MIRROR) {
           ekind = kEvReflect;
-          snode = (m_prev >= 0 && S.nodes[m_prev].kind == RBG_KIND_LENS) ? m_prev : k;
-        } else if (n_in != n_out) {
-          ekind = kEvRefract;
-          e_eta = n_in / n_out;
-          // the crossed surface belongs to the node entered, or to the one left
-          snode = is_within(S, m_prev, m_next) && m_next != m_prev ? m_next : m_prev;
+          snode = k;
+        } else if (lenses) {
+          const double n_in = medium_n(S, m_prev, lam), n_out = medium_n(S, m_next, lam);
+          const d3 din = normalized(pt(j) - pt(j - 1)), dout = normalized(pt(j + 1) - pt(j));
+          if (m_prev == m_next && dot(din - dout, din - dout) > 1e-18) {
+            // Fresnel or total internal reflection at a lens face
+            ekind = kEvReflect;
+            snode = (m_prev >= 0 && S.nodes[m_prev].kind == RBG_KIND_LENS) ? m_prev : k;
+          } else if (n_in != n_out) {
+            ekind = kEvRefract;
+            e_eta = n_in / n_out;
+            // the crossed surface belongs to the node entered, or to the one left
+            snode = is_within(S, m_prev, m_next) && m_next != m_prev ? m_next : m_prev;
+          }
         }
+        if (ekind >= 0) {
+          if (ne >= kAdjMaxEvents - 1 || snode < 0) {
+            ok = false;
+            break;
+          }
+          ev[ne] = j;
+          evk[ne] = ekind;
+          evs[ne] = snode;
+          eta[ne] = e_eta;
+          ++ne;
+        }
+        m_prev = m_next;
       }
-      if (ekind >= 0) {
-        if (ne >= kAdjMaxEvents - 1 || snode < 0) {
+      if (!ok) {
+        ++nskip;
+        continue;
+      }
+      ev[ne] = np - 1;
+      evk[ne] = kEvFinal;
+      ++ne;
+      // final point: intersection with the surface of the entered node (or
+      // the top volume when the ray left it)
+      int m = ne - 1;
+      Pbar = Pbar + gpt(ev[m]);
+      d3 Pm = pt(ev[m]);
+      d3 Pprev = pt(ev[m - 1]);
+      d3 dseg = normalized(Pm - Pprev);
+      double tseg = sqrt(dot(Pm - Pprev, Pm - Pprev));
+      int fnode = hn[ev[m]];
+      if (fnode < 0) fnode = 0;
+      Surf sf;
+      if (!surface_at(S, fnode, Pm, sf)) {
+        ++nskip;
+        continue;
+      }
+      double gd = dot(sf.g, dseg);
+      if (gd == 0) {
+        ++nskip;
+        continue;
+      }
+      const double cf = -dot(Pbar, dseg) / gd;
+      // at the final point gbar = 0: only the value terms c df remain
+      add_terms<MAXP>(S, params, n_params, fnode, Pm, sf, 0.0, cf * sf.g, mk(0, 0, 0), cf, acc);
+      d3 obar = Pbar + cf * sf.g;
+      d3 dbar = tseg * obar;
+      for (int e = m - 1; e >= 1; --e) {
+        const d3 Prec = pt(ev[e]);
+        const d3 Pin = pt(ev[e - 1]);
+        const d3 seg = Prec - Pin;
+        const double L = sqrt(dot(seg, seg));
+        if (!(L > 0)) {
           ok = false;
           break;
         }
-        ev[ne] = j;
-        evk[ne] = ekind;
-        evs[ne] = snode;
-        eta[ne] = e_eta;
-        ++ne;
-      }
-      m_prev = m_next;
-    }
-    if (!ok) {
-      ++nskip;
-      continue;
-    }
-    ev[ne] = np - 1;
-    evk[ne] = kEvFinal;
-    ++ne;
-    // final point: intersection with the surface of the entered node (or
-    // the top volume when the ray left it)
-    int m = ne - 1;
-    Pbar = Pbar + gpt(ev[m]);
-    d3 Pm = pt(ev[m]);
-    d3 Pprev = pt(ev[m - 1]);
-    d3 dseg = normalized(Pm - Pprev);
-    double tseg = sqrt(dot(Pm - Pprev, Pm - Pprev));
-    int fnode = hn[ev[m]];
-    if (fnode < 0) fnode = 0;
-    Surf sf;
-    if (!surface_at(S, fnode, Pm, sf)) {
-      ++nskip;
-      continue;
-    }
-    double gd = dot(sf.g, dseg);
-    if (gd == 0) {
-      ++nskip;
-      continue;
-    }
-    const double cf = -dot(Pbar, dseg) / gd;
-    // at the final point gbar = 0: only the value terms c df remain
-    add_terms<MAXP>(S, params, n_params, fnode, Pm, sf, 0.0, cf * sf.g, mk(0, 0, 0), cf, acc);
-    d3 obar = Pbar + cf * sf.g;
-    d3 dbar = tseg * obar;
-    for (int e = m - 1; e >= 1; --e) {
-      const d3 Prec = pt(ev[e]);
-      const d3 Pin = pt(ev[e - 1]);
-      const d3 seg = Prec - Pin;
-      const double L = sqrt(dot(seg, seg));
-      if (!(L > 0)) {
-        ok = false;
-        break;
-      }
-      const d3 din = (1.0 / L) * seg;
-      const bool refl = evk[e] == kEvReflect;
-      // recorded point: reflection = hit - eps d_in (the step back),
-      // refraction = hit + push d_in (the boundary push)
-      const double off = refl ? -RBG_REFLECT_BACKSTEP : RBG_BOUNDARY_PUSH;
-      const d3 Phit = Prec - off * din;
-      const double t_in = L - off;
-      const int node = evs[e];
-      if (!surface_at(S, node, Phit, sf)) {
-        ok = false;
-        break;
-      }
-      const double rgn = rsqrt(dot(sf.g, sf.g));  // 1 / |g|
-      // o_next = the recorded point = Phit + off d_in, with its own cotangent
-      const d3 Precbar = obar + gpt(ev[e]);
-      d3 Phbar = Precbar;
-      d3 dinbar = off * Precbar;
-      d3 gbar;
-      if (refl) {
-        const d3 nrm = rgn * sf.g;
-        // d_out = din - 2 (din.n) n
-        const double dn = dot(din, nrm), ndb = dot(nrm, dbar);
-        dinbar = dinbar + dbar - (2 * ndb) * nrm;
-        const d3 nbar = (-2.0) * (dn * dbar + ndb * din);
-        gbar = rgn * (nbar - dot(nrm, nbar) * nrm);
-      } else {
-        // d_out = eta din + (c2 - eta c1) nh, nh = s g / |g| oriented along
-        // din, c1 = din.nh, c2 = sqrt(1 - eta^2 (1 - c1^2))
-        const double sgn = dot(sf.g, din) < 0 ? -1.0 : 1.0;
-        const d3 nh = (sgn * rgn) * sf.g;
-        const double et = eta[e];
-        const double c1 = dot(din, nh);
-        const double s2 = 1 - et * et * (1 - c1 * c1);
-        if (!(s2 > 0)) {
+        const d3 din = (1.0 / L) * seg;
+        const bool refl = evk[e] == kEvReflect;
+        // recorded point: reflection = hit - eps d_in (the step back),
+        // refraction = hit + push d_in (the boundary push)
+        const double off = refl ? -RBG_REFLECT_BACKSTEP : RBG_BOUNDARY_PUSH;
+        const d3 Phit = Prec - off * din;
+        const double t_in = L - off;
+        const int node = evs[e];
+        if (!surface_at(S, node, Phit, sf)) {
           ok = false;
           break;
         }
-        const double c2 = sqrt(s2);
-        const double kk = et * et * c1 / c2 - et, sd = dot(nh, dbar);
-        dinbar = dinbar + et * dbar + (kk * sd) * nh;
-        const d3 nhbar = (c2 - et * c1) * dbar + (kk * sd) * din;
-        gbar = (sgn * rgn) * (nhbar - dot(nh, nhbar) * nh);
+        const double rgn = rsqrt(dot(sf.g, sf.g));  // 1 / |g|
+        // o_next = the recorded point = Phit + off d_in, with its own cotangent
+        const d3 Precbar = obar + gpt(ev[e]);
+        d3 Phbar = Precbar;
+        d3 dinbar = off * Precbar;
+        d3 gbar;
+        if (refl) {
+          const d3 nrm = rgn * sf.g;
+          // d_out = din - 2 (din.n) n
+          const double dn = dot(din, nrm), ndb = dot(nrm, dbar);
+          dinbar = dinbar + dbar - (2 * ndb) * nrm;
+          const d3 nbar = (-2.0) * (dn * dbar + ndb * din);
+          gbar = rgn * (nbar - dot(nrm, nbar) * nrm);
+        } else {
+          // d_out = eta din + (c2 - eta c1) nh, nh = s g / |g| oriented along
+          // din, c1 = din.nh, c2 = sqrt(1 - eta^2 (1 - c1^2))
+          const double sgn = dot(sf.g, din) < 0 ? -1.0 : 1.0;
+          const d3 nh = (sgn * rgn) * sf.g;
+          const double et = eta[e];
+          const double c1 = dot(din, nh);
+          const double s2 = 1 - et * et * (1 - c1 * c1);
+          if (!(s2 > 0)) {
+            ok = false;
+            break;
+          }
+          const double c2 = sqrt(s2);
+          const double kk = et * et * c1 / c2 - et, sd = dot(nh, dbar);
+          dinbar = dinbar + et * dbar + (kk * sd) * nh;
+          const d3 nhbar = (c2 - et * c1) * dbar + (kk * sd) * din;
+          gbar = (sgn * rgn) * (nhbar - dot(nh, nhbar) * nh);
+        }
+        d3 gbl;  // gbar in the surface's frame
+        const d3 Hgbar = hess_vec(sf, gbar, gbl);
+        Phbar = Phbar + Hgbar;
+        const double gdi = dot(sf.g, din);
+        if (gdi == 0) {
+          ok = false;
+          break;
+        }
+        const double c = -dot(Phbar, din) / gdi;
+        add_terms<MAXP>(S, params, n_params, node, Phit, sf, gbl.x * sf.x + gbl.y * sf.y, Hgbar + c * sf.g,
+                        cross(sf.g, gbar), c, acc);
+        obar = Phbar + c * sf.g;
+        dbar = dinbar + t_in * obar;
       }
-      d3 gbl;  // gbar in the surface's frame
-      const d3 Hgbar = hess_vec(sf, gbar, gbl);
-      Phbar = Phbar + Hgbar;
-      const double gdi = dot(sf.g, din);
-      if (gdi == 0) {
-        ok = false;
-        break;
-      }
-      const double c = -dot(Phbar, din) / gdi;
-      add_terms<MAXP>(S, params, n_params, node, Phit, sf, gbl.x * sf.x + gbl.y * sf.y, Hgbar + c * sf.g,
-                      cross(sf.g, gbar), c, acc);
-      obar = Phbar + c * sf.g;
-      dbar = dinbar + t_in * obar;
+      if (!ok) ++nskip;
     }
-    if (!ok) ++nskip;
+    __syncthreads();  // the tile list is rewritten next
   }
   // warp reduction, one atomic per warp and parameter
 #pragma unroll
@@ -551,8 +616,8 @@ extern "C" int rbg_trace_adjoint(rbg_scene* s, int64_t n, const rbg_result* fwd,
   for (int k = 0; k < n_params; ++k) pv.p[k] = params[k];
   unsigned long long* dskip = s->dev->adj_skip;
   if (cudaMemsetAsync(dskip, 0, sizeof(unsigned long long), st) != cudaSuccess) return RBG_ERR_CUDA;
-  int block = 128;
-  int blocks = (int)std::min<int64_t>((n + block - 1) / block, (int64_t)sm_count() * 8);
+  const int block = kAdjThreads;
+  const int blocks = (int)std::min<int64_t>((n + kAdjTile - 1) / kAdjTile, (int64_t)sm_count() * 8);
   // a small parameter list keeps its accumulators in registers
   if (n_params <= 24)
     adjoint_kernel<24><<<blocks, block, 0, st>>>(s->dev->view, n, fwd->status, fwd->npoints, fwd->hist_cap,

@@ -43,13 +43,41 @@ __global__ void focal_moments_kernel(int64_t n, const uint8_t* status, const dou
   if (shared)
     for (int k = threadIdx.x; k < n_groups * 6; k += blockDim.x) acc[k] = 0;
   __syncthreads();
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    if (status[i] != RBG_FOCUS) continue;
-    int g = group ? group[i] : 0;
-    if (g < 0 || g >= n_groups) continue;
-    double v[6] = {1.0, x[i], y[i], x[i] * x[i], y[i] * y[i], t ? t[i] : 0.0};
-    double* dst = shared ? acc + g * 6 : sums + g * 6;
-    for (int k = 0; k < 6; ++k) atomicAdd(dst + k, v[k]);
+  // a warp whose rays all belong to one group (batches are laid out group
+  // by group) sums its values by shuffles and adds once; other warps add
+  // per ray.  Rays that are not focused add zeros to their group.
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    int g = -1;
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    if (i < n) {
+      g = group ? group[i] : 0;
+      if (g < 0 || g >= n_groups) g = -1;
+      if (g >= 0 && status[i] == RBG_FOCUS) {
+        v[0] = 1.0;
+        v[1] = x[i];
+        v[2] = y[i];
+        v[3] = x[i] * x[i];
+        v[4] = y[i] * y[i];
+        v[5] = t ? t[i] : 0.0;
+      }
+    }
+    const unsigned peers = __match_any_sync(FULL, g);
+    if (peers == FULL) {
+      if (g >= 0) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+          for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_xor_sync(FULL, v[k], off);
+        double* dst = shared ? acc + g * 6 : sums + g * 6;
+        if (lane == 0 && v[0] != 0)
+          for (int k = 0; k < 6; ++k) atomicAdd(dst + k, v[k]);
+      }
+    } else if (g >= 0 && v[0] != 0) {
+      double* dst = shared ? acc + g * 6 : sums + g * 6;
+      for (int k = 0; k < 6; ++k) atomicAdd(dst + k, v[k]);
+    }
   }
   __syncthreads();
   if (shared)
