@@ -166,7 +166,7 @@ def grad_bench(batch, rays, steps, device, N, torch):
     TF = A.make_trace_function()
 
     def loss_of(x, y, keep):
-        return sum(A.rms_spot(x, y, keep & (group == g)) for g in range(n_groups))
+        return A.rms_spot_groups(x, y, keep, group, n_groups)
 
     h = A.fd_steps(p0)
     res = device.alloc_result(rays["x"].numel(), rays["x"].device)

@@ -143,6 +143,45 @@ def rms_spot(x, y, mask):
     return ((w * ((xm - mx) ** 2 + (ym - my) ** 2)).sum() / n).sqrt()
 
 
+def rms_spot_groups(x, y, mask, group, n_groups):
+    """Sum over groups g < n_groups of the RMS spot radius of the rays of
+    `mask` in group g (each group's radius as rms_spot).  Two passes of
+    rbg_focal_moments: every group's count and centroid, then the sums of
+    squares about the centroids (no cancellation between <x^2> and
+    <x>^2); the backward pass is one elementwise expression,
+    d r_g / d x_i = (x_i - <x>_g) / (n_g r_g)."""
+    import torch
+
+    from . import device
+
+    class _RmsGroups(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, xx, yy):
+            status = torch.where(mask, torch.full_like(mask, N.RBG_FOCUS, dtype=torch.uint8),
+                                 torch.zeros_like(mask, dtype=torch.uint8))
+            m = device.focal_moments({"status": status, "x": xx, "y": yy, "t": None}, group, n_groups)
+            n = m[:, 0].clamp(min=1.0)
+            g = group.long()
+            mx, my = m[:, 1] / n, m[:, 2] / n
+            d = device.focal_moments({"status": status, "x": xx - mx[g], "y": yy - my[g], "t": None}, group,
+                                     n_groups)
+            ex, ey = d[:, 1] / n, d[:, 2] / n  # the first pass's centroid error
+            mx, my = mx + ex, my + ey
+            r = ((d[:, 3] + d[:, 4]) / n - ex * ex - ey * ey).clamp(min=0.0).sqrt()
+            ctx.save_for_backward(xx, yy, mx, my, n, r)
+            return r[m[:, 0] > 0].sum()
+
+        @staticmethod
+        def backward(ctx, go):
+            xx, yy, mx, my, n, r = ctx.saved_tensors
+            g = group.long()
+            k = torch.where(r > 0, go / (n * r), torch.zeros_like(r))
+            kg = torch.where(mask, k[g], torch.zeros_like(xx))
+            return kg * (xx - mx[g]), kg * (yy - my[g])
+
+    return _RmsGroups.apply(x, y)
+
+
 def r80_smooth(x, y, mask, width_frac=0.05, fraction=0.8):
     """Differentiable 80 % containment radius about the centroid: the root r
     of G(r) = <sigmoid((r - rho_i) / (w r))> - fraction = 0 with w =

@@ -88,3 +88,26 @@ def test_sc_gradient_vs_finite_differences(kind):
     err = np.abs((g - fd) * h)
     rel = err / np.maximum(np.abs(fd * h), 1e-3 * scale)
     assert rel.max() < 1e-4, (rel.max(), int(rel.argmax()), g, fd)
+
+
+def test_rms_spot_groups_matches_per_group():
+    """The grouped RMS loss (two moment passes on the device, elementwise
+    backward) equals the sum of the per-group losses and their gradients."""
+    import torch
+
+    g = torch.Generator().manual_seed(4)
+    n, groups = 200_000, 5
+    x = (30 * torch.rand(n, generator=g, dtype=torch.float64) + 0.2 * torch.randn(n, generator=g,
+                                                                                  dtype=torch.float64)).cuda()
+    y = (0.2 * torch.randn(n, generator=g, dtype=torch.float64)).cuda()
+    group = (torch.arange(n) * groups // n).to(torch.int32).cuda()
+    mask = (torch.rand(n, generator=g) < 0.6).cuda()
+    xa, ya = x.clone().requires_grad_(), y.clone().requires_grad_()
+    la = A.rms_spot_groups(xa, ya, mask, group, groups)
+    la.backward()
+    xb, yb = x.clone().requires_grad_(), y.clone().requires_grad_()
+    lb = sum(A.rms_spot(xb, yb, mask & (group == k)) for k in range(groups))
+    lb.backward()
+    assert abs(float(la) - float(lb)) <= 1e-12 * abs(float(lb))
+    for a, b in ((xa.grad, xb.grad), (ya.grad, yb.grad)):
+        assert float((a - b).abs().max()) <= 1e-12 * float(b.abs().max())
