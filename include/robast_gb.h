@@ -478,10 +478,10 @@ int rbg_trace_host(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
  * opts->precision == RBG_PREC_MIXED is accepted.  Calls share the array and
  * it keeps the last call's contents: calls that overlap on the GPU race.
  * Each call copies the scene tables in from host memory and waits for its
- * stream to read the error word back.  The first call on a device looks up
- * the array's address with that device current; make it before any stream
- * capture begins.  It sets no device limit: no tracer kernel recurses, and
- * the driver sizes each launch's stack to the kernel's static need. */
+ * stream to read the error word back, so it cannot be captured into a CUDA
+ * graph.  The first call on a device looks up the array's address with
+ * that device current.  It sets no device limit: no tracer kernel recurses,
+ * and the driver sizes each launch's stack to the kernel's static need. */
 int rbg_trace_noalloc(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
                       const rbg_trace_opts* opts, void* stream);
 

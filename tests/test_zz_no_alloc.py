@@ -64,9 +64,9 @@ NM = 1e-7
 ])
 def test_noalloc_matches_trace_twice(name, kw):
     """The no-allocation call runs first, on a scene no other entry point
-    has touched (its tables, its thin-film table fill and the per-thread
-    stack limit are all set up by rbg_trace_noalloc itself, twice in a row);
-    the reference is rbg_trace on a second, identical scene afterwards."""
+    has touched (its tables and its thin-film table fill are set up by
+    rbg_trace_noalloc itself, twice in a row); the reference is rbg_trace
+    on a second, identical scene afterwards."""
     import torch
 
     from robast_gb300 import device
