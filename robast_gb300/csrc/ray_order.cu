@@ -23,6 +23,7 @@
 // order is whatever the atomics give.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 
@@ -32,9 +33,10 @@
 namespace rbg {
 namespace {
 
-// key bits: about 4 cells per ray, at most 2^24 cells; a quarter of the
-// bits (at most 6) number the direction cell
-constexpr int kMinKeyBits = 12, kMaxKeyBits = 24, kMaxDirBits = 6;
+// key bits: about 4 cells per ray up to 2^24 cells, then about one cell
+// per ray up to 2^26; a quarter of the bits (at most 6) number the
+// direction cell
+constexpr int kMinKeyBits = 12, kMaxKeyBits = 26, kMaxDirBits = 6;
 // Index chunks (off): with kChunkShift = s > 0 the rays [c 2^s, (c + 1) 2^s)
 // are ordered among themselves and chunk c's rays are taken up before chunk
 // c + 1's (the chunk is the key's top field), so the rays in flight write
@@ -46,7 +48,7 @@ constexpr int kMinKeyBits = 12, kMaxKeyBits = 24, kMaxDirBits = 6;
 // batch is ordered as one chunk.  s is raised until there are at most
 // kMaxChunks chunks.
 constexpr int kChunkShift = 0, kMaxChunks = 32;
-constexpr int64_t kMaxBuckets = int64_t(1) << 25;
+constexpr int64_t kMaxBuckets = int64_t(1) << 26;
 constexpr int kScanTile = 1024;
 constexpr int kThreads = 256;
 
@@ -145,6 +147,12 @@ __global__ void plan_kernel(const uint32_t* box, int dir_bits, int pos_bits, int
     P.bits[a] = 0;
   }
   const double ext[6] = {size[0], size[1], size[2], size[3], size[4], size[5]};
+  // a batch of parallel rays (one direction) gives every key bit to the
+  // start point
+  if (!(size[3] > 0) && !(size[4] > 0) && !(size[5] > 0)) {
+    pos_bits += dir_bits;
+    dir_bits = 0;
+  }
   int seq[kMaxKeyBits];
   const int total = dir_bits + pos_bits;
   for (int b = 0; b < total; ++b) {
@@ -269,7 +277,8 @@ Layout layout(int64_t n) {
   const int64_t chunks = cs > 0 ? ((n - 1) >> cs) + 1 : 1;
   const int64_t per = cs > 0 ? (int64_t(1) << cs) : n;
   int kb = kMinKeyBits;
-  while (kb < kMaxKeyBits && (int64_t(1) << kb) < 4 * per) ++kb;
+  const int64_t cells = std::min<int64_t>(4 * per, std::max<int64_t>(int64_t(1) << 24, per));
+  while (kb < kMaxKeyBits && (int64_t(1) << kb) < cells) ++kb;
   while (kb > kMinKeyBits && (chunks << kb) > kMaxBuckets) --kb;
   L.chunk_shift = cs;
   L.dir_bits = kb / 4 < kMaxDirBits ? kb / 4 : kMaxDirBits;
