@@ -1583,94 +1583,6 @@ RBG_D double asph_dist_out_f(const double* P, const float* Pf, const LRay& L, bo
   return asph_dist4_f(P, Pf, L, twin, face);
 }
 
-// FP32 bracket [lo, hi] of the entering distance asph_dist_out_f returns
-// (DistFromOutside, :383-412), so that a boundary search polishes in FP64
-// only the daughter that can be the nearest.  lo = 3e38: the ray misses the
-// bounding tube.  face = 1 or 2: the distance is that face's root (polish it
-// from t0 with the slope factor sc); face = 0: only lo is known (from the
-// tube), evaluate the whole shape.  A single face decides when the faces are
-// twins (same polynomial, vertices dz apart): face 2's root lies sc dz past
-// face 1's to first order, so the face met first is known from the sign of
-// sc dz even where the two roots are closer than the FP32 error (1 um
-// shells); that face's root must then be accepted beyond doubt (t clearly
-// positive, the hit radius clearly inside [rmin, rmax]) and neither wall
-// reachable before it, and the incidence not grazing (|sc| < 100, where the
-// first-order relation holds to better than 1e-3 of sc dz).
-struct AsphBracket {
-  float lo, hi;
-  int face;
-  float t0, sc;
-};
-RBG_D void asph_bracket_out_f(const double* P, const float* Pf, const double* T, const LRay& L, bool twin,
-                              AsphBracket& b) {
-  b.lo = 3e38f;
-  b.hi = 3e38f;
-  b.face = 0;
-  b.t0 = 0.f;
-  b.sc = 0.f;
-  // the bounding-tube screen of asph_dist_out_f
-  const float pad = 1e-4f + 1e-5f * (Pf[RBG_ASPH_RMAX] + Pf[RBG_ASPH_DZ]) +
-                    1e-6f * (fabsf(L.pf.x) + fabsf(L.pf.y) + fabsf(L.pf.z) + fabsf(Pf[RBG_ASPH_ORIGIN_Z]));
-  const float R = Pf[RBG_ASPH_RMAX] + pad, Z = Pf[RBG_ASPH_DZ] + pad;
-  const float ox = L.pf.x, oy = L.pf.y, oz = L.pf.z - Pf[RBG_ASPH_ORIGIN_Z];
-  const float dx = L.df.x, dy = L.df.y, dzz = L.df.z;
-  float t0 = 0.f, t1 = 3.0e38f;
-  if (dzz != 0.f) {
-    float ta = (-Z - oz) / dzz, tb = (Z - oz) / dzz;
-    t0 = fmaxf(t0, fminf(ta, tb));
-    t1 = fminf(t1, fmaxf(ta, tb));
-  } else if (fabsf(oz) > Z) {
-    return;
-  }
-  if (t0 > t1) return;
-  float lo = t0;
-  float A = dx * dx + dy * dy, B = ox * dx + oy * dy, C = ox * ox + oy * oy - R * R;
-  if (A == 0.f) {
-    if (C > 0.f) return;
-  } else {
-    float disc = B * B - A * C;
-    if (disc < 0.f) return;
-    float sq = sqrtf(disc);
-    float c0 = (-B - sq) / A, c1 = (-B + sq) / A;
-    lo = fmaxf(t0, c0);
-    const float hi = fminf(t1, c1);
-    if (lo > hi + pad + 1e-5f * (fabsf(lo) + fabsf(hi))) return;
-  }
-  // no crossing of the disk comes before the ray enters its (enlarged) tube
-  b.lo = fmaxf(0.f, lo - pad - 1e-5f * fabsf(lo));
-  if (!twin) return;
-  float tf, sf, ef;
-  if (!asph_newton_f(Pf, 1, L, tf, sf, &ef)) return;
-  if (!(fabsf(sf) < 100.f)) return;
-  const float dzf = (float)T[RBG_TRIG_ASPH_DZ];
-  const float step2 = sf * dzf;  // face 2's root minus face 1's, to first order
-  if (!(fabsf(step2) > 1e-3f * fabsf(dzf))) return;
-  const int near = step2 > 0.f ? 1 : 2;
-  const float tn = near == 1 ? tf : tf + step2;
-  const float M = ef + 1e-3f * fabsf(step2);
-  if (!(tn > M)) return;
-  const float hx = ox + tn * dx, hy = oy + tn * dy;
-  const float rh = sqrtf(hx * hx + hy * hy);
-  const float pr = M + 1e-4f + 1e-6f * (fabsf(ox) + fabsf(oy) + tn);
-  if (rh > Pf[RBG_ASPH_RMAX] - pr) return;
-  if (Pf[RBG_ASPH_RSEG] != 0.f && rh < Pf[RBG_ASPH_RMIN] + pr) return;
-  if (asph_wall_maybe_f(Pf, false, L, tn + M) || asph_wall_maybe_f(Pf, true, L, tn + M)) return;
-  b.face = near;
-  b.t0 = tn;
-  b.sc = sf;
-  b.lo = tn - M;
-  b.hi = tn + M;
-}
-
-// The distance a face = 1 / 2 bracket promises: that face's root polished in
-// FP64 from t0 and accepted as asph_accept does; kBig when the polish or the
-// acceptance fails (then the caller evaluates the whole shape).
-RBG_D double asph_face_dist(const double* P, const LRay& L, const AsphBracket& b) {
-  double t = (double)b.t0;
-  if (!asph_polish(P, b.face, L, (double)b.sc, t)) return kBig;
-  return asph_accept(P, L, t);
-}
-
 // Contains (:330-347) behind FP32 screens of the radius and of both sags
 // (faces with c == 0; the screen margin is 2e-5 of the sum of the sag's term
 // magnitudes plus the coordinates, >10x the FP32 rounding of the sums)
