@@ -833,7 +833,8 @@ def main():
     for f in ("x", "y", "z", "t", "dx", "dy", "dz"):
         setattr(rr, f, C.cast(C.c_void_p(host_out[f].data_ptr()), dp))
     opts = man.trace_options(prec)
-    N.lib().rbg_trace_host(man.scene.handle, C.byref(rs), C.byref(rr), C.byref(opts))
+    for _ in range(max(1, args.warmup)):
+        N.lib().rbg_trace_host(man.scene.handle, C.byref(rs), C.byref(rr), C.byref(opts))
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
