@@ -771,7 +771,7 @@ def main():
     tuned = None
     if prec == N.PREC_MIXED and args.compaction == 0:
         tuned = device.autotune(man, rays, res)
-    block_used, _, chunk_used = device.tuning(man) if prec == N.PREC_MIXED else (128, 0, 0)
+    block_used = device.tuning(man)[0] if prec == N.PREC_MIXED else 128
     ms, launches, clocks = timed(prec, res)
     kms = float(np.mean(kernel_ms)) if kernel_ms and min(kernel_ms) > 0 else None
     seg = int((res["npoints"].to(torch.int64) - 1).sum().item())
@@ -854,7 +854,6 @@ def main():
             "segments_per_step": seg,
             "compaction": args.compaction or tuned,
             "block_size": block_used,
-            "ray_order_chunk_shift": chunk_used,
             "tracer_kernel_ms": kms,
             "roofline": roof,
             "e2e": e2e, "clocks": clocks, "vs_plain_fp64": compare}

@@ -448,26 +448,21 @@ int rbg_multilayer_rt(rbg_scene* scene, int32_t multilayer, int32_t mode, int32_
  * traces the DEVICE rays `in` with each candidate block size (256 and 128
  * where the scene runs the lean instance) and compaction threshold (1, 8,
  * 16, 32), two rounds each, keeps the fastest pair in the scene for later
- * calls that leave opts->block_size / opts->compaction at 0, then times
- * the spatial take-up order in index chunks of 2^21 rays against one
- * chunk (batches of more than 2^21 rays) and keeps the faster; returns the
- * threshold in *chosen (rbg_scene_tuning reads all three).  `out` receives
+ * calls that leave opts->block_size / opts->compaction at 0, and returns
+ * the threshold in *chosen (rbg_scene_tuning reads both).  `out` receives
  * the trace results (identical for every candidate).  Synchronises
  * `stream`. */
 int rbg_scene_autotune(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
                        const rbg_trace_opts* opts, void* stream, int32_t* chosen);
-/* The mixed tracer's block size, compaction threshold and take-up order
- * chunk shift for the scene: rbg_scene_autotune's choice, else the
- * defaults (block: 256 for scenes of the lean instance, else the
- * instance's own size; threshold 32; chunk shift 0, the batch as one
- * chunk).  Any output pointer may be NULL. */
-int rbg_scene_tuning(const rbg_scene* scene, int32_t* block_size, int32_t* compaction,
-                     int32_t* order_chunk_shift);
+/* The mixed tracer's block size and compaction threshold for the scene:
+ * rbg_scene_autotune's choice, else the defaults (block: 256 for scenes of
+ * the lean instance, else the instance's own size; threshold 32).  Either
+ * output pointer may be NULL. */
+int rbg_scene_tuning(const rbg_scene* scene, int32_t* block_size, int32_t* compaction);
 /* Set the scene's tuning directly (for instance an earlier process's
  * rbg_scene_autotune choice): block size 0 (default), 128 or 256;
- * compaction 0 (default) .. 32; chunk shift 0 or 21.  Results do not
- * depend on any of them. */
-int rbg_scene_set_tuning(rbg_scene* scene, int32_t block_size, int32_t compaction, int32_t order_chunk_shift);
+ * compaction 0 (default) .. 32.  Results do not depend on either. */
+int rbg_scene_set_tuning(rbg_scene* scene, int32_t block_size, int32_t compaction);
 
 /* Same, with HOST buffers: copies the rays in, traces, copies the results
  * out and synchronises (the call a ROOT-side AOpticsManager binding makes,

@@ -197,8 +197,8 @@ def _declare(L):
     L.rbg_trace_host.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts)]
     L.rbg_scene_autotune.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts), vp,
                                      C.POINTER(C.c_int32)]
-    L.rbg_scene_tuning.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
-    L.rbg_scene_set_tuning.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
+    L.rbg_scene_tuning.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    L.rbg_scene_set_tuning.argtypes = [vp, C.c_int32, C.c_int32]
     L.rbg_last_launch_count.argtypes = [vp]
     L.rbg_scene_set_timing.argtypes = [vp, C.c_int32]
     L.rbg_last_kernel_ms.argtypes = [vp]

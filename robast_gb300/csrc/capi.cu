@@ -181,6 +181,8 @@ extern "C" double rbg_last_kernel_ms(const rbg_scene* s) { return s && s->timing
 
 // the two tracer launchers (trace_mixed.cu, trace_fp64.cu)
 namespace rbg {
+size_t ray_order_bytes(int64_t n);
+int build_ray_order(const KernelRays& in, int64_t n, void* ws, KernelRays* sorted, cudaStream_t st);
 int mixed_block_size(unsigned features);
 int launch_mixed(const DevScene& S, const KernelRays& in, const KernelOut& out, int64_t n, const rbg_trace_opts& o,
                  cudaStream_t st, unsigned* err_flags, unsigned long long* counter, int* launches);
@@ -255,7 +257,7 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
     if (o.workspace && o.workspace_bytes >= need) ws = o.workspace;
     else if (s->order_ws && s->order_ws_bytes >= need) ws = s->order_ws;
     if (ws) {
-      if ((rc = build_ray_order(kr, in->n, ws, &kr, st, s->tuned_chunk))) return rc;
+      if ((rc = build_ray_order(kr, in->n, ws, &kr, st))) return rc;
       launches += 7;
     }
   }
@@ -283,23 +285,19 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
 // stream, and keep the fastest in the scene (used by every later call
 // whose options leave them at 0).  The results in `out` are those of any
 // single trace: they depend on neither.
-extern "C" int rbg_scene_tuning(const rbg_scene* s, int32_t* block_size, int32_t* compaction,
-                                int32_t* order_chunk_shift) {
+extern "C" int rbg_scene_tuning(const rbg_scene* s, int32_t* block_size, int32_t* compaction) {
   if (!s) return RBG_ERR_ARG;
-  if (order_chunk_shift) *order_chunk_shift = s->tuned_chunk;
   const int fixed = mixed_block_size(s->features);
   if (block_size) *block_size = fixed ? fixed : (s->tuned_block ? s->tuned_block : 256);
   if (compaction) *compaction = s->tuned_compaction ? s->tuned_compaction : 32;
   return RBG_OK;
 }
 
-extern "C" int rbg_scene_set_tuning(rbg_scene* s, int32_t block_size, int32_t compaction, int32_t order_chunk_shift) {
-  if (!s || compaction < 0 || compaction > 32 || (order_chunk_shift != 0 && order_chunk_shift != kRayOrderChunkShift))
-    return RBG_ERR_ARG;
+extern "C" int rbg_scene_set_tuning(rbg_scene* s, int32_t block_size, int32_t compaction) {
+  if (!s || compaction < 0 || compaction > 32) return RBG_ERR_ARG;
   if (block_size != 0 && block_size != 128 && block_size != 256) return RBG_ERR_ARG;
   s->tuned_block = block_size;
   s->tuned_compaction = compaction;
-  s->tuned_chunk = order_chunk_shift;
   return RBG_OK;
 }
 
@@ -357,40 +355,11 @@ extern "C" int rbg_scene_autotune(rbg_scene* s, const rbg_rays* in, rbg_result* 
         best_block = lean ? kLeanBlocks[b] : 0;
         first = false;
       }
-  // then the take-up order in index chunks against one chunk, with that
-  // pair (batches beyond one chunk taken up in spatial order only)
-  int32_t best_chunk = 0;
-  if ((rc == RBG_OK || rc == RBG_ERR_NAN || rc == RBG_ERR_CAP) && o.ray_order == RBG_ORDER_SPATIAL &&
-      in->n > (int64_t(1) << kRayOrderChunkShift)) {
-    o.block_size = best_block;
-    o.compaction = best;
-    const int saved = s->tuned_chunk;
-    float ms_chunk = 0.f;
-    for (int round = 0; round < 2; ++round) {
-      s->tuned_chunk = kRayOrderChunkShift;
-      float ms = 0.f;
-      if (cudaEventRecord(e0, st) != cudaSuccess) {
-        rc = RBG_ERR_CUDA;
-        break;
-      }
-      rc = rbg_trace(s, in, out, &o, stream);
-      if (rc != RBG_OK && rc != RBG_ERR_NAN && rc != RBG_ERR_CAP) break;
-      if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
-          cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
-        rc = RBG_ERR_CUDA;
-        break;
-      }
-      ms_chunk = round == 0 ? ms : (ms < ms_chunk ? ms : ms_chunk);
-    }
-    s->tuned_chunk = saved;
-    if (ms_chunk > 0.f && ms_chunk < best_ms) best_chunk = kRayOrderChunkShift;
-  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc != RBG_OK && rc != RBG_ERR_NAN && rc != RBG_ERR_CAP) return rc;
   s->tuned_compaction = best;
   s->tuned_block = best_block;
-  s->tuned_chunk = best_chunk;
   if (chosen) *chosen = best;
   return rc;
 }
@@ -544,7 +513,7 @@ extern "C" int rbg_trace_host(rbg_scene* s, const rbg_rays* in, rbg_result* out,
     if (o.block_size == 0 && o.precision == RBG_PREC_MIXED) o.block_size = s->tuned_block;
     int nl = 0;
     if (want_ray_order(o, m)) {
-      if ((rc = build_ray_order(kr, m, sl.order_ws, &kr, st, s->tuned_chunk))) return rc;
+      if ((rc = build_ray_order(kr, m, sl.order_ws, &kr, st))) return rc;
       nl += 7;
     }
     if ((rc = launch_trace(s, kr, ko, m, o, st, sl.err, sl.counter, &nl))) return rc;

@@ -14,13 +14,6 @@ struct rbg_device_scene {
 };
 
 namespace rbg {
-// the index-chunk shift of the take-up order the autotuner may choose
-// (ray_order.cu); 0 orders a batch as one chunk
-constexpr int kRayOrderChunkShift = 21;
-struct KernelRays;
-size_t ray_order_bytes(int64_t n);
-int build_ray_order(const KernelRays& in, int64_t n, void* ws, KernelRays* sorted, cudaStream_t st,
-                    int chunk_shift);
 int ensure_device(rbg_scene* s);  // upload on first use (capi.cu)
 int sm_count();     // SMs of the current device
 // precalculated thin-film tables of s into `tables` (device), tmm.cu

@@ -27,7 +27,6 @@
 #include <cstdint>
 #include <cstring>
 
-#include "device_state.cuh"
 #include "robast_gb.h"
 #include "tracer.cuh"
 
@@ -38,18 +37,18 @@ namespace {
 // per ray up to 2^26; a quarter of the bits (at most 6) number the
 // direction cell
 constexpr int kMinKeyBits = 12, kMaxKeyBits = 26, kMaxDirBits = 6;
-// Index chunks: with a chunk shift s > 0 the rays [c 2^s, (c + 1) 2^s) are
-// ordered among themselves and chunk c's rays are taken up before chunk
-// c + 1's (the chunk is the key's top field).  Batches are usually laid out
-// variant by variant (field angles, misalignment samples, cone geometries),
-// so a chunk holds few variants, and the rays in flight meet the geometry
-// of few copies at once and write their results into one chunk's stretch
-// of the output arrays.  On 4e7 Schmidt-Cassegrain rays (256 misalignment
-// samples) chunks of 2^21 rays trace 31 % faster; on the Schwarzschild-
-// Couder batch (5 field angles) they cost 1-7 % (sparser cells), so the
-// autotuner decides (rbg_scene_autotune).  s is raised until there are at
-// most kMaxChunks chunks.
-constexpr int kMaxChunks = 64;
+// Index chunks (off): with kChunkShift = s > 0 the rays [c 2^s, (c + 1) 2^s)
+// are ordered among themselves and chunk c's rays are taken up before chunk
+// c + 1's (the chunk is the key's top field), so the rays in flight write
+// their results into one or two chunks' stretch of the output arrays and L2
+// completes more of their 32-byte sectors before writing them back.  On
+// 1e7 Schwarzschild-Couder rays, s = 20 cut the trace kernel's DRAM traffic
+// from 600 to 390 B per ray but made it 5-7 % slower (sparser cells, less
+// coherent warps); s = 21 was 0.3-2 % slower on the light guide, the
+// Davies-Cotton dish and 4e7 Schmidt-Cassegrain rays.  Throughput is what
+// the trace is bound by, so the batch is ordered as one chunk.  s is raised until there are at most
+// kMaxChunks chunks.
+constexpr int kChunkShift = 0, kMaxChunks = 32;
 constexpr int64_t kMaxBuckets = int64_t(1) << 26;
 constexpr int kScanTile = 1024;
 constexpr int kThreads = 256;
@@ -270,9 +269,9 @@ struct Layout {
   size_t box, plan, keys, counts, tile_sum, order, sorted, total;
 };
 
-Layout layout(int64_t n, int chunk_shift) {
+Layout layout(int64_t n) {
   Layout L;
-  int cs = chunk_shift;
+  int cs = kChunkShift;
   if (cs > 0)
     while (((n - 1) >> cs) + 1 > kMaxChunks) ++cs;
   if (cs > 0 && (n - 1) >> cs == 0) cs = 0;  // one chunk
@@ -301,20 +300,14 @@ Layout layout(int64_t n, int chunk_shift) {
 
 }  // namespace
 
-// the workspace covers every chunk shift the tracer may use
-size_t ray_order_bytes(int64_t n) {
-  if (!(n > 0 && n <= 0x7fffffff)) return 0;
-  return std::max(layout(n, 0).total, layout(n, kRayOrderChunkShift).total);
-}
+size_t ray_order_bytes(int64_t n) { return n > 0 && n <= 0x7fffffff ? layout(n).total : 0; }
 
 // Write the take-up order of rays 0..n-1 and the rays in that order into
 // `ws` (ray_order_bytes(n) bytes) on stream st; *sorted describes them
-// (gathered, with the order).  n must fit in an int32; chunk_shift 0 orders
-// the batch as one chunk, else as index chunks of 2^chunk_shift rays.
-int build_ray_order(const KernelRays& in, int64_t n, void* ws, KernelRays* sorted, cudaStream_t st,
-                    int chunk_shift) {
-  if (n <= 0 || n > 0x7fffffff || !ws || !sorted || chunk_shift < 0 || chunk_shift > 30) return RBG_ERR_ARG;
-  const Layout L = layout(n, chunk_shift);
+// (gathered, with the order).  n must fit in an int32.
+int build_ray_order(const KernelRays& in, int64_t n, void* ws, KernelRays* sorted, cudaStream_t st) {
+  if (n <= 0 || n > 0x7fffffff || !ws || !sorted) return RBG_ERR_ARG;
+  const Layout L = layout(n);
   char* base = static_cast<char*>(ws);
   auto* box = reinterpret_cast<uint32_t*>(base + L.box);
   auto* plan = reinterpret_cast<Plan*>(base + L.plan);

@@ -51,7 +51,6 @@ struct rbg_scene {
   float last_kernel_ms = -1.f;
   int tuned_compaction = 0;  // rbg_scene_autotune's choice, 0: none yet
   int tuned_block = 0;       // its block size for the lean mixed instance, 0: none yet
-  int tuned_chunk = 0;       // its take-up order chunk shift (0: one chunk)
   void* workspace = nullptr;
   size_t workspace_bytes = 0;
   // rbg_trace's ray-order workspace (grown on demand, freed with the scene)

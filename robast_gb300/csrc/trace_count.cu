@@ -58,6 +58,8 @@ extern "C" int rbg_event_flops(int32_t kind, double* fp64, double* fp32) {
 }
 
 namespace rbg {
+size_t ray_order_bytes(int64_t n);
+int build_ray_order(const KernelRays& in, int64_t n, void* ws, KernelRays* sorted, cudaStream_t st);
 }  // namespace rbg
 
 // rbg_trace (mixed precision) through the counting build: counts[k] gets
@@ -81,7 +83,7 @@ extern "C" int rbg_trace_count_events(rbg_scene* s, const rbg_rays* in, rbg_resu
   // the take-up order of rbg_trace, when the caller lends its workspace
   if (in->n >= (1 << 14) && opts->ray_order == RBG_ORDER_SPATIAL && opts->workspace &&
       opts->workspace_bytes >= ray_order_bytes(in->n))
-    if ((rc = build_ray_order(kr, in->n, opts->workspace, &kr, st, s->tuned_chunk))) return rc;
+    if ((rc = build_ray_order(kr, in->n, opts->workspace, &kr, st))) return rc;
   rbg_trace_opts o = *opts;
   if (o.compaction == 0) o.compaction = s->tuned_compaction;
   if (in->n > 0 &&

@@ -150,13 +150,12 @@ def autotune(manager, rays, res=None, stream=None) -> int:
 
 
 def tuning(manager):
-    """(block size, compaction threshold, take-up order chunk shift) of the
-    mixed tracer for the scene (rbg_scene_tuning: the autotuner's choice,
-    else the defaults)."""
+    """(block size, compaction threshold) of the mixed tracer for the scene
+    (rbg_scene_tuning: the autotuner's choice, else the defaults)."""
     scene = manager._ensure_scene()
-    b, c, k = C.c_int32(0), C.c_int32(0), C.c_int32(0)
-    N.check(N.lib().rbg_scene_tuning(scene.handle, C.byref(b), C.byref(c), C.byref(k)), "rbg_scene_tuning")
-    return int(b.value), int(c.value), int(k.value)
+    b, c = C.c_int32(0), C.c_int32(0)
+    N.check(N.lib().rbg_scene_tuning(scene.handle, C.byref(b), C.byref(c)), "rbg_scene_tuning")
+    return int(b.value), int(c.value)
 
 
 def focal_moments(res, group=None, n_groups: int = 1, stream=None):
@@ -245,12 +244,11 @@ def shoot(kind: int, params, n: int, lam: float, rot=None, tr=None, v=None, seed
     return {f: t[:m] for f, t in out.items()}
 
 
-def set_tuning(manager, block_size: int = 0, compaction: int = 0, order_chunk_shift: int = 0):
-    """rbg_scene_set_tuning: the mixed tracer's block size, compaction
-    threshold and take-up order chunk shift for the scene, set directly."""
+def set_tuning(manager, block_size: int = 0, compaction: int = 0):
+    """rbg_scene_set_tuning: the mixed tracer's block size and compaction
+    threshold for the scene, set directly."""
     scene = manager._ensure_scene()
-    N.check(N.lib().rbg_scene_set_tuning(scene.handle, int(block_size), int(compaction), int(order_chunk_shift)),
-            "rbg_scene_set_tuning")
+    N.check(N.lib().rbg_scene_set_tuning(scene.handle, int(block_size), int(compaction)), "rbg_scene_set_tuning")
 
 
 # event kinds of rbg_trace_count_events, in the order of the counts

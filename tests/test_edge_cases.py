@@ -188,13 +188,16 @@ def test_autotune_picks_a_candidate_and_keeps_results():
     assert st == N.RBG_OK
     rays = device.to_device(batch, "cuda:0")
     res = device.alloc_result(len(batch["x"]), "cuda:0")
-    assert device.tuning(man) == (256, 32, 0)  # the lean instance's defaults before tuning
+    assert device.tuning(man) == (256, 32)  # the lean instance's defaults before tuning
     chosen = device.autotune(man, rays, res)
     torch.cuda.synchronize()
     assert chosen in (1, 8, 16, 32)
     # the tuned pair: a block size the lean instance is compiled for
-    block, thr, chunk = device.tuning(man)
-    assert block in (128, 256) and thr == chosen and chunk == 0  # 2e4 rays: one chunk
+    block, thr = device.tuning(man)
+    assert block in (128, 256) and thr == chosen
+    # a tuning set directly is the one reported, and changes no result
+    device.set_tuning(man, 128, 1)
+    assert device.tuning(man) == (128, 1)
     assert man.scene is not None
     tuned = {k: res[k].cpu().numpy() for k in FIELDS}
     _same(tuned, ref)

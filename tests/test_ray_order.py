@@ -53,20 +53,3 @@ def test_spatial_order_histories_and_host_pipeline():
         np.testing.assert_array_equal(getattr(arr, f), a[f])
     np.testing.assert_array_equal(arr.x, a["x"])
 
-
-def test_index_chunked_order_changes_no_result():
-    """The take-up order in index chunks of 2^21 rays (the autotuner's
-    alternative for batches laid out variant by variant) against input
-    order, on a light-guide batch of 64 cone variants and more than two
-    chunks; and the tuning the scene reports back."""
-    from robast_gb300 import device
-
-    man, batch = configs.light_guide(n_rays=4_500_000, n_variants=64)
-    st0, a = _device(man, batch, N.ORDER_INPUT)
-    device.reserve(man, len(batch["x"]))
-    device.set_tuning(man, 0, 0, 21)
-    assert device.tuning(man)[2] == 21
-    st1, b = _device(man, batch, N.ORDER_SPATIAL)
-    assert st0 == st1
-    for f in FIELDS:
-        np.testing.assert_array_equal(a[f], b[f], err_msg=f)
