@@ -382,6 +382,18 @@ size_t rbg_trace_workspace_bytes(int64_t n_rays);
  * its own scene). */
 int rbg_trace(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
               const rbg_trace_opts* opts, void* stream);
+/* rbg_trace without waiting: everything the trace does is put on `stream`
+ * and the call returns; nothing is read back, allocated or synchronised,
+ * so a host loop can run ahead and a CUDA graph can capture the call (the
+ * tracer's whole batch then replays as one graph of the take-up order's
+ * kernels and the persistent tracer).  The scene must already be on the
+ * device (rbg_scene_reserve, or an earlier trace), and the workspace rule
+ * is rbg_trace's.  No timing events are recorded.  rbg_trace_status reads
+ * the status of the scene's last trace on `stream` (it waits for the
+ * stream): RBG_OK, RBG_ERR_NAN or RBG_ERR_CAP, as rbg_trace returns. */
+int rbg_trace_async(rbg_scene* scene, const rbg_rays* in, rbg_result* out,
+                    const rbg_trace_opts* opts, void* stream);
+int rbg_trace_status(rbg_scene* scene, void* stream);
 
 /* ACorsikaIACTFile::Open (src/ACorsikaIACTFile.cxx:191-257) on an
  * in-memory, decompressed eventio stream (the caller inflates .gz files):

@@ -194,6 +194,8 @@ def _declare(L):
                                          C.POINTER(C.c_uint64), C.c_int32]
     L.rbg_trace_workspace_bytes.restype = C.c_size_t
     L.rbg_trace.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts), vp]
+    L.rbg_trace_async.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts), vp]
+    L.rbg_trace_status.argtypes = [vp, vp]
     L.rbg_trace_host.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts)]
     L.rbg_scene_autotune.argtypes = [vp, C.POINTER(Rays), C.POINTER(Result), C.POINTER(TraceOpts), vp,
                                      C.POINTER(C.c_int32)]

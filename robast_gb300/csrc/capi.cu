@@ -228,8 +228,13 @@ extern "C" int rbg_scene_reserve(rbg_scene* s, int64_t max_rays, int32_t hist_ca
   return host_workspace_reserve(s, max_rays, hist_cap);
 }
 
-extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, const rbg_trace_opts* opts,
-                         void* stream) {
+namespace rbg {
+namespace {
+// Everything a trace puts on the stream -- the error word's reset, the
+// take-up order, the tracer kernel (and its timing events) -- without
+// reading anything back
+int trace_enqueue(rbg_scene* s, const rbg_rays* in, rbg_result* out, const rbg_trace_opts* opts, cudaStream_t st,
+                  bool timed) {
   if (!s || !in || !out || !opts) return RBG_ERR_ARG;
   if (in->n < 0 || opts->limit <= 0) return RBG_ERR_ARG;
   if (in->n > 0 && (!in->x || !in->y || !in->z || !in->dx || !in->dy || !in->dz || !in->lambda)) return RBG_ERR_ARG;
@@ -237,10 +242,9 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
   if (opts->workspace && (reinterpret_cast<uintptr_t>(opts->workspace) & 255)) return RBG_ERR_ARG;
   int rc = ensure_device(s);
   if (rc) return rc;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   s->last_launches = 0;
-  if (in->n == 0) return RBG_OK;
   if (cudaMemsetAsync(s->dev->err_flags, 0, sizeof(unsigned), st) != cudaSuccess) return RBG_ERR_CUDA;
+  if (in->n == 0) return RBG_OK;
   KernelRays kr{in->x, in->y, in->z, in->t, in->dx, in->dy, in->dz, in->lambda};
   KernelOut ko{out->status, out->npoints, out->last_node, out->x, out->y, out->z, out->t,
                out->dx, out->dy, out->dz, out->hist_cap, out->hist_xyzt, out->hist_node};
@@ -262,29 +266,54 @@ extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, cons
     }
   }
   cudaEvent_t* tev = reinterpret_cast<cudaEvent_t*>(s->tev);
-  if (s->timing && cudaEventRecord(tev[0], st) != cudaSuccess) return RBG_ERR_CUDA;
+  if (timed && cudaEventRecord(tev[0], st) != cudaSuccess) return RBG_ERR_CUDA;
   if (o.precision == RBG_PREC_MIXED)
     rc = launch_mixed(s->dev->view, kr, ko, in->n, o, st, s->dev->err_flags, s->dev->counter, &launches);
   else
     rc = launch_fp64(s->dev->view, kr, ko, in->n, o, st, s->dev->err_flags, &launches);
   if (rc) return rc;
-  if (s->timing && cudaEventRecord(tev[1], st) != cudaSuccess) return RBG_ERR_CUDA;
+  if (timed && cudaEventRecord(tev[1], st) != cudaSuccess) return RBG_ERR_CUDA;
   s->last_launches = launches;
-  unsigned bits = 0;
-  if ((rc = read_errors(s, st, &bits))) return rc;
-  if (s->timing && cudaEventElapsedTime(&s->last_kernel_ms, tev[0], tev[1]) != cudaSuccess) return RBG_ERR_CUDA;
+  return RBG_OK;
+}
+
+int status_of(unsigned bits) {
   if (bits & ERR_BIT_NAN) return RBG_ERR_NAN;
   if (bits & ERR_BIT_CAP) return RBG_ERR_CAP;
   return RBG_OK;
 }
+}  // namespace
+}  // namespace rbg
 
-// The autotuner of the mixed tracer: trace the caller's rays once to warm
-// up, then once per candidate (block size, compaction threshold) -- block
-// sizes 256 and 128 for scenes the lean instance traces, the instance's
-// fixed 128 otherwise; thresholds 1, 8, 16, 32 -- timed with events on the
-// stream, and keep the fastest in the scene (used by every later call
-// whose options leave them at 0).  The results in `out` are those of any
-// single trace: they depend on neither.
+extern "C" int rbg_trace(rbg_scene* s, const rbg_rays* in, rbg_result* out, const rbg_trace_opts* opts,
+                         void* stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const bool timed = s && s->timing;
+  int rc = trace_enqueue(s, in, out, opts, st, timed);
+  if (rc) return rc;
+  if (in->n == 0) return RBG_OK;
+  unsigned bits = 0;
+  if ((rc = read_errors(s, st, &bits))) return rc;
+  cudaEvent_t* tev = reinterpret_cast<cudaEvent_t*>(s->tev);
+  if (timed && cudaEventElapsedTime(&s->last_kernel_ms, tev[0], tev[1]) != cudaSuccess) return RBG_ERR_CUDA;
+  return status_of(bits);
+}
+
+// rbg_trace without the read-back: stream-ordered, so that a host loop or
+// a CUDA graph can hold it
+extern "C" int rbg_trace_async(rbg_scene* s, const rbg_rays* in, rbg_result* out, const rbg_trace_opts* opts,
+                               void* stream) {
+  if (s && !s->dev) return RBG_ERR_ARG;  // the scene must be on the device already (rbg_scene_reserve)
+  return trace_enqueue(s, in, out, opts, static_cast<cudaStream_t>(stream), false);
+}
+
+extern "C" int rbg_trace_status(rbg_scene* s, void* stream) {
+  if (!s || !s->dev) return RBG_ERR_ARG;
+  unsigned bits = 0;
+  int rc = read_errors(s, static_cast<cudaStream_t>(stream), &bits);
+  return rc ? rc : status_of(bits);
+}
+
 extern "C" int rbg_scene_tuning(const rbg_scene* s, int32_t* block_size, int32_t* compaction) {
   if (!s) return RBG_ERR_ARG;
   const int fixed = mixed_block_size(s->features);
@@ -301,6 +330,13 @@ extern "C" int rbg_scene_set_tuning(rbg_scene* s, int32_t block_size, int32_t co
   return RBG_OK;
 }
 
+// The autotuner of the mixed tracer: trace the caller's rays once to warm
+// up, then once per candidate (block size, compaction threshold) -- block
+// sizes 256 and 128 for scenes the lean instance traces, the instance's
+// fixed 128 otherwise; thresholds 1, 8, 16, 32 -- timed with events on the
+// stream, and keep the fastest in the scene (used by every later call
+// whose options leave them at 0).  The results in `out` are those of any
+// single trace: they depend on neither.
 extern "C" int rbg_scene_autotune(rbg_scene* s, const rbg_rays* in, rbg_result* out, const rbg_trace_opts* opts,
                                   void* stream, int32_t* chosen) {
   if (!s || !in || !out || !opts) return RBG_ERR_ARG;

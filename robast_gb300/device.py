@@ -126,6 +126,34 @@ def trace(manager, rays, res=None, precision: Optional[int] = None, stream=None,
     return res, status
 
 
+def trace_async(manager, rays, res=None, precision: Optional[int] = None, stream=None, workspace_buf="auto"):
+    """rbg_trace_async: the trace of `trace` put on the stream without
+    waiting (capturable into a CUDA graph); rbg_trace_status (status())
+    reads its status later.  The scene must be on the device already
+    (reserve(), or an earlier trace).  Returns the result dict."""
+    torch = _torch()
+    scene = manager._ensure_scene()
+    n = rays["x"].numel()
+    if res is None:
+        res = alloc_result(n, rays["x"].device)
+    opts = manager.trace_options(precision)
+    ws = workspace(n, rays["x"].device) if isinstance(workspace_buf, str) else workspace_buf
+    if ws is not None:
+        opts.workspace = ws.data_ptr()
+        opts.workspace_bytes = ws.numel()
+    st_ptr = (stream if stream is not None else torch.cuda.current_stream()).cuda_stream
+    N.check(N.lib().rbg_trace_async(scene.handle, C.byref(_rays_struct(rays)), C.byref(_result_struct(res)),
+                                    C.byref(opts), C.c_void_p(st_ptr)), "rbg_trace_async")
+    return res
+
+
+def status(manager, stream=None) -> int:
+    """rbg_trace_status: the status of the scene's last trace on `stream`."""
+    torch = _torch()
+    st_ptr = (stream if stream is not None else torch.cuda.current_stream()).cuda_stream
+    return int(N.lib().rbg_trace_status(manager._ensure_scene().handle, C.c_void_p(st_ptr)))
+
+
 def autotune(manager, rays, res=None, stream=None) -> int:
     """Pick the mixed tracer's block size and compaction threshold for this
     scene from a timed trace of `rays` per candidate (rbg_scene_autotune);

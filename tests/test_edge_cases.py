@@ -204,3 +204,38 @@ def test_autotune_picks_a_candidate_and_keeps_results():
     st, after = _trace(man, batch, N.PREC_MIXED)
     assert st == N.RBG_OK
     _same(after, ref)
+
+
+def test_trace_async_in_a_cuda_graph():
+    """rbg_trace_async puts the whole trace (take-up order and persistent
+    tracer) on the stream without reading anything back, so a CUDA graph
+    captures it; replays give rbg_trace's results, and rbg_trace_status
+    reads the status afterwards."""
+    import torch
+
+    from robast_gb300 import device
+
+    man, batch = configs.schwarzschild_couder(n_rays=60000, seed=9)
+    n = len(batch["x"])
+    rays = device.to_device(batch, "cuda:0")
+    device.reserve(man, n)
+    ref, st = device.trace(man, rays, precision=N.PREC_MIXED)
+    assert st == N.RBG_OK
+    ref = {k: ref[k].cpu().numpy() for k in FIELDS}
+    res = device.alloc_result(n, "cuda:0")
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):  # warm-up on the capture stream
+        device.trace_async(man, rays, res, precision=N.PREC_MIXED, stream=side)
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side):
+        device.trace_async(man, rays, res, precision=N.PREC_MIXED, stream=side)
+    for _ in range(2):
+        for v in res.values():
+            v.fill_(7)
+        graph.replay()
+        torch.cuda.synchronize()
+        assert device.status(man) == N.RBG_OK
+        _same({k: res[k].cpu().numpy() for k in FIELDS}, ref)
