@@ -627,8 +627,9 @@ def run_kernels(args):
     command of the ncu captures under profiles/): the Schwarzschild-Couder
     batch traced by both tracers (with the take-up order's kernels), the
     adjoint of its RMS spot, the focal-plane moments, histogram and
-    ContainmentRadius, and a device ray source.  Prints a one-line
-    summary; no timing."""
+    ContainmentRadius, and a device ray source; with --workload another
+    configuration, traced by its mixed-tracer instance and the FP64 tracer.
+    Prints a one-line summary; no timing."""
     import torch
 
     from robast_gb300 import _native as N
@@ -636,6 +637,19 @@ def run_kernels(args):
     from robast_gb300 import build, configs, device
 
     build.build_library()
+    if args.workload != "schwarzschild_couder":
+        # another scene class: its mixed-tracer instance and the FP64 tracer
+        man, batch = build_workload(args.workload, args.rays or 1_000_000)
+        rays = device.to_device(batch)
+        res = device.alloc_result(len(batch["x"]))
+        device.reserve(man, len(batch["x"]))
+        for _ in range(max(1, args.warmup)):
+            device.trace(man, rays, res, precision=N.PREC_MIXED)
+        device.trace(man, rays, res, precision=N.PREC_FP64)
+        torch.cuda.synchronize()
+        print(json.dumps({"kernels": "ok", "workload": args.workload, "rays": len(batch["x"]),
+                          "focused": int((res["status"] == N.RBG_FOCUS).sum().item())}))
+        return
     n = args.rays or 3_000_000
     _, batch = configs.schwarzschild_couder(n_rays=n)
     rays = device.to_device(batch)
