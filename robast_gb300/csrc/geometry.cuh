@@ -1421,7 +1421,7 @@ RBG_D bool asph_newton_f(const float* Pf, int n, const LRay& L, float& t_out, fl
 // until |step| < 1e-10 (the reference's stopping rule), or after a first
 // step that the FP32 root leaves small (below).  Returns false when it does
 // not converge in 8 steps or leaves the conic's domain.
-RBG_D bool asph_polish(const double* P, int n, const LRay& L, double sc, double& t) {
+RBG_D bool asph_polish(const double* P, int n, const LRay& L, double sc, double& t, bool fast = true) {
   const int s1 = n == 1;
   const int npol1 = (int)P[RBG_ASPH_NPOL1];
   const int npol = s1 ? npol1 : (int)P[RBG_ASPH_NPOL2];
@@ -1444,11 +1444,12 @@ RBG_D bool asph_polish(const double* P, int n, const LRay& L, double sc, double&
     t += e;
     if (fabs(e) < 1e-10) return true;
     // A first step below 1e-3 cm at a slope that is not grazing leaves t
-    // within (slope error) x |e| of the root: ~1e-13 cm at near-normal
-    // incidence, up to 5e-8 cm for rays meeting a curved face at ~56 deg
-    // (the FP32 slope then off by ~5e-5).  Stopping there saves the
-    // evaluation that would only confirm it.
-    if (it == 0 && fabs(e) < 1e-3 && fabs(sc) < 10) return true;
+    // within (the slope's relative error) x |e| of the root, ~1e-13 cm with
+    // the face's own FP32 slope.  Stopping there saves the evaluation that
+    // would only confirm it.  (A twin face polished with the other face's
+    // slope is not `fast`: across a 1 mm shell met at 56 deg that slope is
+    // ~1 % off.)
+    if (fast && it == 0 && fabs(e) < 1e-3 && fabs(sc) < 10) return true;
   }
   return false;
 }
@@ -1484,7 +1485,7 @@ RBG_D void asph_faces_f(const double* P, const float* Pf, const LRay& L, bool tw
   bool ok2;
   if (twin && ok1) {
     t2 = t1 + sc * (P[RBG_ASPH_Z2] - P[RBG_ASPH_Z1]);
-    ok2 = asph_polish(P, 2, L, sc, t2);
+    ok2 = asph_polish(P, 2, L, sc, t2, false);
   } else {
     ok2 = asph_newton_f(Pf, 2, L, tf, sf);
     if (ok2) {

@@ -130,10 +130,7 @@ def test_device_history_tail_is_defined(precision):
     ost, ref = oracle_ref.trace(man, configs.to_array(batch), threads=8, history=cap)
     assert ost == 0
     np.testing.assert_array_equal(hn, ref["hist_node"].reshape(n, cap))
-    # the FP64 tracer to rounding; the mixed tracer to the parity tolerance
-    # (its one-step polish leaves oblique focal-surface hits up to 5e-8 cm off)
-    tol = 1e-9 if precision == "fp64" else 1e-6
-    np.testing.assert_allclose(hx, ref["hist_xyzt"].reshape(n, cap, 4), rtol=tol, atol=tol)
+    np.testing.assert_allclose(hx, ref["hist_xyzt"].reshape(n, cap, 4), rtol=1e-9, atol=1e-9)
 
 
 @pytest.mark.gpu
