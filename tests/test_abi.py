@@ -164,3 +164,40 @@ def test_boolean_expression_parser():
     left = comp.left
     assert left.op == N.OP_UNION and left.left is a and left.left_matrix is t
     assert left.right.op == N.OP_INTERSECTION
+
+
+def test_scene_tuning_set_and_read_back():
+    """rbg_scene_set_tuning validates its arguments and rbg_scene_tuning
+    reports the tuning (host state only: no device needed)."""
+    from robast_gb300 import configs
+
+    man, _ = configs.schwarzschild_couder(n_rays=5)
+    h = man.scene.handle
+    L = N.lib()
+    b, c = C.c_int32(0), C.c_int32(0)
+    assert L.rbg_scene_tuning(h, C.byref(b), C.byref(c)) == N.RBG_OK
+    assert (b.value, c.value) == (256, 32)  # the lean instance's defaults
+    assert L.rbg_scene_set_tuning(h, 128, 8) == N.RBG_OK
+    assert L.rbg_scene_tuning(h, C.byref(b), None) == N.RBG_OK and b.value == 128
+    assert L.rbg_scene_tuning(h, None, C.byref(c)) == N.RBG_OK and c.value == 8
+    for bad in ((64, 8), (512, 8), (128, 33), (128, -1)):
+        assert L.rbg_scene_set_tuning(h, *bad) == N.RBG_ERR_ARG
+    assert L.rbg_scene_set_tuning(None, 0, 0) == N.RBG_ERR_ARG
+    # another scene class runs at its instance's own block size
+    man2, _ = configs.davies_cotton(n_rays=5)
+    assert L.rbg_scene_tuning(man2.scene.handle, C.byref(b), C.byref(c)) == N.RBG_OK
+    assert b.value == 256 and c.value == 32
+
+
+def test_trace_async_needs_the_scene_on_the_device():
+    """rbg_trace_async never uploads (an upload allocates and copies, which
+    a graph capture cannot hold): a scene not yet on a device is an argument
+    error, and so is reading the status of a scene that never traced."""
+    from robast_gb300 import configs
+
+    man, _ = configs.paraboloid(n_rays=5)
+    L = N.lib()
+    rays, res, opts = N.Rays(), N.Result(), man.trace_options()
+    assert L.rbg_trace_async(man.scene.handle, C.byref(rays), C.byref(res), C.byref(opts), None) == N.RBG_ERR_ARG
+    assert L.rbg_trace_status(man.scene.handle, None) == N.RBG_ERR_ARG
+    assert L.rbg_trace_status(None, None) == N.RBG_ERR_ARG
